@@ -1,0 +1,381 @@
+"""Benchmark: beta^2 frequency-points/s of the batched cheerleader solve.
+
+Workload (one "step"): one 20-disk booster request -- cheerleader, 128x128
+grid over 1 m, eps 24, 1 mm disks, gaps U(7.5, 8.5) mm, per-disk tilts
+U(-0.5, 0.5) mrad, 256 frequencies 19.5-20.5 GHz solved as one batch, 401
+bounce iterations (nmax = 400), complex64 fields with FP64 phase arguments and
+FP64 exit accumulation.  Seeded synthetic geometry (no dataset exists).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Under torchrun every rank solves its own
+request (weak scaling, no collective on the data path).
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "boostfractor.jl_gb300")
+for _p in (REPO, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "beta2 freq-points/s (cheerleader, 20 disks, 128x128, 256 freqs, 401 bounces; <=1e-4 rel err vs FP64)"
+UNIT = "freq-points/s"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload(rank=0, **over):
+    from bfgb300 import workloads as W
+    w = W.config2_cheerleader(seed=2 + rank, **over)
+    return w
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle (numpy) on a bounded sample
+# --------------------------------------------------------------------------
+def _cpu_worker(args):
+    w, f, nmax_s = args
+    sys.path.insert(0, REPO)
+    from oracle import bf_oracle as O  # the CPU baseline leg may run the oracle
+    co = O.seed_coordinate_system(X=w["X"], Y=w["Y"])
+    sb = O.seed_setup_boundaries(co, diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"],
+                                 epsilon=w["eps"], relative_tilt_x=w["relative_tilt_x"],
+                                 relative_tilt_y=w["relative_tilt_y"])
+    t = time.perf_counter()
+    E = O.cheerleader(0, nmax_s, sb, co, f=f, diskR=w["diskR"])
+    dt = time.perf_counter() - t
+    return dt, float(np.sum(np.abs(E) ** 2))
+
+
+def cpu_baseline(w, nmax_s=60, workers=None):
+    """Time the oracle on `workers` host cores, one frequency each, nmax_s+1 bounces;
+    extrapolate linearly in propagations to the full request."""
+    P = workers or os.cpu_count() or 1
+    freqs = w["freqs"][np.linspace(0, len(w["freqs"]) - 1, P).astype(int)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(P) as pool:
+        res = pool.map(_cpu_worker, [(w, float(f), nmax_s) for f in freqs])
+    wall = time.perf_counter() - t0
+    nd = len(w["distance"])
+    props = lambda nm: (nd - 2) + (nm + 1) * 2 * (nd - 2)
+    scale = props(w["nmax"]) / props(nmax_s)
+    per_point = max(r[0] for r in res) * scale
+    value = P / per_point
+    return dict(value=value, unit=UNIT, cores=P, kind="port",
+                sample=f"FP64 numpy oracle, {P} frequencies x {nmax_s + 1} of {w['nmax'] + 1} bounces "
+                       f"({P} spawned processes, one per core), extrapolated x{scale:.2f} in propagations; "
+                       f"pool wall {wall:.1f}s")
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per propagation of the fused stage kernel from the committed ncu summary."""
+    p = os.path.join(REPO, "profiles", "fused_stage_ncu.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["dram_bytes_per_propagation"])
+        except Exception:
+            return None
+    return None
+
+
+# --------------------------------------------------------------------------
+# our implementation
+# --------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+
+    over = {}
+    if args.nf:
+        over["nf"] = args.nf
+    if args.nmax is not None:
+        over["nmax"] = args.nmax
+    w = workload(rank, **over)
+    nf, nmax = len(w["freqs"]), w["nmax"]
+    h = B.Handle(dev)
+    stream = torch.cuda.current_stream()
+    h.set_stream(stream.cuda_stream)
+    c = B.SeedCoordinateSystem(X=w["X"], Y=w["Y"])
+    sb = B.SeedSetupBoundaries(c, diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"],
+                               epsilon=w["eps"], relative_tilt_x=w["relative_tilt_x"],
+                               relative_tilt_y=w["relative_tilt_y"])
+    st = B.Stack(sb, c, w["diskR"], handle=h)
+    npix = len(w["X"]) * len(w["Y"])
+    out_right = torch.empty((nf, npix * 2), dtype=torch.float64, device="cuda")
+    out_beta2 = torch.empty((nf,), dtype=torch.float64, device="cuda")
+
+    def step():
+        st.cheerleader_device(w["freqs"], out_right.data_ptr(), out_beta2.data_ptr(), nmax=nmax,
+                              precision="mixed")
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+
+    # accuracy of the mixed path vs the FP64 GPU path on a subset of frequencies
+    sub = np.unique(np.linspace(0, nf - 1, min(nf, 16)).astype(int))
+    b_mixed = out_beta2.cpu().numpy()[sub]
+    _, _, b_fp64 = st.cheerleader(w["freqs"][sub], nmax=nmax, precision="fp64")
+    errs = np.abs(b_mixed - b_fp64) / np.abs(b_fp64)
+    rel_err = float(np.max(errs))
+    rel_err_med = float(np.median(errs))
+    # the plain FP64 single-stack path (one frequency per solve)
+    t0 = time.perf_counter()
+    st.cheerleader(w["freqs"][:1], nmax=nmax, precision="fp64")
+    torch.cuda.synchronize()
+    fp64_single = 1.0 / (time.perf_counter() - t0)
+
+    # ---- timed region
+    h.set_profiling(True)
+    clocks = ClockSampler(dev if ws == 1 else local)
+    clocks.start()
+    time.sleep(0.4)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stage_ms, launches, stage_launches, props = 0.0, 0, 0, 0
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        p = h.last_profile()
+        stage_ms += p["stages_ms"]
+        launches += int(p["launches"])
+        stage_launches += int(p["stage_launches"])
+        props += int(p["propagations"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    ms_total = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    h.set_profiling(False)
+    if ws > 1:
+        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = nf * ws / (ms_step / 1000.0)
+
+    # roofline of the fused stage kernel (bytes per propagation: read + write of
+    # the complex64 field, 2*N^2*8)
+    N = len(w["X"])
+    alg_bytes_per_prop = 2 * N * N * 8
+    achieved = alg_bytes_per_prop * props / (stage_ms / 1000.0) / 1e9
+    peak, peak_kind = measured_peaks()
+    tr = ncu_traffic()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "traffic": None if tr is None else tr * props / stage_launches,
+            "kernel": "k_fused_stage", "launch_avg_ms": stage_ms / max(stage_launches, 1),
+            "alg_bytes_per_launch": alg_bytes_per_prop * props / max(stage_launches, 1),
+            "fft_gflops": props * (2 * N + 2 * 38) * 5 * N * math.log2(N) / (stage_ms / 1000.0) / 1e9}
+
+    # ---- end to end through the one-shot C ABI call with host buffers
+    import ctypes
+    from bfgb300 import _lib
+    L = _lib.lib()
+    r = B.workloads.fresnel_r(w["eps"])
+    host_in = dict(distance=np.ascontiguousarray(w["distance"]), r=np.ascontiguousarray(r),
+                   eps=np.ascontiguousarray(w["eps"]), tx=np.ascontiguousarray(w["relative_tilt_x"]),
+                   ty=np.ascontiguousarray(w["relative_tilt_y"]), X=c.X, Y=c.Y, kX=c.kX, kY=c.kY,
+                   freqs=np.ascontiguousarray(w["freqs"]))
+    pin = {k: torch.from_numpy(v.view(np.float64) if v.dtype == np.complex128 else v).pin_memory()
+           for k, v in host_in.items()}
+    out_host = torch.empty((nf, npix * 2), dtype=torch.float64).pin_memory()
+    b2_host = torch.empty((nf,), dtype=torch.float64).pin_memory()
+    P = lambda t: ctypes.cast(ctypes.c_void_p(t.data_ptr()), ctypes.POINTER(ctypes.c_double))
+    scale = st.beta2_scale()
+
+    def e2e_step():
+        h.check(L.bf_cheerleader(h.ptr, len(w["distance"]), P(pin["distance"]), P(pin["r"]), P(pin["eps"]),
+                                 P(pin["tx"]), P(pin["ty"]), None, len(c.X), len(c.Y), P(pin["X"]),
+                                 P(pin["Y"]), P(pin["kX"]), P(pin["kY"]), w["diskR"], nf, P(pin["freqs"]),
+                                 0.0, nmax, _lib.BF_PROP_3D, _lib.BF_PREC_MIXED, None, None, 0, scale,
+                                 P(out_host), None, P(b2_host)))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    ke = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / ke
+    h2d = int(sum(t.numel() * t.element_size() for t in pin.values()))
+    d2h = int(out_host.numel() * 8 + b2_host.numel() * 8)
+    b2_e2e = b2_host.numpy().copy()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (fields, FFTs), f64 (phase kz*dz, exit accumulation)",
+        "data": "synthetic (seeded geometry, no dataset)",
+        "config": {"workload": w["name"] + f"-{nf}f-{nmax + 1}bounces", "grid": N,
+                   "disks": (len(w["distance"]) - 2) // 2, "freqs": nf, "bounces": nmax + 1,
+                   "precision": "mixed", "per_gpu_request": "one 256-frequency request per GPU",
+                   "l2": "no flush: per-step working set (phasor tables + fields) > L2"},
+        "beta2_rel_err_vs_fp64": rel_err,
+        "beta2_rel_err_vs_fp64_median": rel_err_med,
+        "beta2_checked_freqs": int(len(sub)),
+        "plain_fp64_single_freqpts_per_s": fp64_single,
+        "gpu_launches": launches,
+        "roofline": roof,
+        "e2e": {"value": nf / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": "bf_cheerleader (one-shot C ABI, pinned host buffers; stack upload, tables, solve, D2H)"},
+        "clocks": clk,
+    }
+    if ws == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(w, nmax_s=args.cpu_nmax)
+    assert np.all(np.isfinite(b2_e2e))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    st.close()
+    h.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    over = {}
+    if args.nf:
+        over["nf"] = args.nf
+    if args.nmax is not None:
+        over["nmax"] = args.nmax
+    w = workload(0, **over)
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(w, nmax_s=2)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cb = cpu_baseline(w, nmax_s=args.cpu_nmax)
+        vals.append(cb["value"])
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    cb["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * len(w["freqs"]) / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 oracle)",
+            "data": "synthetic (seeded geometry, no dataset)",
+            "config": {"workload": w["name"] + f"-{len(w['freqs'])}f-{w['nmax'] + 1}bounces"},
+            "impl": "reference", "cpu_baseline": cb,
+            "reference_note": "the reference is Julia (not installed); its algorithm runs as the FP64 numpy "
+                              "restatement pinned to the reference's golden vectors",
+            "wall_s": wall,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nf", type=int, default=0, help="override frequency count (testing only)")
+    ap.add_argument("--nmax", type=int, default=None, help="override nmax (testing only)")
+    ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

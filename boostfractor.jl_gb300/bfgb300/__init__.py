@@ -1,0 +1,403 @@
+"""Python mirror of BoostFractor.jl's public API on the GB300 C ABI.
+
+Same names, keyword arguments and array semantics as the reference module
+(src/BoostFractor.jl:5-20): ``SeedCoordinateSystem``, ``SeedSetupBoundaries``,
+``propagator`` & co. (the ``prop=`` plug-ins), ``cheerleader``, ``dancer``.
+Arrays follow the reference's index order with 0-based numpy indexing
+(``E[x, y]``, ``relative_surfaces[region, x, y]``, ``emit[region, dir, x, y]``);
+they are handed to the C ABI in Julia's column-major memory layout.
+
+Extensions over the reference signatures (all keyword-only, with defaults that
+keep the reference behaviour):
+  * ``f`` may be an array: the frequencies are solved as one batch and the
+    outputs gain a leading frequency axis;
+  * ``precision``: ``"fp64"`` (default, complex128 everywhere) or ``"mixed"``
+    (complex64 fields, FP64 phase arguments and exit accumulation);
+  * ``handle``: a :class:`Handle` (one per host thread; a default one is made).
+"""
+import math
+import threading
+
+import numpy as np
+
+from . import _lib
+from ._lib import BFError
+
+__all__ = [
+    "CoordinateSystem", "SeedCoordinateSystem", "SetupBoundaries", "SeedSetupBoundaries",
+    "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
+    "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
+]
+
+SPEED_OF_LIGHT = 299792458.0
+
+
+def wavelength(frequency):
+    """src/boost_fractor.jl:16-19."""
+    return SPEED_OF_LIGHT / frequency
+
+
+# --------------------------------------------------------------------------
+# handle
+# --------------------------------------------------------------------------
+class Handle:
+    """One CUDA stream + device allocations (bf_create / bf_destroy)."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        L = _lib.lib()
+        h = _lib._vp()
+        rc = L.bf_create(int(device), int(hbm_budget_bytes), _lib.ctypes.byref(h))
+        if rc != _lib.BF_OK:
+            raise BFError(rc, "bf_create failed (no usable CUDA device?)")
+        self._h = h
+        self.device = device
+
+    @property
+    def ptr(self):
+        return self._h
+
+    def check(self, rc):
+        if rc != _lib.BF_OK:
+            msg = _lib.lib().bf_last_error(self._h)
+            raise BFError(rc, msg.decode() if msg else "")
+
+    def device_bytes(self):
+        return int(_lib.lib().bf_device_bytes(self._h))
+
+    def set_stream(self, cuda_stream_ptr):
+        """Run on a caller's cudaStream_t (integer handle; 0 = the handle's own stream)."""
+        self.check(_lib.lib().bf_set_stream(self._h, _lib._vp(int(cuda_stream_ptr) or None)))
+
+    def set_profiling(self, enable=True):
+        self.check(_lib.lib().bf_set_profiling(self._h, int(bool(enable))))
+
+    def last_profile(self):
+        """dict of the last solve's device profile (see bf_last_profile)."""
+        out = np.zeros(8)
+        self.check(_lib.lib().bf_last_profile(self._h, _lib.ptr(out)))
+        keys = ["solve_ms", "stages_ms", "tables_ms", "exits_ms", "stage_launches", "launches",
+                "propagations", "nfreq"]
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if self._h:
+            _lib.lib().bf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tls = threading.local()
+
+
+def default_handle():
+    h = getattr(_tls, "handle", None)
+    if h is None:
+        h = Handle(0)
+        _tls.handle = h
+    return h
+
+
+# --------------------------------------------------------------------------
+# geometry (src/boost_fractor.jl:16-108)
+# --------------------------------------------------------------------------
+class CoordinateSystem:
+    """src/boost_fractor.jl:21-28."""
+
+    def __init__(self, X, Y, kX, kY):
+        self.X = np.ascontiguousarray(X, dtype=np.float64)
+        self.Y = np.ascontiguousarray(Y, dtype=np.float64)
+        self.kX = np.ascontiguousarray(kX, dtype=np.float64)
+        self.kY = np.ascontiguousarray(kY, dtype=np.float64)
+
+
+def get_kspace_coords(real_coords):
+    """src/boost_fractor.jl:42-47 (evaluated by the C ABI's host helper)."""
+    x = np.ascontiguousarray(real_coords, dtype=np.float64)
+    out = np.empty_like(x)
+    rc = _lib.lib().bf_get_kspace_coords(len(x), _lib.ptr(x), _lib.ptr(out))
+    if rc != _lib.BF_OK:
+        raise BFError(rc, "get_kspace_coords")
+    return out
+
+
+def SeedCoordinateSystem(X=None, Y=None):
+    """src/boost_fractor.jl:30-34; default X = Y = -0.5:0.01:0.5."""
+    if X is None:
+        X = np.array([i / 100 for i in range(-50, 51)])
+    if Y is None:
+        Y = np.array([i / 100 for i in range(-50, 51)])
+    X = np.asarray(X, dtype=np.float64)
+    Y = np.asarray(Y, dtype=np.float64)
+    return CoordinateSystem(X, Y, get_kspace_coords(X), get_kspace_coords(Y))
+
+
+class SetupBoundaries:
+    """src/boost_fractor.jl:63-71."""
+
+    def __init__(self, distance, r, eps, relative_tilt_x, relative_tilt_y, relative_surfaces):
+        self.distance = np.array(distance, dtype=np.float64)
+        self.r = np.array(r, dtype=np.complex128)
+        self.eps = np.array(eps, dtype=np.complex128)
+        self.relative_tilt_x = np.array(relative_tilt_x, dtype=np.float64)
+        self.relative_tilt_y = np.array(relative_tilt_y, dtype=np.float64)
+        self.relative_surfaces = np.array(relative_surfaces, dtype=np.complex128)
+
+
+def _eps_cast(eps):
+    eps = np.array(eps, dtype=np.complex128)
+    eps.imag[eps.imag == 0.0] = -0.0
+    return eps
+
+
+def SeedSetupBoundaries(coords, diskno=3, distance=None, epsilon=None, relative_tilt_x=None,
+                        relative_tilt_y=None, relative_surfaces=None):
+    """src/boost_fractor.jl:83-108 (defaults, Fresnel r, dimension check)."""
+    nd0 = 2 * diskno + 2
+    if relative_tilt_x is None:
+        relative_tilt_x = np.zeros(nd0)
+    if relative_tilt_y is None:
+        relative_tilt_y = np.zeros(nd0)
+    if relative_surfaces is None:
+        relative_surfaces = np.zeros((nd0, len(coords.X), len(coords.Y)))
+    if distance is None:
+        distance = [0.0] + [8e-3 if x % 2 == 1 else 1e-3 for x in range(1, 2 * diskno + 1)] + [0.0]
+    if epsilon is None:
+        epsilon = [np.nan] + [1.0 if x % 2 == 1 else 9.0 for x in range(1, 2 * diskno + 1)] + [1.0]
+    eps = _eps_cast(epsilon)
+    r = np.zeros(len(eps) - 1, dtype=np.complex128)
+    if len(eps) >= 2:
+        e = np.ascontiguousarray(eps)
+        rc = _lib.lib().bf_fresnel_reflectivities(len(e), _lib.ptr(e.view(np.float64)),
+                                                  _lib.ptr(r.view(np.float64)))
+        if rc != _lib.BF_OK:
+            raise BFError(rc, "fresnel")
+    relative_surfaces = np.asarray(relative_surfaces)
+    if not (len(distance) == len(r) + 1 == len(eps) == len(relative_tilt_x) == len(relative_tilt_y)
+            == relative_surfaces.shape[0]):
+        raise ValueError("DimensionMismatch: the arrays in your SetupBoundaries objects don't fit together!")
+    return SetupBoundaries(distance, r, eps, relative_tilt_x, relative_tilt_y, relative_surfaces)
+
+
+# --------------------------------------------------------------------------
+# propagators: the prop= plug-ins (src/boost_fractor.jl:137-227)
+# --------------------------------------------------------------------------
+_PREC = {"fp64": _lib.BF_PREC_FP64, "mixed": _lib.BF_PREC_MIXED}
+
+
+def _prec(p):
+    if isinstance(p, int):
+        return p
+    return _PREC[p]
+
+
+class _Propagator:
+    def __init__(self, kind, name):
+        self.kind = kind
+        self.__name__ = name
+
+    def __call__(self, E0, dz, diskR, eps, tilt_x, tilt_y, surface, lam, coords, precision="fp64",
+                 handle=None):
+        h = handle or default_handle()
+        E = np.asfortranarray(np.array(E0, dtype=np.complex128))
+        nx, ny = E.shape
+        surf = None
+        if surface is not None:
+            s = np.asarray(surface)
+            if np.any(s != 0):
+                surf = np.asfortranarray(np.broadcast_to(s, (nx, ny)).astype(np.complex128))
+        eps = complex(eps)
+        h.check(_lib.lib().bf_propagate(
+            h.ptr, self.kind, _prec(precision), _lib.ptr(_fbuf(E)), nx, ny,
+            _lib.ptr(coords.X), _lib.ptr(coords.Y), _lib.ptr(coords.kX), _lib.ptr(coords.kY),
+            float(dz), float(diskR), eps.real, eps.imag, float(tilt_x), float(tilt_y),
+            _lib.ptr(None if surf is None else _fbuf(surf)), float(lam)))
+        return E
+
+    def __repr__(self):
+        return self.__name__
+
+
+def _fbuf(a):
+    """float64 view (shared memory) of an F-contiguous complex array, in Julia memory order."""
+    assert a.flags.f_contiguous
+    return a.T.view(np.float64).reshape(-1)
+
+
+propagator = _Propagator(_lib.BF_PROP_3D, "propagator")
+propagatorNoTilts = _Propagator(_lib.BF_PROP_NOTILTS, "propagatorNoTilts")
+propagatorMomentumSpace = _Propagator(_lib.BF_PROP_MOMENTUM, "propagatorMomentumSpace")
+propagator1D = _Propagator(_lib.BF_PROP_1D, "propagator1D")
+
+
+def _prop_kind(prop):
+    if isinstance(prop, _Propagator):
+        return prop.kind
+    if isinstance(prop, int):
+        return prop
+    raise ValueError("prop must be one of propagator, propagatorNoTilts, propagatorMomentumSpace, "
+                     "propagator1D (a custom Python propagator cannot run on the GPU path)")
+
+
+# --------------------------------------------------------------------------
+# resident stacks and the solvers
+# --------------------------------------------------------------------------
+def _fcplx(a, shape):
+    """complex128 array in Julia column-major layout, as a float64 buffer."""
+    a = np.asfortranarray(np.broadcast_to(np.asarray(a, dtype=np.complex128), shape))
+    return a, _fbuf(a)
+
+
+class Stack:
+    """A SetupBoundaries + CoordinateSystem resident on the device (bf_stack_create)."""
+
+    def __init__(self, bdry, coords, diskR, handle=None):
+        self.h = handle or default_handle()
+        self.coords = coords
+        self.diskR = float(diskR)
+        nd = len(bdry.distance)
+        nx, ny = len(coords.X), len(coords.Y)
+        self.nd, self.nx, self.ny = nd, nx, ny
+        self._keep = []
+        dist = np.ascontiguousarray(bdry.distance, dtype=np.float64)
+        r = np.ascontiguousarray(bdry.r, dtype=np.complex128)
+        eps = np.ascontiguousarray(bdry.eps, dtype=np.complex128)
+        tx = np.ascontiguousarray(bdry.relative_tilt_x, dtype=np.float64)
+        ty = np.ascontiguousarray(bdry.relative_tilt_y, dtype=np.float64)
+        surf = np.asarray(bdry.relative_surfaces)
+        sbuf = None
+        if surf is not None and surf.size and np.any(surf != 0):
+            sarr, sbuf = _fcplx(surf, (nd, nx, ny))
+            self._keep.append(sarr)
+        s = _lib._vp()
+        self.h.check(_lib.lib().bf_stack_create(
+            self.h.ptr, nd, _lib.ptr(dist), _lib.ptr(r.view(np.float64)), _lib.ptr(eps.view(np.float64)),
+            _lib.ptr(tx), _lib.ptr(ty), _lib.ptr(sbuf), nx, ny, _lib.ptr(coords.X), _lib.ptr(coords.Y),
+            _lib.ptr(coords.kX), _lib.ptr(coords.kY), self.diskR, _lib.ctypes.byref(s)))
+        self._s = s
+
+    def set_distance(self, distance):
+        d = np.ascontiguousarray(distance, dtype=np.float64)
+        self.h.check(_lib.lib().bf_stack_set_distance(self.h.ptr, self._s, _lib.ptr(d)))
+
+    def beta2_scale(self):
+        X, Y = self.coords.X, self.coords.Y
+        dx = X[1] - X[0] if len(X) > 1 else 1.0
+        dy = Y[1] - Y[0] if len(Y) > 1 else 1.0
+        return dx * dy / (math.pi * self.diskR ** 2)
+
+    def cheerleader(self, freqs, amin=0.0, nmax=100, prop=None, emit=None, reflect=None,
+                    returnboth=False, precision="fp64", beta2_scale=None, out_device=None):
+        """Batched cheerleader; returns (right[nf, nx, ny], left or None, beta2[nf])."""
+        freqs = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+        nf = len(freqs)
+        nx, ny, nd = self.nx, self.ny, self.nd
+        kind = _prop_kind(prop or propagator)
+        ebuf = rbuf = None
+        if emit is not None:
+            earr, ebuf = _fcplx(emit, (nd, 2, nx, ny))
+        if reflect is not None:
+            rarr, rbuf = _fcplx(reflect, (nx, ny))
+        right = np.empty((nf, ny, nx), dtype=np.complex128)
+        left = np.empty((nf, ny, nx), dtype=np.complex128) if returnboth else None
+        beta2 = np.empty(nf, dtype=np.float64)
+        scale = self.beta2_scale() if beta2_scale is None else beta2_scale
+        self.h.check(_lib.lib().bf_stack_cheerleader(
+            self.h.ptr, self._s, nf, _lib.ptr(freqs), float(amin), int(nmax), kind, _prec(precision),
+            _lib.ptr(ebuf), _lib.ptr(rbuf), int(bool(returnboth)), float(scale), 0,
+            _lib.ptr(right.view(np.float64)), _lib.ptr(None if left is None else left.view(np.float64)),
+            _lib.ptr(beta2)))
+        return right.transpose(0, 2, 1), (None if left is None else left.transpose(0, 2, 1)), beta2
+
+    def cheerleader_device(self, freqs, out_right_ptr, out_beta2_ptr, nmax=100, prop=None,
+                           precision="mixed", out_left_ptr=None, beta2_scale=None):
+        """Batched cheerleader with outputs left in device memory (raw device pointers:
+        out_right [nf][ny][nx] complex128, out_beta2 [nf] float64)."""
+        freqs = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+        scale = self.beta2_scale() if beta2_scale is None else beta2_scale
+        P = _lib.ctypes.POINTER(_lib.ctypes.c_double)
+        cast = lambda v: None if v is None else _lib.ctypes.cast(_lib.ctypes.c_void_p(int(v)), P)
+        self.h.check(_lib.lib().bf_stack_cheerleader(
+            self.h.ptr, self._s, len(freqs), _lib.ptr(freqs), 0.0, int(nmax),
+            _prop_kind(prop or propagator), _prec(precision), None, None,
+            int(out_left_ptr is not None), float(scale), _lib.BF_OUT_DEVICE,
+            cast(out_right_ptr), cast(out_left_ptr), cast(out_beta2_ptr)))
+
+    def dancer(self, freqs, amin=0.0, nmax=200, prop=None, emit=None, reflect=None, returnsum=True,
+               immediatesum=True, precision="fp64", beta2_scale=None):
+        """Batched dancer; returns (Eout, beta2[nf]); Eout is [nf, nx, ny] or [nf, nx, ny, nmax+1]."""
+        freqs = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+        nf = len(freqs)
+        nx, ny, nd = self.nx, self.ny, self.nd
+        kind = _prop_kind(prop or propagator)
+        ebuf = rbuf = None
+        if emit is not None:
+            earr, ebuf = _fcplx(emit, (nd - 1, 2, nx, ny))
+        if reflect is not None:
+            rarr, rbuf = _fcplx(reflect, (nx, ny))
+        if returnsum or immediatesum:
+            out = np.empty((nf, ny, nx), dtype=np.complex128)
+        else:
+            out = np.empty((nf, nmax + 1, ny, nx), dtype=np.complex128)
+        beta2 = np.empty(nf, dtype=np.float64)
+        scale = self.beta2_scale() if beta2_scale is None else beta2_scale
+        self.h.check(_lib.lib().bf_stack_dancer(
+            self.h.ptr, self._s, nf, _lib.ptr(freqs), float(amin), int(nmax), kind, _prec(precision),
+            _lib.ptr(ebuf), _lib.ptr(rbuf), int(bool(returnsum)), int(bool(immediatesum)), float(scale), 0,
+            _lib.ptr(out.view(np.float64)), _lib.ptr(beta2)))
+        if out.ndim == 3:
+            return out.transpose(0, 2, 1), beta2
+        return out.transpose(0, 3, 2, 1), beta2
+
+    def close(self):
+        if getattr(self, "_s", None):
+            _lib.lib().bf_stack_destroy(self.h.ptr, self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _maybe_scalar(f, arr):
+    return arr[0] if np.ndim(f) == 0 else arr
+
+
+def cheerleader(amin, nmax, bdry, coords, f=10.0e9, prop=propagator, emit=None, reflect=None,
+                diskR=0.1, returnboth=False, precision="fp64", handle=None):
+    """src/boost_fractor_recurprop.jl:226-363 on the GPU."""
+    st = Stack(bdry, coords, diskR, handle=handle)
+    try:
+        right, left, _ = st.cheerleader(f, amin=amin, nmax=nmax, prop=prop, emit=emit, reflect=reflect,
+                                        returnboth=returnboth, precision=precision)
+    finally:
+        st.close()
+    if returnboth:
+        return _maybe_scalar(f, left), _maybe_scalar(f, right)
+    return _maybe_scalar(f, right)
+
+
+def dancer(amin, nmax, sbdry, coords, f=10.0e9, prop=propagator, emit=None, reflect=None, diskR=0.1,
+           returnsum=True, immediatesum=True, precision="fp64", handle=None):
+    """src/boost_fractor_recurprop.jl:25-146 on the GPU."""
+    st = Stack(sbdry, coords, diskR, handle=handle)
+    try:
+        out, _ = st.dancer(f, amin=amin, nmax=nmax, prop=prop, emit=emit, reflect=reflect,
+                           returnsum=returnsum, immediatesum=immediatesum, precision=precision)
+    finally:
+        st.close()
+    return _maybe_scalar(f, out)
+
+
+def boost_factor(E, coords, diskR):
+    """beta^2 = sum|E|^2 dx dy / (pi diskR^2) (test/runtests.jl:74)."""
+    X, Y = coords.X, coords.Y
+    dx = X[1] - X[0] if len(X) > 1 else 1.0
+    dy = Y[1] - Y[0] if len(Y) > 1 else 1.0
+    return float(np.sum(np.abs(E) ** 2) * dx * dy / (math.pi * diskR ** 2))

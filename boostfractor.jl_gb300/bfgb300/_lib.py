@@ -1,0 +1,101 @@
+"""ctypes binding of libbfgb300.so (the C ABI in include/boostfractor_gb300.h).
+
+The library is built in-tree by ``boostfractor.jl_gb300/build.py``.  Loading
+fails loudly when it is missing: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+LIB_PATH = os.path.join(PKG, "lib", "libbfgb300.so")
+
+BF_OK = 0
+BF_ERR_INVALID = 1
+BF_ERR_NOMEM = 2
+BF_ERR_CUDA = 3
+BF_ERR_TIMEOUT = 4
+BF_ERR_UNSUPPORTED = 5
+
+BF_PROP_3D = 0
+BF_PROP_NOTILTS = 1
+BF_PROP_MOMENTUM = 2
+BF_PROP_1D = 3
+
+BF_PREC_FP64 = 0
+BF_PREC_MIXED = 1
+
+BF_OUT_DEVICE = 1
+
+_c_int = ctypes.c_int
+_c_dbl = ctypes.c_double
+_p_dbl = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+_ull = ctypes.c_ulonglong
+
+# name -> (restype, argtypes); every symbol declared in include/boostfractor_gb300.h
+_SIGS = {
+    "bf_version": (_c_int, []),
+    "bf_create": (_c_int, [_c_int, _ull, ctypes.POINTER(_vp)]),
+    "bf_destroy": (_c_int, [_vp]),
+    "bf_last_error": (ctypes.c_char_p, [_vp]),
+    "bf_device_bytes": (_ull, [_vp]),
+    "bf_set_stream": (_c_int, [_vp, _vp]),
+    "bf_set_profiling": (_c_int, [_vp, _c_int]),
+    "bf_last_profile": (_c_int, [_vp, _p_dbl]),
+    "bf_get_kspace_coords": (_c_int, [_c_int, _p_dbl, _p_dbl]),
+    "bf_fresnel_reflectivities": (_c_int, [_c_int, _p_dbl, _p_dbl]),
+    "bf_propagate": (_c_int, [_vp, _c_int, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl,
+                              _p_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
+    "bf_stack_create": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
+                                 _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, ctypes.POINTER(_vp)]),
+    "bf_stack_destroy": (_c_int, [_vp, _vp]),
+    "bf_stack_set_distance": (_c_int, [_vp, _vp, _p_dbl]),
+    "bf_stack_cheerleader": (_c_int, [_vp, _vp, _c_int, _p_dbl, _c_dbl, _c_int, _c_int, _c_int, _p_dbl,
+                                      _p_dbl, _c_int, _c_dbl, _c_int, _p_dbl, _p_dbl, _p_dbl]),
+    "bf_stack_dancer": (_c_int, [_vp, _vp, _c_int, _p_dbl, _c_dbl, _c_int, _c_int, _c_int, _p_dbl,
+                                 _p_dbl, _c_int, _c_int, _c_dbl, _c_int, _p_dbl, _p_dbl]),
+    "bf_cheerleader": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
+                                _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, _c_int, _p_dbl, _c_dbl,
+                                _c_int, _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _c_dbl, _p_dbl, _p_dbl,
+                                _p_dbl]),
+    "bf_dancer": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int, _c_int,
+                           _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, _c_int, _p_dbl, _c_dbl, _c_int,
+                           _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _c_int, _c_dbl, _p_dbl, _p_dbl]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library (loads on first use; raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python boostfractor.jl_gb300/build.py` "
+                "(there is no CPU fallback)")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def symbols():
+    return list(_SIGS)
+
+
+class BFError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"bf error {code}: {msg}")
+        self.code = code
+
+
+def ptr(a):
+    """double* of a contiguous numpy array (None -> NULL)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(_p_dbl)

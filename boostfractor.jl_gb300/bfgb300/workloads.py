@@ -1,0 +1,71 @@
+"""Seeded synthetic disk stacks for the benchmark configurations.
+
+No public dataset is involved: every input is generated from a numpy
+``default_rng(seed)``.  Each function returns a dict with the reference's
+geometry arrays (``distance``, ``eps``, ``relative_tilt_x/y``,
+``relative_surfaces`` or None), the grid ``X``/``Y``, ``diskR``, the
+frequencies and the solver settings.
+"""
+import numpy as np
+
+
+def symmetric_grid(n, width=1.0):
+    """n points from -width/2 to +width/2, exactly antisymmetric in floating point."""
+    i = np.arange(n, dtype=np.float64)
+    return width * (2 * i - (n - 1)) / (2.0 * (n - 1)) if n > 1 else np.zeros(1)
+
+
+def booster(ndisk, gaps, eps_disk=24.0, thickness=1e-3, tilt_x=None, tilt_y=None):
+    """Mirror + ndisk disks: regions [mirror, gap1, disk1, ..., gapN, diskN, exit]."""
+    nd = 2 * ndisk + 2
+    distance = np.zeros(nd)
+    eps = np.ones(nd, dtype=np.complex128)
+    eps[0] = np.nan
+    for k in range(ndisk):
+        distance[1 + 2 * k] = gaps[k]
+        distance[2 + 2 * k] = thickness
+        eps[2 + 2 * k] = eps_disk
+    tx = np.zeros(nd) if tilt_x is None else np.asarray(tilt_x, dtype=np.float64)
+    ty = np.zeros(nd) if tilt_y is None else np.asarray(tilt_y, dtype=np.float64)
+    return distance, eps, tx, ty
+
+
+def config1_dancer():
+    """Plain dancer, complex128: mirror + 1 disk (eps 24, 1 mm, R 0.15 m, gap 8 mm),
+    64x64 grid over 1 m, 20 GHz, homogeneous emission, nmax = 200 (201 bounces)."""
+    distance, eps, tx, ty = booster(1, [8e-3])
+    X = symmetric_grid(64)
+    return dict(name="dancer-1disk-64", solver="dancer", distance=distance, eps=eps,
+                relative_tilt_x=tx, relative_tilt_y=ty, relative_surfaces=None, X=X, Y=X.copy(),
+                diskR=0.15, freqs=np.array([20e9]), nmax=200, precision="fp64")
+
+
+def config2_cheerleader(seed=2, n=128, ndisk=20, nf=256, nmax=400, f_lo=19.5e9, f_hi=20.5e9):
+    """20-disk booster, cheerleader: 128x128 over 1 m, R 0.15 m, eps 24, 1 mm disks,
+    gaps U(7.5, 8.5) mm, per-disk tilts U(-0.5, 0.5) mrad (air regions untilted),
+    256 frequencies 19.5-20.5 GHz, 400 bounces (nmax = 400), mixed precision."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.uniform(7.5e-3, 8.5e-3, ndisk)
+    nd = 2 * ndisk + 2
+    tx = np.zeros(nd)
+    ty = np.zeros(nd)
+    for k in range(ndisk):
+        tx[2 + 2 * k] = rng.uniform(-0.5e-3, 0.5e-3)
+        ty[2 + 2 * k] = rng.uniform(-0.5e-3, 0.5e-3)
+    distance, eps, tx, ty = booster(ndisk, gaps, tilt_x=tx, tilt_y=ty)
+    X = symmetric_grid(n)
+    return dict(name=f"cheerleader-{ndisk}disk-{n}", solver="cheerleader", distance=distance,
+                eps=eps, relative_tilt_x=tx, relative_tilt_y=ty, relative_surfaces=None, X=X,
+                Y=X.copy(), diskR=0.15, freqs=np.linspace(f_lo, f_hi, nf), nmax=nmax,
+                precision="mixed")
+
+
+def fresnel_r(eps):
+    """SeedSetupBoundaries' reflectivities (src/boost_fractor.jl:98-103), numpy form."""
+    e = np.array(eps, dtype=np.complex128)
+    e.imag[e.imag == 0.0] = -0.0
+    r = [1.0 + 0j]
+    for i in range(2, len(e)):
+        a, b = np.sqrt(e[i - 1]), np.sqrt(e[i])
+        r.append((a - b) / (a + b))
+    return np.array(r, dtype=np.complex128)

@@ -1,0 +1,905 @@
+// Device kernels of the GB300 boost-factor library.
+//
+// * k_fused_stage   -- the hot path: one launch runs one bounce stage of the
+//   recursive Fourier propagation for every frequency of a batch.  Each CTA
+//   propagates one or two region fields through the angular-spectrum
+//   propagator (src/boost_fractor.jl:137-179) and applies the boundary's
+//   reflection/transmission (src/boost_fractor_recurprop.jl:90-120, 310-345)
+//   in its epilogue.  Fields are stored only on the pruned box of pixels the
+//   disk mask can reach; the 2D FFT is separable, so the forward row pass,
+//   the fused column pass (FFT, phasor, inverse FFT) and the inverse row pass
+//   each touch only the lines that can be non-zero or are needed.
+// * phasor / tilt table kernels -- FP64 phase arguments, stored in the field
+//   precision.
+// * general full-grid path -- any grid size (also odd sizes like 101), used
+//   for the per-op propagator, the exit fields and the exact (unpruned) mode.
+// * 1D-propagator solvers -- every pixel is independent.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+
+#include "bf_common.cuh"
+#include "bf_device.cuh"
+#include "bf_fft.cuh"
+
+namespace bf {
+
+static unsigned long long g_launches = 0;
+unsigned long long launch_count() { return g_launches; }
+#define COUNT_LAUNCH() (++g_launches)
+
+// Round an FP64 complex value to complex64 so that the modulus error is as
+// small as possible: of the float pairs within one ulp of (re, im) take the one
+// whose squared modulus is closest to the FP64 one.  Plain rounding leaves a
+// random modulus error of ~6e-8 per value, and a phasor or twiddle that is
+// applied to the same k-bin on every bounce turns that into a systematic gain
+// or loss that compounds over hundreds of bounces.
+__host__ __device__ inline float2 round_c64_host_device(double re, double im) {
+  const float fr = (float)re, fi = (float)im;
+  const double m2 = re * re + im * im;
+  float best_r = fr, best_i = fi;
+  double best = 1e300;
+  for (int a = -1; a <= 1; ++a)
+    for (int b = -1; b <= 1; ++b) {
+      float cr = a == 0 ? fr : nextafterf(fr, a > 0 ? INFINITY : -INFINITY);
+      float ci = b == 0 ? fi : nextafterf(fi, b > 0 ? INFINITY : -INFINITY);
+      double d = fabs((double)cr * cr + (double)ci * ci - m2);
+      // prefer the plain rounding on ties (keeps exact values exact)
+      if (d < best || (d == best && a == 0 && b == 0)) {
+        best = d;
+        best_r = cr;
+        best_i = ci;
+      }
+    }
+  return make_float2(best_r, best_i);
+}
+
+void init_constant_roots() {
+  static double2 hd[1024];
+  static float2 hf[1024];
+  for (int k = 0; k < 1024; ++k) {
+    // exp(-2 pi i k / 1024); cos/sin evaluated on the first octant and mapped
+    // by symmetry so that the table is exactly symmetric
+    int q = k / 256, r = k % 256;
+    double c, s;
+    int rr = r <= 128 ? r : 256 - r;
+    double a = M_PI * rr / 512.0;
+    double cr = cos(a), sr = sin(a);
+    if (r > 128) { double t = cr; cr = sr; sr = t; }
+    // float copy of the first-octant pair, rounded for the smallest modulus error,
+    // then mapped by the same exact symmetry as the FP64 pair
+    const float2 o = round_c64_host_device(cr, sr);
+    float cf, sf;
+    // angle theta = 2 pi k / 1024 = q*pi/2 + 2 pi r/1024; (cos, sin) of theta
+    switch (q) {
+      case 0: c = cr; s = sr; cf = o.x; sf = o.y; break;
+      case 1: c = -sr; s = cr; cf = -o.y; sf = o.x; break;
+      case 2: c = -cr; s = -sr; cf = -o.x; sf = -o.y; break;
+      default: c = sr; s = -cr; cf = o.y; sf = -o.x; break;
+    }
+    hd[k] = make_double2(c, -s);
+    hf[k] = make_float2(cf, -sf);
+  }
+  cudaMemcpyToSymbol(c_root1024_d, hd, sizeof(hd));
+  cudaMemcpyToSymbol(c_root1024_f, hf, sizeof(hf));
+}
+
+// ---------------------------------------------------------------------------
+// small FP64 complex helpers (phase arguments are always FP64)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 dcsqrt(double x, double y) {
+  // principal square root honouring the sign of a zero imaginary part, so that
+  // sqrt(a - 0.0im) = 0 - sqrt(|a|)im for a < 0 (evanescent bins decay)
+  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
+  double t = sqrt((fabs(x) + hypot(x, y)) * 0.5);
+  if (x >= 0.0) return make_double2(t, y / (2.0 * t));
+  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
+__device__ __forceinline__ double2 dcexp(double re, double im) {
+  double s, c;
+  sincos(im, &s, &c);
+  double m = exp(re);
+  return make_double2(m * c, m * s);
+}
+// k0 = 2 pi / lambda * sqrt(eps), eps real -> re - 0.0im (src/boost_fractor.jl:140,:161)
+__device__ __forceinline__ double2 k0_of(double lambda, double eps_re, double eps_im) {
+  if (eps_im == 0.0) eps_im = -0.0;
+  double2 s = dcsqrt(eps_re, eps_im);
+  double c = 2.0 * M_PI / lambda;
+  return make_double2(c * s.x, c * s.y);
+}
+// exp(-1im * sqrt(k0^2 - kx^2 - ky^2) * dz)
+__device__ __forceinline__ double2 phasor_value(double2 k0, double kx, double ky, double dz) {
+  double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+  double re = (k0sq.x - kx * kx) - ky * ky;
+  double2 kz = dcsqrt(re, k0sq.y);
+  // -1im * kz * dz = (kz.y * dz, -kz.x * dz)
+  return dcexp(kz.y * dz, -kz.x * dz);
+}
+// exp(-1im * k0 * t) for complex k0 and real t
+__device__ __forceinline__ double2 phase_k0(double2 k0, double t) {
+  return dcexp(k0.y * t, -k0.x * t);
+}
+// exp(-1im * k0 * s) for complex k0 and complex s
+__device__ __forceinline__ double2 phase_k0c(double2 k0, double2 s) {
+  double re = k0.x * s.x - k0.y * s.y, im = k0.x * s.y + k0.y * s.x;
+  return dcexp(im, -re);
+}
+
+template <typename C> __device__ __forceinline__ C from_d(double2 v);
+template <> __device__ __forceinline__ float2 from_d<float2>(double2 v) {
+  return make_float2((float)v.x, (float)v.y);
+}
+template <> __device__ __forceinline__ double2 from_d<double2>(double2 v) { return v; }
+// phase factors: modulus-aware rounding to complex64
+template <typename C> __device__ __forceinline__ C from_d_phase(double2 v);
+template <> __device__ __forceinline__ float2 from_d_phase<float2>(double2 v) {
+  return round_c64_host_device(v.x, v.y);
+}
+template <> __device__ __forceinline__ double2 from_d_phase<double2>(double2 v) { return v; }
+template <typename C> __device__ __forceinline__ C czero() { return from_d<C>(make_double2(0.0, 0.0)); }
+
+#define SPEED_OF_LIGHT 299792458.0
+
+// ---------------------------------------------------------------------------
+// Fused box stage kernel
+// ---------------------------------------------------------------------------
+constexpr int kFusedThreads = 256;
+
+template <int N>
+__host__ __device__ constexpr int fused_pitch() { return N + 2; }
+
+template <typename C, int N>
+struct FusedCtx {
+  using T = Team<N>;
+  static constexpr int G = T::G, RR = T::RR, CC = T::C;
+  static constexpr int P = fused_pitch<N>();
+  static constexpr int NTEAM = kFusedThreads / G;
+};
+
+// Phases 1-2 of one propagation: forward row FFTs of the masked box rows
+// (exit accumulation of the masked input on the way), then the column pass
+// (forward FFT, phasor, inverse FFT) in place in M.
+template <typename C, int N>
+__device__ __forceinline__ void fused_rows_cols(const FusedArgs<C>& a, int f, int slot, int region,
+                                                int exitk, C* M, C* scr,
+                                                const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nbx = a.nbx, nby = a.nby;
+  const C* src = a.state + ((size_t)f * a.nslots + slot) * (size_t)(nby * nbx);
+  double2* acc = exitk >= 0 ? a.exitacc + ((size_t)exitk * a.nfreq + f) * (size_t)(nby * nbx) : nullptr;
+
+  // phase 1: forward FFT along x of every box row
+  for (int base = 0; base < nby; base += NTEAM) {
+    const int y = base + team;
+    const bool act = y < nby;
+    C v[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      const int x = g + G * r;
+      C val = czero<C>();
+      if (act && x < nbx) {
+        const int i = y * nbx + x;
+        if (a.mask[i]) {
+          val = src[i];
+          if (acc) {
+            double2 t = acc[i];
+            double2 d = to_d(val);
+            acc[i] = make_double2(t.x + d.x, t.y + d.y);
+          }
+        }
+      }
+      v[r] = val;
+    }
+    X::T::forward(v, tw, scr, g);
+    if (act) {
+#pragma unroll
+      for (int j = 0; j < CC; ++j)
+#pragma unroll
+        for (int q = 0; q < G; ++q) M[y * P + g * CC + j + RR * q] = v[j * G + q];
+    }
+  }
+  __syncthreads();
+
+  // phase 2: per column kx: FFT along y, phasor, inverse FFT along y
+  const int QW = a.fold ? N / 2 : N;
+  const C* Q = a.phasor + ((size_t)f * a.ntab + region) * (size_t)(QW * QW);
+  for (int base = 0; base < N; base += NTEAM) {
+    const int kx = base + team;
+    const bool act = kx < N;
+    C v[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      const int y = g + G * r;
+      v[r] = (act && y < nby) ? M[y * P + kx] : czero<C>();
+    }
+    X::T::forward(v, tw, scr, g);
+    if (act) {
+      const int kxf = a.fold ? (kx < N / 2 ? kx : N - 1 - kx) : kx;
+      const C* Qrow = Q + (size_t)kxf * QW;
+#pragma unroll
+      for (int j = 0; j < CC; ++j)
+#pragma unroll
+        for (int q = 0; q < G; ++q) {
+          const int ky = g * CC + j + RR * q;
+          const int kyf = a.fold ? (ky < N / 2 ? ky : N - 1 - ky) : ky;
+          v[j * G + q] = cmul(v[j * G + q], Qrow[kyf]);
+        }
+    }
+    X::T::inverse(v, tw, scr, g);
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < RR; ++r) {
+        const int y = g + G * r;
+        if (y < nby) M[y * P + kx] = v[r];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Phase 3: inverse FFT along x of every box row, tilt/surface map, then the
+// epilogue: store (first of two propagations) or boundary mix.
+template <typename C, int N, bool MIX>
+__device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const StepDesc& sd, int f,
+                                               int region, bool prop_is_b, C* M, C* scr,
+                                               C* obuf, int obuf_pitch,
+                                               const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nbx = a.nbx, nby = a.nby;
+  const size_t plane = (size_t)nby * nbx;
+  const int ti = a.tilt_idx[region];
+  const C* tmap = ti >= 0 ? a.tilt + ((size_t)f * a.ntilt + ti) * plane : nullptr;
+  C* stA = sd.sa >= 0 ? a.state + ((size_t)f * a.nslots + sd.sa) * plane : nullptr;
+  C* stB = sd.sb >= 0 ? a.state + ((size_t)f * a.nslots + sd.sb) * plane : nullptr;
+  const C* add = (MIX && sd.addA >= 0) ? a.addbuf + (size_t)sd.addA * plane : nullptr;
+  C cAA, cAB, cBA, cBB;
+  if (MIX) {
+    const double2* cf = a.coefs + 4 * sd.coef;
+    cAA = from_d<C>(cf[0]); cAB = from_d<C>(cf[1]); cBA = from_d<C>(cf[2]); cBB = from_d<C>(cf[3]);
+  }
+  for (int base = 0; base < nby; base += NTEAM) {
+    const int y = base + team;
+    const bool act = y < nby;
+    C v[RR];
+#pragma unroll
+    for (int j = 0; j < CC; ++j)
+#pragma unroll
+      for (int q = 0; q < G; ++q) v[j * G + q] = act ? M[y * P + g * CC + j + RR * q] : czero<C>();
+    X::T::inverse(v, tw, scr, g);
+    if (!act) continue;
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      const int x = g + G * r;
+      if (x >= nbx) continue;
+      const int i = y * nbx + x;
+      C p = v[r];
+      if (tmap) p = cmul(p, tmap[i]);
+      if (!MIX) {
+        obuf[y * obuf_pitch + x] = p;
+      } else {
+        C tA, tB;
+        if (prop_is_b) {
+          tB = p;
+          if (sd.ra >= 0) tA = obuf[y * obuf_pitch + x];
+          else tA = stA ? stA[i] : czero<C>();
+        } else {
+          tA = p;
+          tB = stB ? stB[i] : czero<C>();
+        }
+        if (stA) {
+          C o = cadd(cmul(cAA, tA), cmul(cAB, tB));
+          if (add) o = cadd(o, add[i]);
+          stA[i] = o;
+        }
+        if (stB) stB[i] = cadd(cmul(cBA, tA), cmul(cBB, tB));
+      }
+    }
+  }
+}
+
+template <typename R, int N>
+__global__ void __launch_bounds__(kFusedThreads, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
+k_fused_stage(FusedArgs<cplx_t<R>> a, int obuf_smem) {
+  using C = cplx_t<R>;
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, P = X::P;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nbx = a.nbx, nby = a.nby;
+  C* M = reinterpret_cast<C*>(smem_raw);
+  C* obuf_s = M + nby * P;
+  C* scr_all = obuf_s + (obuf_smem ? nby * nbx : 0);
+  const int tid = threadIdx.x, team = tid / G, g = tid % G;
+  C* scr = scr_all + team * X::T::SCR;
+  const StepDesc sd = a.steps[blockIdx.x];
+  const int f = blockIdx.y;
+  C tw[RR];
+  team_twiddles<N>(tw, g);
+
+  const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
+  if (pa && pb) {
+    // first propagation (A) -> obuf (shared memory, or the A slot itself)
+    C* obuf = obuf_smem ? obuf_s : a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * nbx);
+    fused_rows_cols<C, N>(a, f, sd.sa, sd.ra, sd.exitA, M, scr, tw, team, g);
+    fused_rows_inv<C, N, false>(a, sd, f, sd.ra, false, M, scr, obuf, nbx, tw, team, g);
+    __syncthreads();
+    fused_rows_cols<C, N>(a, f, sd.sb, sd.rb, sd.exitB, M, scr, tw, team, g);
+    fused_rows_inv<C, N, true>(a, sd, f, sd.rb, true, M, scr, obuf, nbx, tw, team, g);
+  } else if (pa) {
+    fused_rows_cols<C, N>(a, f, sd.sa, sd.ra, sd.exitA, M, scr, tw, team, g);
+    fused_rows_inv<C, N, true>(a, sd, f, sd.ra, false, M, scr, nullptr, nbx, tw, team, g);
+  } else if (pb) {
+    fused_rows_cols<C, N>(a, f, sd.sb, sd.rb, sd.exitB, M, scr, tw, team, g);
+    fused_rows_inv<C, N, true>(a, sd, f, sd.rb, true, M, scr, nullptr, nbx, tw, team, g);
+  }
+}
+
+template <int N>
+static size_t fused_smem_for(int nbx, int nby, size_t csz, bool obuf) {
+  const int G = Team<N>::G;
+  const size_t nteam = kFusedThreads / G;
+  return csz * ((size_t)nby * fused_pitch<N>() + (obuf ? (size_t)nby * nbx : 0) +
+                nteam * Team<N>::SCR);
+}
+
+static size_t smem_for(int N, int nbx, int nby, size_t csz, bool obuf) {
+  switch (N) {
+    case 8: return fused_smem_for<8>(nbx, nby, csz, obuf);
+    case 16: return fused_smem_for<16>(nbx, nby, csz, obuf);
+    case 32: return fused_smem_for<32>(nbx, nby, csz, obuf);
+    case 64: return fused_smem_for<64>(nbx, nby, csz, obuf);
+    case 128: return fused_smem_for<128>(nbx, nby, csz, obuf);
+    case 256: return fused_smem_for<256>(nbx, nby, csz, obuf);
+    case 512: return fused_smem_for<512>(nbx, nby, csz, obuf);
+    default: return (size_t)-1;
+  }
+}
+
+static const size_t kMaxSmem = 227 * 1024;
+
+size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64) {
+  size_t csz = fp64 ? 16 : 8;
+  size_t s = smem_for(N, nbx, nby, csz, true);
+  if (s <= kMaxSmem) return s;
+  return smem_for(N, nbx, nby, csz, false);
+}
+
+bool fused_supported(int N, int nbx, int nby, bool fp64) {
+  if (N < 8 || N > 512 || (N & (N - 1))) return false;
+  if (nbx < 1 || nby < 1 || nbx > N || nby > N) return false;
+  return fused_smem_bytes(N, nbx, nby, fp64) <= kMaxSmem;
+}
+
+template <typename R, int N>
+static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
+  const size_t csz = sizeof(cplx_t<R>);
+  size_t smem = smem_for(N, a.nbx, a.nby, csz, true);
+  int obuf = 1;
+  if (smem > kMaxSmem) {
+    smem = smem_for(N, a.nbx, a.nby, csz, false);
+    obuf = 0;
+  }
+  if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  dim3 grid(nsteps, a.nfreq);
+  COUNT_LAUNCH();
+  k_fused_stage<R, N><<<grid, kFusedThreads, smem, st>>>(a, obuf);
+  return (int)cudaGetLastError();
+}
+
+template <typename R>
+static int launch_fused_dispatch(int N, const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
+  if (nsteps <= 0 || a.nfreq <= 0) return 0;
+  switch (N) {
+    case 8: return launch_fused_t<R, 8>(a, nsteps, st);
+    case 16: return launch_fused_t<R, 16>(a, nsteps, st);
+    case 32: return launch_fused_t<R, 32>(a, nsteps, st);
+    case 64: return launch_fused_t<R, 64>(a, nsteps, st);
+    case 128: return launch_fused_t<R, 128>(a, nsteps, st);
+    case 256: return launch_fused_t<R, 256>(a, nsteps, st);
+    case 512: return launch_fused_t<R, 512>(a, nsteps, st);
+    default: return (int)cudaErrorInvalidValue;
+  }
+}
+
+int launch_fused_stage_f(int N, const FusedArgs<float2>& a, int nsteps, cudaStream_t st) {
+  return launch_fused_dispatch<float>(N, a, nsteps, st);
+}
+int launch_fused_stage_d(int N, const FusedArgs<double2>& a, int nsteps, cudaStream_t st) {
+  return launch_fused_dispatch<double>(N, a, nsteps, st);
+}
+
+// ---------------------------------------------------------------------------
+// Phasor and tilt tables
+// ---------------------------------------------------------------------------
+template <typename C>
+__global__ void k_phasor_table(C* out, int nfreq, const double* freqs, int ntab, const int* regions,
+                               const RegionGeo* geo, int N, const double* kX, const double* kY,
+                               int fold) {
+  const int W = fold ? N / 2 : N;
+  const int per = W * W;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y, f = blockIdx.z;
+  if (idx >= per) return;
+  const int kxb = idx / W, kyb = idx % W;
+  const int sx = (kxb + N / 2) % N, sy = (kyb + N / 2) % N;
+  const RegionGeo gg = geo[regions[t]];
+  const double lambda = SPEED_OF_LIGHT / freqs[f];
+  const double2 k0 = k0_of(lambda, gg.eps_re, gg.eps_im);
+  double2 v = phasor_value(k0, kX[sx], kY[sy], gg.dz);
+  const double sc = 1.0 / ((double)N * (double)N);   // a power of two: exact
+  out[((size_t)f * ntab + t) * per + idx] = from_d_phase<C>(make_double2(v.x * sc, v.y * sc));
+}
+
+int launch_phasor_table(bool fp64, void* out, int nfreq, const double* d_freqs, int ntab,
+                        const int* d_regions, const RegionGeo* d_geo, int N, const double* d_kX,
+                        const double* d_kY, int fold, cudaStream_t st) {
+  if (ntab <= 0 || nfreq <= 0) return 0;
+  const int W = fold ? N / 2 : N;
+  dim3 grid((W * W + 255) / 256, ntab, nfreq);
+  if (fp64) { COUNT_LAUNCH(); k_phasor_table<double2><<<grid, 256, 0, st>>>((double2*)out, nfreq, d_freqs, ntab, d_regions, d_geo, N, d_kX, d_kY, fold); }
+  else { COUNT_LAUNCH(); k_phasor_table<float2><<<grid, 256, 0, st>>>((float2*)out, nfreq, d_freqs, ntab, d_regions, d_geo, N, d_kX, d_kY, fold); }
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_tilt_table(C* out, int nfreq, const double* freqs, int nmaps, const int* regions,
+                             const RegionGeo* geo, int nbx, int nby, int bx0, int by0, int nx, int ny,
+                             const double* X, const double* Y, const double2* surf) {
+  const int per = nbx * nby;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int m = blockIdx.y, f = blockIdx.z;
+  if (idx >= per) return;
+  const int iy = idx / nbx, ix = idx % nbx;
+  const int x = bx0 + ix, y = by0 + iy;
+  const int reg = regions[m];
+  const RegionGeo gg = geo[reg];
+  const double lambda = SPEED_OF_LIGHT / freqs[f];
+  const double2 k0 = k0_of(lambda, gg.eps_re, gg.eps_im);
+  double2 v = cmul(phase_k0(k0, gg.tilt_x * X[x]), phase_k0(k0, gg.tilt_y * Y[y]));
+  if (surf) v = cmul(v, phase_k0c(k0, surf[((size_t)reg * ny + y) * nx + x]));
+  out[((size_t)f * nmaps + m) * per + idx] = from_d_phase<C>(v);
+}
+
+int launch_tilt_table(bool fp64, void* out, int nfreq, const double* d_freqs, int nmaps,
+                      const int* d_regions, const RegionGeo* d_geo, int nbx, int nby, int bx0,
+                      int by0, int nx, int ny, const double* d_X, const double* d_Y,
+                      const double2* d_surf, cudaStream_t st) {
+  if (nmaps <= 0 || nfreq <= 0) return 0;
+  dim3 grid((nbx * nby + 255) / 256, nmaps, nfreq);
+  if (fp64) { COUNT_LAUNCH(); k_tilt_table<double2><<<grid, 256, 0, st>>>((double2*)out, nfreq, d_freqs, nmaps, d_regions, d_geo, nbx, nby, bx0, by0, nx, ny, d_X, d_Y, d_surf); }
+  else { COUNT_LAUNCH(); k_tilt_table<float2><<<grid, 256, 0, st>>>((float2*)out, nfreq, d_freqs, nmaps, d_regions, d_geo, nbx, nby, bx0, by0, nx, ny, d_X, d_Y, d_surf); }
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// General full-grid path
+// ---------------------------------------------------------------------------
+// One block transforms one line of length n held in shared memory: radix-2
+// Stockham for powers of two, direct O(n^2) evaluation otherwise.  Roots are
+// evaluated in FP64 (sincospi) for either field precision.
+template <typename C>
+__global__ void k_line_dft(C* data, int nx, int ny, int axis, int inverse) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int n = axis == 0 ? nx : ny;
+  C* buf0 = reinterpret_cast<C*>(sm);
+  C* buf1 = buf0 + n;
+  C* tw = buf1 + n;   // tw[m] = exp(-+2 pi i m / n)
+  const int line = blockIdx.x, b = blockIdx.y;
+  const size_t base = (size_t)b * nx * ny;
+  const size_t stride = axis == 0 ? 1 : nx;
+  const size_t off = axis == 0 ? (size_t)line * nx : (size_t)line;
+  const double sgn = inverse ? 2.0 : -2.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    buf0[i] = data[base + off + i * stride];
+    double s, c;
+    sincospi(sgn * (double)i / (double)n, &s, &c);
+    tw[i] = from_d<C>(make_double2(c, s));
+  }
+  __syncthreads();
+  if ((n & (n - 1)) == 0) {
+    // Stockham autosort, radix 2
+    C* src = buf0;
+    C* dst = buf1;
+    for (int l = 1; l < n; l <<= 1) {   // l = size of the sub-transforms being combined
+      const int tstep = n / (2 * l);
+      for (int i = threadIdx.x; i < n / 2; i += blockDim.x) {
+        const int j = i % l;            // position within sub-transform
+        const int k = i / l;            // sub-transform index
+        const C w = tw[j * tstep];
+        C u = src[k * l + j];
+        C v = cmul(src[k * l + j + n / 2], w);
+        dst[2 * k * l + j] = cadd(u, v);
+        dst[2 * k * l + j + l] = csub(u, v);
+      }
+      __syncthreads();
+      C* t = src; src = dst; dst = t;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) data[base + off + i * stride] = src[i];
+  } else {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      double2 acc = make_double2(0.0, 0.0);
+      int m = 0;
+      for (int j = 0; j < n; ++j) {
+        const double2 w = to_d(tw[m]);
+        const double2 x = to_d(buf0[j]);
+        acc.x += x.x * w.x - x.y * w.y;
+        acc.y += x.x * w.y + x.y * w.x;
+        m += k;
+        if (m >= n) m -= n;
+      }
+      buf1[k] = from_d<C>(acc);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) data[base + off + i * stride] = buf1[i];
+  }
+}
+
+int launch_line_dft(bool fp64, void* data, int nb, int nx, int ny, int axis, int inverse,
+                    cudaStream_t st) {
+  const int n = axis == 0 ? nx : ny;
+  const int nlines = axis == 0 ? ny : nx;
+  if (n <= 1) return 0;
+  const size_t smem = (fp64 ? 16 : 8) * (size_t)(3 * n);
+  if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
+  dim3 grid(nlines, nb);
+  int thr = n >= 256 ? 256 : ((n + 31) / 32) * 32;
+  if (fp64) {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      COUNT_LAUNCH();
+      k_line_dft<double2><<<grid, thr, smem, st>>>((double2*)data, nx, ny, axis, inverse);
+  } else {
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      COUNT_LAUNCH();
+      k_line_dft<float2><<<grid, thr, smem, st>>>((float2*)data, nx, ny, axis, inverse);
+  }
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_mul_mask(C* data, size_t total, int npix, const unsigned char* mask) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    if (!mask[i % npix]) data[i] = czero<C>();
+}
+
+static dim3 grid1d(size_t n) {
+  size_t b = (n + 255) / 256;
+  if (b > 65535 * 16) b = 65535 * 16;
+  if (b < 1) b = 1;
+  return dim3((unsigned)b);
+}
+
+int launch_mul_mask(bool fp64, void* data, int nb, int nx, int ny, const unsigned char* d_mask,
+                    cudaStream_t st) {
+  size_t total = (size_t)nb * nx * ny;
+  if (fp64) { COUNT_LAUNCH(); k_mul_mask<double2><<<grid1d(total), 256, 0, st>>>((double2*)data, total, nx * ny, d_mask); }
+  else { COUNT_LAUNCH(); k_mul_mask<float2><<<grid1d(total), 256, 0, st>>>((float2*)data, total, nx * ny, d_mask); }
+  return (int)cudaGetLastError();
+}
+
+__device__ __forceinline__ double lambda_of(const double* freqs, const double* lambdas, int b) {
+  return lambdas ? lambdas[b] : SPEED_OF_LIGHT / freqs[b];
+}
+
+template <typename C>
+__global__ void k_mul_phasor_full(C* data, int nb, int nx, int ny, const double* freqs,
+                                  const double* lambdas, RegionGeo g, const double* kX,
+                                  const double* kY, int shifted, double scale) {
+  const size_t total = (size_t)nb * nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const int y = (int)((i / nx) % ny);
+    const int b = (int)(i / ((size_t)nx * ny));
+    const int sx = shifted ? x : (x + nx / 2) % nx;
+    const int sy = shifted ? y : (y + ny / 2) % ny;
+    const double2 k0 = k0_of(lambda_of(freqs, lambdas, b), g.eps_re, g.eps_im);
+    double2 p = phasor_value(k0, kX[sx], kY[sy], g.dz);
+    p.x *= scale; p.y *= scale;
+    double2 d = to_d(data[i]);
+    data[i] = from_d<C>(cmul(d, p));
+  }
+}
+
+int launch_mul_phasor_full(bool fp64, void* data, int nb, int nx, int ny, const double* d_freqs,
+                           const double* d_lambda, RegionGeo g, const double* d_kX,
+                           const double* d_kY, int shifted_layout, double scale, cudaStream_t st) {
+  size_t total = (size_t)nb * nx * ny;
+  if (fp64) { COUNT_LAUNCH(); k_mul_phasor_full<double2><<<grid1d(total), 256, 0, st>>>((double2*)data, nb, nx, ny, d_freqs, d_lambda, g, d_kX, d_kY, shifted_layout, scale); }
+  else { COUNT_LAUNCH(); k_mul_phasor_full<float2><<<grid1d(total), 256, 0, st>>>((float2*)data, nb, nx, ny, d_freqs, d_lambda, g, d_kX, d_kY, shifted_layout, scale); }
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_mul_tilt_full(C* data, int nb, int nx, int ny, const double* freqs,
+                                const double* lambdas, RegionGeo g, const double* X, const double* Y,
+                                const double2* surf, int only_if_nonzero) {
+  const size_t total = (size_t)nb * nx * ny;
+  const bool do_tilt = !only_if_nonzero || g.tilt_x != 0.0 || g.tilt_y != 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const int y = (int)((i / nx) % ny);
+    const int b = (int)(i / ((size_t)nx * ny));
+    const double2 k0 = k0_of(lambda_of(freqs, lambdas, b), g.eps_re, g.eps_im);
+    double2 d = to_d(data[i]);
+    if (do_tilt) d = cmul(d, cmul(phase_k0(k0, g.tilt_x * X[x]), phase_k0(k0, g.tilt_y * Y[y])));
+    if (surf) d = cmul(d, phase_k0c(k0, surf[(size_t)y * nx + x]));
+    data[i] = from_d<C>(d);
+  }
+}
+
+int launch_mul_tilt_full(bool fp64, void* data, int nb, int nx, int ny, const double* d_freqs,
+                         const double* d_lambda, RegionGeo g, const double* d_X, const double* d_Y,
+                         const double2* d_surf, int only_if_nonzero, cudaStream_t st) {
+  size_t total = (size_t)nb * nx * ny;
+  if (fp64) { COUNT_LAUNCH(); k_mul_tilt_full<double2><<<grid1d(total), 256, 0, st>>>((double2*)data, nb, nx, ny, d_freqs, d_lambda, g, d_X, d_Y, d_surf, only_if_nonzero); }
+  else { COUNT_LAUNCH(); k_mul_tilt_full<float2><<<grid1d(total), 256, 0, st>>>((float2*)data, nb, nx, ny, d_freqs, d_lambda, g, d_X, d_Y, d_surf, only_if_nonzero); }
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_mul_phase1d(C* data, int nb, int npix, const double* freqs, const double* lambdas,
+                              RegionGeo g) {
+  const size_t total = (size_t)nb * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(i / npix);
+    const double2 k0 = k0_of(lambda_of(freqs, lambdas, b), g.eps_re, g.eps_im);
+    data[i] = from_d<C>(cmul(to_d(data[i]), phase_k0(k0, g.dz)));
+  }
+}
+
+int launch_mul_scalar_phase_1d(bool fp64, void* data, int nb, int nx, int ny, const double* d_freqs,
+                               const double* d_lambda, RegionGeo g, cudaStream_t st) {
+  size_t total = (size_t)nb * nx * ny;
+  if (fp64) { COUNT_LAUNCH(); k_mul_phase1d<double2><<<grid1d(total), 256, 0, st>>>((double2*)data, nb, nx * ny, d_freqs, d_lambda, g); }
+  else { COUNT_LAUNCH(); k_mul_phase1d<float2><<<grid1d(total), 256, 0, st>>>((float2*)data, nb, nx * ny, d_freqs, d_lambda, g); }
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_roll(const C* in, C* out, int nb, int nx, int ny, int sx, int sy) {
+  const size_t total = (size_t)nb * nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const int y = (int)((i / nx) % ny);
+    const size_t b = i / ((size_t)nx * ny);
+    const int xs = ((x - sx) % nx + nx) % nx;
+    const int ys = ((y - sy) % ny + ny) % ny;
+    out[i] = in[(b * ny + ys) * nx + xs];
+  }
+}
+
+int launch_roll(bool fp64, const void* in, void* out, int nb, int nx, int ny, int sx, int sy,
+                cudaStream_t st) {
+  size_t total = (size_t)nb * nx * ny;
+  if (fp64) { COUNT_LAUNCH(); k_roll<double2><<<grid1d(total), 256, 0, st>>>((const double2*)in, (double2*)out, nb, nx, ny, sx, sy); }
+  else { COUNT_LAUNCH(); k_roll<float2><<<grid1d(total), 256, 0, st>>>((const float2*)in, (float2*)out, nb, nx, ny, sx, sy); }
+  return (int)cudaGetLastError();
+}
+
+template <typename CI, typename CO>
+__global__ void k_convert(const CI* in, CO* out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = from_d<CO>(to_d(in[i]));
+}
+
+int launch_convert(const void* in, bool in_fp64, void* out, bool out_fp64, size_t n, cudaStream_t st) {
+  if (in_fp64 && out_fp64) { COUNT_LAUNCH(); k_convert<double2, double2><<<grid1d(n), 256, 0, st>>>((const double2*)in, (double2*)out, n); }
+  else if (in_fp64) { COUNT_LAUNCH(); k_convert<double2, float2><<<grid1d(n), 256, 0, st>>>((const double2*)in, (float2*)out, n); }
+  else if (out_fp64) { COUNT_LAUNCH(); k_convert<float2, double2><<<grid1d(n), 256, 0, st>>>((const float2*)in, (double2*)out, n); }
+  else { COUNT_LAUNCH(); k_convert<float2, float2><<<grid1d(n), 256, 0, st>>>((const float2*)in, (float2*)out, n); }
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// exits, broadcast, reductions
+// ---------------------------------------------------------------------------
+__global__ void k_exit_combine(double2* out, const double2* full, const double2* direct, double2 coef,
+                               int nfreq, int npix) {
+  const size_t total = (size_t)nfreq * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    double2 v = cmul(coef, full[i]);
+    if (direct) {
+      double2 d = direct[i % npix];
+      v = make_double2(v.x + d.x, v.y + d.y);
+    }
+    out[i] = v;
+  }
+}
+
+int launch_exit_combine(double2* out, const double2* full, const double2* direct, double2 coef,
+                        int nfreq, int npix, cudaStream_t st) {
+  size_t total = (size_t)nfreq * npix;
+  COUNT_LAUNCH();
+  k_exit_combine<<<grid1d(total), 256, 0, st>>>(out, full, direct, coef, nfreq, npix);
+  return (int)cudaGetLastError();
+}
+
+__global__ void k_embed_box(double2* full, const double2* box, int nfreq, int nx, int ny, int nbx,
+                            int nby, int bx0, int by0) {
+  const size_t total = (size_t)nfreq * nx * ny;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx);
+    const int y = (int)((i / nx) % ny);
+    const size_t f = i / ((size_t)nx * ny);
+    const int ix = x - bx0, iy = y - by0;
+    double2 v = make_double2(0.0, 0.0);
+    if (ix >= 0 && ix < nbx && iy >= 0 && iy < nby) v = box[(f * nby + iy) * nbx + ix];
+    full[i] = v;
+  }
+}
+
+int launch_embed_box(double2* full, const double2* box, int nfreq, int nx, int ny, int nbx, int nby,
+                     int bx0, int by0, cudaStream_t st) {
+  size_t total = (size_t)nfreq * nx * ny;
+  COUNT_LAUNCH();
+  k_embed_box<<<grid1d(total), 256, 0, st>>>(full, box, nfreq, nx, ny, nbx, nby, bx0, by0);
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_broadcast(C* state, const double2* init, int nfreq, size_t per) {
+  const size_t total = (size_t)nfreq * per;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    state[i] = from_d<C>(init[i % per]);
+}
+
+int launch_broadcast_state(bool fp64, void* state, const double2* init, int nfreq, size_t per,
+                           cudaStream_t st) {
+  size_t total = (size_t)nfreq * per;
+  if (fp64) { COUNT_LAUNCH(); k_broadcast<double2><<<grid1d(total), 256, 0, st>>>((double2*)state, init, nfreq, per); }
+  else { COUNT_LAUNCH(); k_broadcast<float2><<<grid1d(total), 256, 0, st>>>((float2*)state, init, nfreq, per); }
+  return (int)cudaGetLastError();
+}
+
+__global__ void k_beta2(double* beta2, const double2* E, int npix, double scale) {
+  __shared__ double red[256];
+  const int f = blockIdx.x;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < npix; i += blockDim.x) {
+    double2 v = E[(size_t)f * npix + i];
+    s += v.x * v.x + v.y * v.y;
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) beta2[f] = red[0] * scale;
+}
+
+int launch_beta2(double* beta2, const double2* E, int nfreq, int npix, double scale, cudaStream_t st) {
+  if (nfreq <= 0) return 0;
+  COUNT_LAUNCH();
+  k_beta2<<<nfreq, 256, 0, st>>>(beta2, E, npix, scale);
+  return (int)cudaGetLastError();
+}
+
+template <typename C>
+__global__ void k_maxabs(unsigned long long* out, const C* data, size_t n) {
+  __shared__ double red[256];
+  double m = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double2 v = to_d(data[i]);
+    m = fmax(m, hypot(v.x, v.y));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  // non-negative doubles order like their bit patterns
+  if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(red[0]));
+}
+
+int launch_maxabs(double* d_out, const void* data, bool fp64, size_t n, cudaStream_t st) {
+  cudaMemsetAsync(d_out, 0, sizeof(double), st);
+  unsigned blocks = (unsigned)((n + 255) / 256);
+  if (blocks > 1024) blocks = 1024;
+  if (blocks < 1) blocks = 1;
+  if (fp64) { COUNT_LAUNCH(); k_maxabs<double2><<<blocks, 256, 0, st>>>((unsigned long long*)d_out, (const double2*)data, n); }
+  else { COUNT_LAUNCH(); k_maxabs<float2><<<blocks, 256, 0, st>>>((unsigned long long*)d_out, (const float2*)data, n); }
+  return (int)cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// 1D propagator solvers: the field at every pixel bounces independently
+// (prop = propagator1D multiplies by exp(-i k0 dz) and applies no mask).
+// FP64 for both precisions.
+// ---------------------------------------------------------------------------
+__global__ void k_rfp1d(Rfp1dArgs a) {
+  const size_t total = (size_t)a.nfreq * a.npix;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const int f = (int)(t / a.npix);
+    const int p = (int)(t % a.npix);
+    const int nd = a.nd;
+    const double2* ph = a.phase + (size_t)f * nd;
+    double2* S = (double2*)a.state;
+    if (a.kind == 0) {
+      // cheerleader (src/boost_fractor_recurprop.jl:226-363); exits in out[f][0]=right, [1]=left
+      auto s_at = [&](int j) -> double2& { return S[((size_t)f * nd + j) * a.npix + p]; };
+      double2* outR = a.out + ((size_t)f * 2 + 0) * a.npix + p;
+      double2* outL = a.out + ((size_t)f * 2 + 1) * a.npix + p;
+      auto em = [&](int j, int d) { return a.emit[((size_t)j * 2 + d) * a.npix + p]; };
+      auto cf = [&](int i, int k) { return a.coef[4 * i + k]; };  // r_r, t_l, r_l, t_r
+      if (a.do_init) {
+        for (int j = 0; j < nd; ++j) s_at(j) = em(j, 0);
+        for (int i = 1; i <= nd - 2; ++i) {
+          s_at(i) = cmul(s_at(i), ph[i]);
+          s_at(i + 1) = cadd(s_at(i + 1), cmul(cf(i, 3), s_at(i)));
+          s_at(i) = cmul(s_at(i), cf(i, 0));
+        }
+        for (int j = 0; j <= nd - 2; ++j) s_at(j) = cadd(s_at(j), em(j, 1));
+        s_at(nd - 2) = cadd(s_at(nd - 2), cmul(cf(nd - 2, 1), em(nd - 1, 1)));
+        s_at(nd - 1) = cadd(s_at(nd - 1), cmul(cf(nd - 2, 2), em(nd - 1, 1)));
+        *outR = s_at(nd - 1);
+        *outL = s_at(0);
+        // the exit regions live in out[] from here on
+        s_at(nd - 1) = make_double2(0.0, 0.0);
+        s_at(0) = make_double2(0.0, 0.0);
+      }
+      double2 eR = *outR, eL = *outL;
+      for (int n = a.n_begin; n < a.n_end; ++n) {
+        double2 f1 = cmul(s_at(1), ph[1]);
+        eL = cadd(eL, cmul(cf(0, 1), f1));
+        s_at(1) = cmul(f1, cf(0, 2));
+        for (int i = 1; i <= nd - 3; ++i) {
+          double2 fi = cmul(s_at(i), ph[i]);
+          double2 fn = cmul(s_at(i + 1), ph[i + 1]);
+          s_at(i + 1) = cadd(cmul(cf(i, 2), fn), cmul(cf(i, 3), fi));
+          s_at(i) = cadd(cmul(cf(i, 0), fi), cmul(cf(i, 1), fn));
+        }
+        const int i = nd - 2;
+        double2 fi = cmul(s_at(i), ph[i]);
+        eR = cadd(eR, cmul(cf(i, 3), fi));
+        s_at(i) = cmul(fi, cf(i, 0));
+      }
+      *outR = eR;
+      *outL = eL;
+    } else {
+      // dancer (src/boost_fractor_recurprop.jl:25-146): nd trimmed regions,
+      // boundaries 0..nd with r[nd] = 0 appended; coef[i].x = r[i]
+      auto s_at = [&](int j, int d) -> double2& { return S[(((size_t)f * nd + j) * 2 + d) * a.npix + p]; };
+      for (int n = a.n_begin; n < a.n_end; ++n) {
+        const int rm = (n + a.rm_phase) & 1, lm = rm ^ 1;
+        for (int i = 0; i <= nd; ++i) {
+          if (i > 0) s_at(i - 1, rm) = cmul(s_at(i - 1, rm), ph[i - 1]);
+          if (i < nd) s_at(i, lm) = cmul(s_at(i, lm), ph[i]);
+          const double2 r = a.coef[4 * i];
+          const double2 one_p = make_double2(1.0 + r.x, r.y), one_m = make_double2(1.0 - r.x, -r.y);
+          const double2 mr = make_double2(-r.x, -r.y);
+          if (i == 0) {
+            s_at(0, lm) = cmul(s_at(0, lm), mr);
+          } else if (i == nd) {
+            double2 e = cmul(one_p, s_at(nd - 1, rm));
+            double2* o = a.out + ((size_t)f * a.nout + (a.per_iter_out ? n : 0)) * a.npix + p;
+            if (a.per_iter_out) *o = e;
+            else *o = cadd(*o, e);
+            s_at(nd - 1, rm) = cmul(s_at(nd - 1, rm), r);
+          } else {
+            double2 c = s_at(i - 1, rm);
+            s_at(i - 1, rm) = cadd(cmul(r, c), cmul(one_m, s_at(i, lm)));
+            s_at(i, lm) = cadd(cmul(mr, s_at(i, lm)), cmul(one_p, c));
+          }
+        }
+      }
+    }
+  }
+}
+
+int launch_rfp1d(bool fp64, const Rfp1dArgs& a, cudaStream_t st) {
+  (void)fp64;
+  size_t total = (size_t)a.nfreq * a.npix;
+  unsigned blocks = (unsigned)((total + 127) / 128);
+  if (blocks < 1) blocks = 1;
+  COUNT_LAUNCH();
+  k_rfp1d<<<blocks, 128, 0, st>>>(a);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace bf

@@ -1,0 +1,160 @@
+// Register-resident FFT building blocks for the fused propagation kernels.
+//
+// A line of N = C*G*G points (N a power of two) is transformed by a "team" of
+// G threads holding RR = C*G points each:
+//   pass 1  every thread does an RR-point DFT over the points x[g + G*r]
+//           (r = 0..RR-1) in registers and multiplies by W_N^(g*s);
+//   exchange through a swizzled shared-memory tile (one write + one read);
+//   pass 2  every thread does C G-point DFTs in registers.
+// Afterwards thread g holds X[(g*C + j) + RR*q] in v[j*G + q].  The inverse is
+// the exact adjoint (same exchange, conjugate roots) and returns the points to
+// the x[g + G*r] layout, unnormalised (a factor N).
+#pragma once
+
+#include "bf_common.cuh"
+
+namespace bf {
+
+// Unit roots W_1024^k = exp(-2 pi i k / 1024), filled from the host in FP64.
+// Register FFTs index them with compile-time offsets, so they compile into
+// constant-bank operands.  Defined here: this header belongs to exactly one
+// translation unit (bf_device.cu).
+__constant__ double2 c_root1024_d[1024];
+__constant__ float2 c_root1024_f[1024];
+
+template <typename C> __device__ __forceinline__ C root1024(int k);
+template <> __device__ __forceinline__ float2 root1024<float2>(int k) { return c_root1024_f[k]; }
+template <> __device__ __forceinline__ double2 root1024<double2>(int k) { return c_root1024_d[k]; }
+
+// v[i] *= W_M^k (forward) or conj(W_M^k) (inverse), k compile-time after unrolling.
+template <int M, bool INV, typename C>
+__device__ __forceinline__ C twiddle_mul(C a, int k) {
+  if (k == 0) return a;
+  if (4 * k == M) return cmul_mi<INV>(a);
+  C w = root1024<C>(k * (1024 / M));
+  return INV ? cmulc(a, w) : cmul(a, w);
+}
+
+template <int M>
+__host__ __device__ constexpr int bitrev(int i) {
+  int r = 0;
+  for (int b = 1; b < M; b <<= 1) {
+    r = (r << 1) | (i & 1);
+    i >>= 1;
+  }
+  return r;
+}
+
+// In-register M-point DFT of v[OFF .. OFF+M-1] (radix-2 decimation in
+// frequency followed by a static bit-reversal permutation).
+template <int M, bool INV, int OFF, int LEN, typename C>
+__device__ __forceinline__ void reg_dft(C (&v)[LEN]) {
+  if constexpr (M == 1) {
+    return;
+  } else {
+#pragma unroll
+    for (int len = M; len >= 2; len >>= 1) {
+      const int half = len >> 1;
+#pragma unroll
+      for (int i = 0; i < M; i += len) {
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+          C a = v[OFF + i + j];
+          C b = v[OFF + i + j + half];
+          v[OFF + i + j] = cadd(a, b);
+          v[OFF + i + j + half] = twiddle_mul<M, INV>(csub(a, b), j * (M / len));
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      const int r = bitrev<M>(i);
+      if (r > i) {
+        C t = v[OFF + i];
+        v[OFF + i] = v[OFF + r];
+        v[OFF + r] = t;
+      }
+    }
+  }
+}
+
+template <int N> struct TeamShape;
+template <> struct TeamShape<8>   { static constexpr int G = 2,  RR = 4;  };
+template <> struct TeamShape<16>  { static constexpr int G = 4,  RR = 4;  };
+template <> struct TeamShape<32>  { static constexpr int G = 4,  RR = 8;  };
+template <> struct TeamShape<64>  { static constexpr int G = 8,  RR = 8;  };
+template <> struct TeamShape<128> { static constexpr int G = 8,  RR = 16; };
+template <> struct TeamShape<256> { static constexpr int G = 16, RR = 16; };
+template <> struct TeamShape<512> { static constexpr int G = 16, RR = 32; };
+
+template <int N>
+struct Team {
+  static constexpr int G = TeamShape<N>::G;
+  static constexpr int RR = TeamShape<N>::RR;
+  static constexpr int C = RR / G;
+  static_assert(C * G * G == N, "team shape");
+  // scratch tile of one team, in complex elements; the pad staggers the tiles
+  // of teams sharing a half-warp across shared-memory banks
+  static constexpr int SCR = RR * G + (G < 16 ? G : 0);
+
+  __device__ static __forceinline__ int swz(int s, int g) { return s * G + (g ^ (s / C)); }
+
+  // forward: v[r] = x[g + G r]  ->  v[j*G + q] = X[(g*C + j) + RR*q]
+  template <typename Cx>
+  __device__ static __forceinline__ void forward(Cx (&v)[RR], const Cx (&tw)[RR], Cx* scr, int g) {
+    reg_dft<RR, false, 0>(v);
+#pragma unroll
+    for (int s = 1; s < RR; ++s) v[s] = cmul(v[s], tw[s]);
+#pragma unroll
+    for (int s = 0; s < RR; ++s) scr[swz(s, g)] = v[s];
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < C; ++j)
+#pragma unroll
+      for (int gp = 0; gp < G; ++gp) v[j * G + gp] = scr[swz(g * C + j, gp)];
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < C; ++j) reg_dft_sub<false>(v, j);
+  }
+
+  // inverse (adjoint of forward, unnormalised): v[j*G + q] = X[(g*C + j) + RR*q] -> v[r] = N x[g + G r]
+  template <typename Cx>
+  __device__ static __forceinline__ void inverse(Cx (&v)[RR], const Cx (&tw)[RR], Cx* scr, int g) {
+#pragma unroll
+    for (int j = 0; j < C; ++j) reg_dft_sub<true>(v, j);
+#pragma unroll
+    for (int j = 0; j < C; ++j)
+#pragma unroll
+      for (int gp = 0; gp < G; ++gp) scr[swz(g * C + j, gp)] = v[j * G + gp];
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < RR; ++s) v[s] = scr[swz(s, g)];
+    __syncwarp();
+#pragma unroll
+    for (int s = 1; s < RR; ++s) v[s] = cmulc(v[s], tw[s]);
+    reg_dft<RR, true, 0>(v);
+  }
+
+ private:
+  template <bool INV, typename Cx>
+  __device__ static __forceinline__ void reg_dft_sub(Cx (&v)[RR], int j) {
+    // j is a compile-time constant after unrolling of the caller's loop
+    static_assert(C == 1 || C == 2, "team shape");
+    if constexpr (C == 1) {
+      reg_dft<G, INV, 0>(v);
+    } else {
+      if (j == 0) reg_dft<G, INV, 0>(v);
+      else reg_dft<G, INV, G>(v);
+    }
+  }
+};
+
+// Per-thread inter-pass twiddles W_N^(g*s), s = 0..RR-1 (g*s < N always).
+template <int N, typename Cx>
+__device__ __forceinline__ void team_twiddles(Cx (&tw)[Team<N>::RR], int g) {
+  static_assert(N <= 1024, "root table");
+#pragma unroll
+  for (int s = 0; s < Team<N>::RR; ++s) tw[s] = root1024<Cx>(g * s * (1024 / N));
+}
+
+}  // namespace bf

@@ -1,0 +1,172 @@
+/*
+ * boostfractor_gb300.h -- C ABI of the GB300-native boost-factor solvers.
+ *
+ * Drop-in boundary for the hot path of BoostFractor.jl: the coordinate
+ * system, the boundary setup, the angular-spectrum propagators, the
+ * recursive-Fourier-propagation solvers (dancer / cheerleader) and the
+ * transfer-matrix mode matching (transformer).  Julia reaches it with
+ * `ccall`; Python tests and benches with ctypes.
+ *
+ * Conventions
+ *   - Every entry point returns an int status (BF_OK = 0); the message of the
+ *     last failure is available from bf_last_error(handle).  Nothing throws
+ *     across the ABI.
+ *   - Arrays are the reference's Julia arrays passed as raw pointers:
+ *     column-major, ComplexF64 interleaved (re, im) doubles.  A field E is
+ *     (nx, ny) with x fastest; relative_surfaces is (nd, nx, ny) with the
+ *     region index fastest; emit is (nd, 2, nx, ny).
+ *   - Caller-owned host buffers are read or written only during the call.
+ *     Device objects (stacks, mode bases) are owned by the handle.
+ *   - A handle is not thread-safe: use one handle per host thread.  It owns
+ *     one CUDA stream, its device allocations and its CUDA graphs.
+ */
+#ifndef BOOSTFRACTOR_GB300_H
+#define BOOSTFRACTOR_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define BF_OK              0
+#define BF_ERR_INVALID     1  /* bad argument: shape mismatch, NaN geometry, null pointer
+                                 (reference: DimensionMismatch, src/boost_fractor.jl:105;
+                                 error(), src/boost_fractor_transformer.jl:101) */
+#define BF_ERR_NOMEM       2  /* device allocation above the handle's HBM budget, or cudaMalloc failed */
+#define BF_ERR_CUDA        3  /* a CUDA runtime call failed */
+#define BF_ERR_TIMEOUT     4  /* a bounded wait expired */
+#define BF_ERR_UNSUPPORTED 5  /* valid request outside what this build implements */
+
+/* ---- propagator plug-ins: the reference's `prop=` keyword ---------------- */
+#define BF_PROP_3D       0  /* propagator              src/boost_fractor.jl:137-149 */
+#define BF_PROP_NOTILTS  1  /* propagatorNoTilts       src/boost_fractor.jl:157-179 */
+#define BF_PROP_MOMENTUM 2  /* propagatorMomentumSpace src/boost_fractor.jl:187-210 */
+#define BF_PROP_1D       3  /* propagator1D            src/boost_fractor.jl:218-227 */
+
+/* ---- arithmetic of a solve ---------------------------------------------- */
+#define BF_PREC_FP64  0  /* complex128 fields, FP64 transforms (the plain FP64 path) */
+#define BF_PREC_MIXED 1  /* complex64 fields and transforms; FP64 phase argument kz*dz,
+                            FP64 exit (bounce-sum) accumulation, FP64 final solve */
+
+/* ---- flags -------------------------------------------------------------- */
+#define BF_OUT_DEVICE 1  /* output pointers are device pointers (results stay in HBM) */
+
+typedef struct bf_handle bf_handle;
+typedef struct bf_stack bf_stack;
+typedef struct bf_modes bf_modes;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int bf_version(void);
+
+/* Create a handle on CUDA device `device`.  `hbm_budget_bytes` caps the
+ * device memory the handle may hold (0 = no cap).  One stream per handle. */
+int bf_create(int device, unsigned long long hbm_budget_bytes, bf_handle** out);
+int bf_destroy(bf_handle* h);
+/* Message of the last failed call on this handle ("" if none). */
+const char* bf_last_error(const bf_handle* h);
+/* Bytes of device memory the handle currently holds. */
+unsigned long long bf_device_bytes(const bf_handle* h);
+
+/* Run the handle's work on a caller's CUDA stream (a cudaStream_t passed as
+ * void*); NULL returns to the handle's own stream.  No reference counterpart:
+ * it lets a caller order the solves with its own device work. */
+int bf_set_stream(bf_handle* h, void* cuda_stream);
+
+/* Profiling of the pruned bounce solver.  When enabled, each solve records
+ * CUDA events on the handle's stream; bf_last_profile fills out[8] with
+ *   [0] device ms of the whole solve, [1] device ms of the bounce stages,
+ *   [2] device ms of table setup, [3] device ms of the exit fields and beta^2,
+ *   [4] bounce-stage kernel launches, [5] kernel launches of the solve,
+ *   [6] propagations run in the bounce stages, [7] frequencies.
+ * Returns BF_ERR_INVALID when the last solve did not record a profile.
+ * No reference counterpart (the reference only times with @time). */
+int bf_set_profiling(bf_handle* h, int enable);
+int bf_last_profile(const bf_handle* h, double* out);
+
+/* ---- host-side geometry helpers (no GPU work) ---------------------------- */
+/* get_kspace_coords: dk = 2pi/(2 max X), values -(n-1)/2*dk ... (n-1)/2*dk.
+ * Replaces src/boost_fractor.jl:42-47 (used by SeedCoordinateSystem :30-34). */
+int bf_get_kspace_coords(int n, const double* real_coords, double* kspace_out);
+/* Fresnel reflectivities of SeedSetupBoundaries: r[0] = 1 (mirror),
+ * r[i-1] = (sqrt(eps[i-1]) - sqrt(eps[i]))/(sqrt(eps[i-1]) + sqrt(eps[i])), i >= 2
+ * (0-based), real eps taken as re - 0.0im.  eps: nd complex, r_out: nd-1 complex.
+ * Replaces src/boost_fractor.jl:98-103. */
+int bf_fresnel_reflectivities(int nd, const double* eps, double* r_out);
+
+/* ---- per-op propagator: the `prop=` drop-in ------------------------------ */
+/* E (nx, ny) complex, propagated in place by distance dz through a medium of
+ * permittivity eps, like prop(E0, dz, diskR, eps, tilt_x, tilt_y, surface,
+ * lambda, coords).  `surface` is (nx, ny) complex or NULL (= zeros).
+ * prop_kind: BF_PROP_*; precision: BF_PREC_*.
+ * Replaces src/boost_fractor.jl:137-227. */
+int bf_propagate(bf_handle* h, int prop_kind, int precision,
+                 double* E, int nx, int ny,
+                 const double* X, const double* Y, const double* kX, const double* kY,
+                 double dz, double diskR, double eps_re, double eps_im,
+                 double tilt_x, double tilt_y, const double* surface, double lambda);
+
+/* ---- resident disk stacks ------------------------------------------------ */
+/* Upload a SetupBoundaries (src/boost_fractor.jl:63-71) and a CoordinateSystem
+ * (:21-28) once; the stack stays in HBM until bf_stack_destroy.
+ *   nd regions; distance[nd]; r[nd-1] complex; eps[nd] complex (NaN allowed
+ *   for the mirror region 0); tilt_x[nd], tilt_y[nd]; surfaces (nd, nx, ny)
+ *   complex or NULL (= zeros); X[nx], Y[ny], kX[nx], kY[ny]; diskR. */
+int bf_stack_create(bf_handle* h, int nd, const double* distance, const double* r,
+                    const double* eps, const double* tilt_x, const double* tilt_y,
+                    const double* surfaces, int nx, int ny, const double* X,
+                    const double* Y, const double* kX, const double* kY, double diskR,
+                    bf_stack** out);
+int bf_stack_destroy(bf_handle* h, bf_stack* s);
+/* Replace the region distances of a resident stack (optimiser step). */
+int bf_stack_set_distance(bf_handle* h, bf_stack* s, const double* distance);
+
+/* ---- recursive Fourier propagation -------------------------------------- */
+/* cheerleader for nf frequencies of one resident stack, batched in one solve.
+ * emit (nd, 2, nx, ny) complex or NULL (= dance_intro default), reflect
+ * (nx, ny) complex or NULL.  Outputs per frequency f: out_right[f] (nx, ny)
+ * complex, out_left[f] (if returnboth; else may be NULL), out_beta2[f] =
+ * beta2_scale * sum |out_right[f]|^2 (may be NULL; the reference's boost
+ * factor uses beta2_scale = dx*dy/(pi diskR^2), test/runtests.jl:74).
+ * nmax+1 bounce iterations run while the field maximum stays >= amin.
+ * flags: BF_OUT_DEVICE.
+ * Replaces src/boost_fractor_recurprop.jl:226-363 (and dance_intro :153-201). */
+int bf_stack_cheerleader(bf_handle* h, bf_stack* s, int nf, const double* freqs,
+                         double amin, int nmax, int prop_kind, int precision,
+                         const double* emit, const double* reflect, int returnboth,
+                         double beta2_scale, int flags,
+                         double* out_right, double* out_left, double* out_beta2);
+
+/* dancer (legacy two-field bounce loop).  Output out[f] is (nx, ny) complex when
+ * returnsum, else (nx, ny, nmax+1) complex per frequency.
+ * Replaces src/boost_fractor_recurprop.jl:25-146. */
+int bf_stack_dancer(bf_handle* h, bf_stack* s, int nf, const double* freqs,
+                    double amin, int nmax, int prop_kind, int precision,
+                    const double* emit, const double* reflect, int returnsum,
+                    int immediatesum, double beta2_scale, int flags,
+                    double* out, double* out_beta2);
+
+/* One-shot forms with host buffers: create a stack, solve, destroy.  Same
+ * arguments as bf_stack_create followed by the solver's. */
+int bf_cheerleader(bf_handle* h, int nd, const double* distance, const double* r,
+                   const double* eps, const double* tilt_x, const double* tilt_y,
+                   const double* surfaces, int nx, int ny, const double* X,
+                   const double* Y, const double* kX, const double* kY, double diskR,
+                   int nf, const double* freqs, double amin, int nmax, int prop_kind,
+                   int precision, const double* emit, const double* reflect,
+                   int returnboth, double beta2_scale,
+                   double* out_right, double* out_left, double* out_beta2);
+int bf_dancer(bf_handle* h, int nd, const double* distance, const double* r,
+              const double* eps, const double* tilt_x, const double* tilt_y,
+              const double* surfaces, int nx, int ny, const double* X,
+              const double* Y, const double* kX, const double* kY, double diskR,
+              int nf, const double* freqs, double amin, int nmax, int prop_kind,
+              int precision, const double* emit, const double* reflect,
+              int returnsum, int immediatesum, double beta2_scale,
+              double* out, double* out_beta2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BOOSTFRACTOR_GB300_H */
