@@ -27,6 +27,8 @@ __all__ = [
     "CoordinateSystem", "SeedCoordinateSystem", "SetupBoundaries", "SeedSetupBoundaries",
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
+    "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
+    "calc_propagation_matrices", "transformer",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -354,9 +356,9 @@ class Stack:
         return out.transpose(0, 3, 2, 1), beta2
 
     def close(self):
-        if getattr(self, "_s", None):
+        if getattr(self, "_s", None) and self.h._h:
             _lib.lib().bf_stack_destroy(self.h.ptr, self._s)
-            self._s = None
+        self._s = None
 
     def __del__(self):
         try:
@@ -401,3 +403,155 @@ def boost_factor(E, coords, diskR):
     dx = X[1] - X[0] if len(X) > 1 else 1.0
     dy = Y[1] - Y[0] if len(Y) > 1 else 1.0
     return float(np.sum(np.abs(E) ** 2) * dx * dy / (math.pi * diskR ** 2))
+
+
+# --------------------------------------------------------------------------
+# transformer (src/boost_fractor_transformer.jl)
+# --------------------------------------------------------------------------
+class Modes:
+    """Resident mode basis (bf_modes_create); mirrors the reference's Modes
+    (src/boost_fractor_transformer.jl:31-38): M, L, mode_patterns, mode_kt."""
+
+    def __init__(self, coords, ThreeDim=False, Mmax=1, Lmax=0, diskR=0.15, pattern_input=None,
+                 kT_arr=None, handle=None):
+        self.h = handle or default_handle()
+        self.coords = coords
+        nx, ny = len(coords.X), len(coords.Y)
+        self.nx, self.ny = nx, ny
+        pbuf = kbuf = None
+        if pattern_input is not None:
+            parr, pbuf = _fcplx(pattern_input, (Mmax, 2 * Lmax + 1, nx, ny, 1))
+            self._p = parr
+        if kT_arr is not None:
+            karr, kbuf = _fcplx(kT_arr, (Mmax, 2 * Lmax + 1))
+            self._k = karr
+        m = _lib._vp()
+        self.h.check(_lib.lib().bf_modes_create(
+            self.h.ptr, nx, ny, _lib.ptr(coords.X), _lib.ptr(coords.Y), int(bool(ThreeDim)), int(Mmax),
+            int(Lmax), float(diskR), _lib.ptr(pbuf), _lib.ptr(kbuf), _lib.ctypes.byref(m)))
+        self._m = m
+        self.M, self.L = (int(Mmax), int(Lmax)) if ThreeDim else (1, 0)
+        self.nm = self.M * (2 * self.L + 1)
+
+    @property
+    def mode_patterns(self):
+        out = np.empty((1, ny := self.ny, self.nx, 2 * self.L + 1, self.M), dtype=np.complex128)
+        n = _lib.ctypes.c_int()
+        self.h.check(_lib.lib().bf_modes_get(self.h.ptr, self._m, _lib.ctypes.byref(n),
+                                             _lib.ptr(out.view(np.float64)), None))
+        return out.transpose(4, 3, 2, 1, 0)
+
+    @property
+    def mode_kt(self):
+        out = np.empty((2 * self.L + 1, self.M), dtype=np.complex128)
+        self.h.check(_lib.lib().bf_modes_get(self.h.ptr, self._m, None, None, _lib.ptr(out.view(np.float64))))
+        return out.T
+
+    def close(self):
+        if getattr(self, "_m", None) and self.h._h:
+            _lib.lib().bf_modes_destroy(self.h.ptr, self._m)
+        self._m = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def SeedModes(coords, ThreeDim=False, Mmax=1, Lmax=0, diskR=0.15, pattern_input=None, kT_arr=None,
+              handle=None):
+    """src/boost_fractor_transformer.jl:46-69."""
+    return Modes(coords, ThreeDim=ThreeDim, Mmax=Mmax, Lmax=Lmax, diskR=diskR,
+                 pattern_input=pattern_input, kT_arr=kT_arr, handle=handle)
+
+
+def axion_induced_modes(coords, modes, B=None, velocity_x=0.0, diskR=0.15, f=20e9):
+    """src/boost_fractor_transformer.jl:115-151."""
+    bbuf = None
+    if B is not None:
+        B = np.asarray(B)
+        if B.ndim == 3:
+            B = B[:, :, 0]
+        barr, bbuf = _fcplx(B, (modes.nx, modes.ny))
+    out = np.empty(modes.nm, dtype=np.complex128)
+    modes.h.check(_lib.lib().bf_axion_induced_modes(modes.h.ptr, modes._m, _lib.ptr(bbuf), float(velocity_x),
+                                                    float(diskR), float(f), _lib.ptr(out.view(np.float64))))
+    return out
+
+
+def field2modes(pattern, coords, modes, diskR=0.15):
+    """src/boost_fractor_transformer.jl:156."""
+    return axion_induced_modes(coords, modes, B=pattern, diskR=diskR)
+
+
+def modes2field(mode_coeffs, coords, modes):
+    """src/boost_fractor_transformer.jl:161-167; returns (nx, ny, 1)."""
+    c = np.ascontiguousarray(mode_coeffs, dtype=np.complex128)
+    out = np.empty((modes.ny, modes.nx), dtype=np.complex128)
+    modes.h.check(_lib.lib().bf_modes2field(modes.h.ptr, modes._m, _lib.ptr(c.view(np.float64)),
+                                            _lib.ptr(out.view(np.float64))))
+    return out.T[:, :, None]
+
+
+def calc_propagation_matrices(bdry, coords, modes, f=10.0e9, prop=propagator, diskR=0.15, precision="fp64"):
+    """src/boost_fractor_transformer.jl:274-280: list of (nm, nm) matrices per region
+    (array [nf, nd, nm, nm] when f is an array)."""
+    freqs = np.ascontiguousarray(np.atleast_1d(f), dtype=np.float64)
+    st = Stack(bdry, coords, diskR, handle=modes.h)
+    try:
+        nd, nm, nf = st.nd, modes.nm, len(freqs)
+        out = np.empty((nf, nd, nm, nm), dtype=np.complex128)
+        st.h.check(_lib.lib().bf_calc_propagation_matrices(
+            st.h.ptr, st._s, modes._m, nf, _lib.ptr(freqs), _prop_kind(prop), _prec(precision),
+            _lib.ptr(out.view(np.float64))))
+    finally:
+        st.close()
+    out = out.transpose(0, 1, 3, 2)   # Julia column-major matrices -> [row, col]
+    if np.ndim(f) == 0:
+        return [out[0, j] for j in range(out.shape[1])]
+    return out
+
+
+def transformer(bdry, coords, modes, f=10.0e9, velocity_x=0.0, prop=propagator, propagation_matrices=None,
+                diskR=0.15, emit=None, reflect=None, precision="fp64"):
+    """src/boost_fractor_transformer.jl:285-359 on the GPU.  Like the reference,
+    NaN permittivities of ``bdry`` are replaced by 1e30 in place (:289)."""
+    freqs = np.ascontiguousarray(np.atleast_1d(f), dtype=np.float64)
+    nf = len(freqs)
+    if emit is None and velocity_x != 0:
+        emit = axion_induced_modes(coords, modes, B=None, velocity_x=velocity_x, diskR=diskR, f=freqs[0])
+    bdry.eps[np.isnan(bdry.eps)] = 1e30
+    st = Stack(bdry, coords, diskR, handle=modes.h)
+    try:
+        nm, nd = modes.nm, st.nd
+        ebuf = rbuf = pbuf = None
+        if emit is not None:
+            e = np.ascontiguousarray(emit, dtype=np.complex128).reshape(nm)
+            ebuf = e.view(np.float64)
+        if reflect is not None:
+            r = np.ascontiguousarray(reflect, dtype=np.complex128).reshape(nm)
+            rbuf = r.view(np.float64)
+        per_freq = 0
+        if propagation_matrices is not None and len(propagation_matrices):
+            pmat = np.asarray(propagation_matrices, dtype=np.complex128)
+            if pmat.ndim == 3:
+                pmat = pmat[None]
+            per_freq = int(pmat.shape[0] == nf and nf > 1)
+            pm = np.ascontiguousarray(pmat.transpose(0, 1, 3, 2))   # [.., row, col] -> Julia column-major
+            pbuf = pm.view(np.float64)
+        boost = np.empty((nf, nm), dtype=np.complex128)
+        refl = np.empty((nf, nm), dtype=np.complex128) if reflect is not None else None
+        beta2 = np.empty(nf, dtype=np.float64)
+        st.h.check(_lib.lib().bf_transformer(
+            st.h.ptr, st._s, modes._m, nf, _lib.ptr(freqs), _prop_kind(prop), _prec(precision), _lib.ptr(ebuf),
+            _lib.ptr(rbuf), _lib.ptr(pbuf), per_freq, _lib.ptr(boost.view(np.float64)),
+            _lib.ptr(None if refl is None else refl.view(np.float64)), _lib.ptr(beta2)))
+    finally:
+        st.close()
+    if np.ndim(f) == 0:
+        boost = boost[0]
+        refl = None if refl is None else refl[0]
+    if reflect is None:
+        return boost
+    return boost, refl

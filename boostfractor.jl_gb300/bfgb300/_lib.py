@@ -62,6 +62,15 @@ _SIGS = {
     "bf_dancer": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int, _c_int,
                            _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, _c_int, _p_dbl, _c_dbl, _c_int,
                            _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _c_int, _c_dbl, _p_dbl, _p_dbl]),
+    "bf_modes_create": (_c_int, [_vp, _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _c_int, _c_int, _c_dbl, _p_dbl,
+                                 _p_dbl, ctypes.POINTER(_vp)]),
+    "bf_modes_destroy": (_c_int, [_vp, _vp]),
+    "bf_modes_get": (_c_int, [_vp, _vp, ctypes.POINTER(_c_int), _p_dbl, _p_dbl]),
+    "bf_axion_induced_modes": (_c_int, [_vp, _vp, _p_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl]),
+    "bf_modes2field": (_c_int, [_vp, _vp, _p_dbl, _p_dbl]),
+    "bf_calc_propagation_matrices": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl]),
+    "bf_transformer": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _c_int,
+                                _p_dbl, _p_dbl, _p_dbl]),
 }
 
 _lib = None

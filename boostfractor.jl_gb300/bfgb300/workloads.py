@@ -60,6 +60,40 @@ def config2_cheerleader(seed=2, n=128, ndisk=20, nf=256, nmax=400, f_lo=19.5e9, 
                 precision="mixed")
 
 
+def surface_roughness(X, Y, ngaps, rng, mag=1e-5, trunc=1e-4, xi=0.02, diskR=0.15):
+    """Gaussian random surface maps, the recipe of the reference's optimiser
+    utilities (examples/transformer_optim_utilities.jl:166-195): white noise of
+    rms `mag`, 2D convolution with exp(-(x^2+y^2)/(2 xi^2)) cropped to the grid,
+    renormalised to rms `mag`, clipped at +-trunc, zero outside r > diskR."""
+    from scipy.signal import fftconvolve
+    n = len(X)
+    init = mag * rng.standard_normal((ngaps, len(X), len(Y)))
+    g = np.exp(-(X[:, None] ** 2 + Y[None, :] ** 2) / (2 * xi ** 2))
+    lo, hi = int(np.floor(n / 2)) - 1, int(np.floor(n * 1.5)) - 1
+    for i in range(ngaps):
+        init[i] = fftconvolve(init[i], g, mode="full")[lo:hi, lo:hi]
+    init /= np.sqrt(np.sum(init ** 2, axis=(1, 2)) / (len(X) * len(Y)))[:, None, None]
+    init *= mag
+    np.clip(init, -trunc, trunc, out=init)
+    init *= ((X[:, None] ** 2 + Y[None, :] ** 2) <= diskR ** 2)[None]
+    return init
+
+
+def config3_transformer(seed=3, n=256, ndisk=20, nf=1024, modes=64, f_lo=19e9, f_hi=21e9):
+    """Transformer mode matching: the 20-disk geometry of the cheerleader
+    workload on a 256x256 grid, per-disk surface maps (GRF, rms 10 um,
+    correlation length 2 cm), 64 Bessel disk modes (M=64, L=0), 1024
+    frequencies 19-21 GHz."""
+    w = config2_cheerleader(seed=seed, n=n, ndisk=ndisk, nf=nf, f_lo=f_lo, f_hi=f_hi)
+    rng = np.random.default_rng(seed + 1000)
+    nd = len(w["distance"])
+    surf = np.zeros((nd, n, n))
+    surf[2:nd - 1:2] = surface_roughness(w["X"], w["Y"], ndisk, rng)
+    w.update(name=f"transformer-{ndisk}disk-{n}-{modes}modes", solver="transformer", relative_surfaces=surf,
+             M=modes, L=0)
+    return w
+
+
 def fresnel_r(eps):
     """SeedSetupBoundaries' reflectivities (src/boost_fractor.jl:98-103), numpy form."""
     e = np.array(eps, dtype=np.complex128)

@@ -19,7 +19,7 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libbfgb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["bf_device.cu", "bf_api.cu"]
+SOURCES = ["bf_device.cu", "bf_api.cu", "bf_transformer.cu", "bf_modes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -58,7 +58,7 @@ def build(force=False, verbose=False):
     nv = nvcc()
     jobs = []
     for src in SOURCES:
-        obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OBJDIR, os.path.splitext(src)[0] + ".o")
         cmd = [nv] + _flags() + ["-c", os.path.join(CSRC, src), "-o", obj]
         jobs.append((cmd, obj))
 

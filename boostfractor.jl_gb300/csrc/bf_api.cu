@@ -41,6 +41,7 @@ static int fail(bf_handle* h, int code, const std::string& msg) {
   if (h) h->err = msg;
   return code;
 }
+int bf_fail(bf_handle* h, int code, const std::string& msg) { return fail(h, code, msg); }
 
 #define CK(call)                                                                         \
   do {                                                                                   \
@@ -265,6 +266,8 @@ static void geo_of(const bf_stack* s, std::vector<RegionGeo>& g) {
 static void stack_free(bf_handle* h, bf_stack* s) {
   delete s->ws;
   s->ws = nullptr;
+  if (s->tf_cache && s->tf_cache_delete) s->tf_cache_delete(s->tf_cache);
+  s->tf_cache = nullptr;
   bf_dfree(h, s->dX); bf_dfree(h, s->dY); bf_dfree(h, s->dkX); bf_dfree(h, s->dkY);
   bf_dfree(h, s->d_mask_full); bf_dfree(h, s->d_mask_box); bf_dfree(h, s->d_surf); bf_dfree(h, s->d_geo);
   s->dX = s->dY = s->dkX = s->dkY = nullptr;
@@ -438,6 +441,11 @@ static int general_prop(bf_handle* h, const bf_stack* s, int kind, bool fp64, vo
   }
 }
 
+int bf_general_prop(bf_handle* h, const bf_stack* s, int kind, bool fp64, void* buf, void* tmp, int nb,
+                    const double* d_freqs, int region) {
+  return general_prop(h, s, kind, fp64, buf, tmp, nb, d_freqs, region);
+}
+
 // ---------------------------------------------------------------------------
 // per-op propagator
 // ---------------------------------------------------------------------------
@@ -515,11 +523,16 @@ static int coef_index(Plan& p, Coef4 c) {
   return (int)p.coefs.size() - 1;
 }
 
+// Box part of a full-grid field, pre-masked with the strict propagator mask:
+// the pruned solver stores fields masked (their next use is a propagation,
+// which masks them, src/boost_fractor.jl:159).
 static std::vector<cd> box_of(const bf_stack* s, const cd* full) {
   std::vector<cd> b((size_t)s->nbx * s->nby);
   for (int y = 0; y < s->nby; ++y)
-    for (int x = 0; x < s->nbx; ++x)
-      b[(size_t)y * s->nbx + x] = full[(size_t)(y + s->by0) * s->nx + (x + s->bx0)];
+    for (int x = 0; x < s->nbx; ++x) {
+      const size_t i = (size_t)y * s->nbx + x;
+      b[i] = s->mask_box[i] ? full[(size_t)(y + s->by0) * s->nx + (x + s->bx0)] : cd(0.0, 0.0);
+    }
   return b;
 }
 
@@ -847,6 +860,8 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
   a.coefs = w.coef.as<double2>();
   a.exitacc = w.exitacc.as<double2>();
   a.addbuf = w.nadd ? w.add.as<C>() : nullptr;
+  a.err = reinterpret_cast<int*>(h->d_scalar + 1);
+  CK(cudaMemsetAsync(a.err, 0, sizeof(int), st));
   prof_mark(h, 1);
   const unsigned long long l1 = bf::launch_count();
   for (size_t k = 0; k < w.stage_off.size(); ++k) {
@@ -961,6 +976,7 @@ static int run_full(bf_handle* h, const bf_stack* s, int solver, int prop_kind, 
     m.nf = nf; m.npix = (int)npix;
     size_t total = (size_t)nf * npix;
     unsigned blocks = (unsigned)std::min<size_t>((total + 255) / 256, 65535 * 8);
+    bf::note_launch();
     if (fp64) k_mix_full<double2><<<blocks, 256, 0, st>>>(m);
     else k_mix_full<float2><<<blocks, 256, 0, st>>>(m);
     CK(cudaGetLastError());
@@ -1249,6 +1265,15 @@ static int finish_beta2(bf_handle* h, const DBuf& field, int nf, size_t npix, do
   return BF_OK;
 }
 
+// a bounded device-side wait that gave up leaves 1 in the handle's error word
+static int check_device_error(bf_handle* h) {
+  int err = 0;
+  CK(cudaMemcpyAsync(&err, h->d_scalar + 1, sizeof(int), cudaMemcpyDeviceToHost, h->stream()));
+  CK(cudaStreamSynchronize(h->stream()));
+  if (err) return fail(h, BF_ERR_TIMEOUT, "a bounded wait for a shared-memory copy expired in the bounce kernel");
+  return BF_OK;
+}
+
 static int finish_beta2_ptr(bf_handle* h, bf_stack* s, const double2* field, int nf, size_t npix,
                             double scale, double* out_beta2, int flags) {
   if (!out_beta2) return BF_OK;
@@ -1347,6 +1372,7 @@ extern "C" int bf_stack_cheerleader(bf_handle* h, bf_stack* s, int nf, const dou
       std::fill(tmp_stack.tilt_y.begin(), tmp_stack.tilt_y.end(), 0.0);
       tmp_stack.d_surf = nullptr;
       tmp_stack.ws = nullptr;
+      tmp_stack.tf_cache = nullptr;
       sp = &tmp_stack;
     }
     const std::string key = (emit || reflect) ? std::string() : "cheer|" + std::to_string(nmax);
@@ -1363,6 +1389,7 @@ extern "C" int bf_stack_cheerleader(bf_handle* h, bf_stack* s, int nf, const dou
       if (rc == BF_OK) rc = finish_beta2_ptr(h, sp, ex[0], nf, npix, beta2_scale, out_beta2, flags);
     }
     if (rc == BF_OK) rc = finish_profile(h);
+    if (rc == BF_OK) rc = check_device_error(h);
     if (sp != s) { delete tmp_stack.ws; tmp_stack.ws = nullptr; }
     if (rc != BF_OK) return rc;
   } else {
@@ -1409,6 +1436,8 @@ extern "C" int bf_stack_dancer(bf_handle* h, bf_stack* s, int nf, const double* 
         std::fill(tmp_stack.tilt_y.begin(), tmp_stack.tilt_y.end(), 0.0);
         tmp_stack.d_surf = nullptr;
         tmp_stack.ws = nullptr;
+        tmp_stack.tf_cache = nullptr;
+      tmp_stack.tf_cache = nullptr;
         sp = &tmp_stack;
       }
       const std::string key = (emit || reflect) ? std::string() : "dancer|" + std::to_string(nmax);
@@ -1423,6 +1452,7 @@ extern "C" int bf_stack_dancer(bf_handle* h, bf_stack* s, int nf, const double* 
         rc = deliver(h, out, ex[0], sizeof(double2) * nf * npix, flags);
         if (rc == BF_OK) rc = finish_beta2_ptr(h, sp, ex[0], nf, npix, beta2_scale, out_beta2, flags);
         if (rc == BF_OK) rc = finish_profile(h);
+        if (rc == BF_OK) rc = check_device_error(h);
       }
       if (sp != s) { delete tmp_stack.ws; tmp_stack.ws = nullptr; }
       if (rc != BF_OK) return rc;

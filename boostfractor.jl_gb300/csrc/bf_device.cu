@@ -26,6 +26,7 @@ namespace bf {
 
 static unsigned long long g_launches = 0;
 unsigned long long launch_count() { return g_launches; }
+void note_launch() { ++g_launches; }
 #define COUNT_LAUNCH() (++g_launches)
 
 // Round an FP64 complex value to complex64 so that the modulus error is as
@@ -145,9 +146,9 @@ template <typename C> __device__ __forceinline__ C czero() { return from_d<C>(ma
 // Fused box stage kernel
 // ---------------------------------------------------------------------------
 constexpr int kFusedThreads = 256;
+constexpr int kSmemHeader = 128;
 
-template <int N>
-__host__ __device__ constexpr int fused_pitch() { return N + 2; }
+template <int N> __host__ __device__ constexpr int fused_pitch() { return N + 2; }
 
 template <typename C, int N>
 struct FusedCtx {
@@ -157,40 +158,41 @@ struct FusedCtx {
   static constexpr int NTEAM = kFusedThreads / G;
 };
 
-// Phases 1-2 of one propagation: forward row FFTs of the masked box rows
-// (exit accumulation of the masked input on the way), then the column pass
-// (forward FFT, phasor, inverse FFT) in place in M.
+// Phase 1 of one propagation: forward FFT along x of every box row.  Fields
+// are stored pre-masked, so only register slots r < ceil(nbx/G) can hold box
+// pixels.  A slot feeding an exit adds its (masked) input to the FP64 exit
+// accumulator on the way.
 template <typename C, int N>
-__device__ __forceinline__ void fused_rows_cols(const FusedArgs<C>& a, int f, int slot, int region,
-                                                int exitk, C* M, C* scr,
-                                                const C (&tw)[Team<N>::RR], int team, int g) {
+__device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int slot, int exitk, C* M,
+                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
   const int nbx = a.nbx, nby = a.nby;
   const C* src = a.state + ((size_t)f * a.nslots + slot) * (size_t)(nby * nbx);
   double2* acc = exitk >= 0 ? a.exitacc + ((size_t)exitk * a.nfreq + f) * (size_t)(nby * nbx) : nullptr;
-
-  // phase 1: forward FFT along x of every box row
+  const int rv = (nbx + G - 1) / G;
   for (int base = 0; base < nby; base += NTEAM) {
     const int y = base + team;
     const bool act = y < nby;
+    if (!__any_sync(0xffffffffu, act)) continue;   // the whole warp is idle
+    const C* row = src + y * nbx;
+    double2* arow = acc ? acc + y * nbx : nullptr;
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
-      const int x = g + G * r;
-      C val = czero<C>();
-      if (act && x < nbx) {
-        const int i = y * nbx + x;
-        if (a.mask[i]) {
-          val = src[i];
-          if (acc) {
-            double2 t = acc[i];
+      v[r] = czero<C>();
+      if (r < rv) {
+        const int x = g + G * r;
+        if (act && x < nbx) {
+          const C val = row[x];
+          v[r] = val;
+          if (arow) {
+            double2 o = arow[x];
             double2 d = to_d(val);
-            acc[i] = make_double2(t.x + d.x, t.y + d.y);
+            arow[x] = make_double2(o.x + d.x, o.y + d.y);
           }
         }
       }
-      v[r] = val;
     }
     X::T::forward(v, tw, scr, g);
     if (act) {
@@ -201,38 +203,59 @@ __device__ __forceinline__ void fused_rows_cols(const FusedArgs<C>& a, int f, in
     }
   }
   __syncthreads();
+}
 
-  // phase 2: per column kx: FFT along y, phasor, inverse FFT along y
+// Phase 2: per column kx, forward FFT along y, phasor, inverse FFT along y,
+// in place in M (only the nby box rows are read and written).
+template <typename C, int N>
+__device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, C* M, C* scr,
+                                             const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
-  const C* Q = a.phasor + ((size_t)f * a.ntab + region) * (size_t)(QW * QW);
+  const int rv = (nby + G - 1) / G;
   for (int base = 0; base < N; base += NTEAM) {
     const int kx = base + team;
     const bool act = kx < N;
+    if (!__any_sync(0xffffffffu, act)) continue;
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
-      const int y = g + G * r;
-      v[r] = (act && y < nby) ? M[y * P + kx] : czero<C>();
+      v[r] = czero<C>();
+      if (r < rv) {
+        const int y = g + G * r;
+        if (act && y < nby) v[r] = M[y * P + kx];
+      }
     }
     X::T::forward(v, tw, scr, g);
     if (act) {
-      const int kxf = a.fold ? (kx < N / 2 ? kx : N - 1 - kx) : kx;
-      const C* Qrow = Q + (size_t)kxf * QW;
+      if (a.fold) {
+        // bins k and N-1-k share a phasor; ky = g*CC + j + RR*q < N/2 exactly when q < G/2
+        const C* Qrow = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
 #pragma unroll
-      for (int j = 0; j < CC; ++j)
+        for (int j = 0; j < CC; ++j)
 #pragma unroll
-        for (int q = 0; q < G; ++q) {
-          const int ky = g * CC + j + RR * q;
-          const int kyf = a.fold ? (ky < N / 2 ? ky : N - 1 - ky) : ky;
-          v[j * G + q] = cmul(v[j * G + q], Qrow[kyf]);
-        }
+          for (int q = 0; q < G; ++q) {
+            const int ky = g * CC + j + RR * q;
+            v[j * G + q] = cmul(v[j * G + q], Qrow[q < G / 2 ? ky : N - 1 - ky]);
+          }
+      } else {
+        const C* Qrow = Q + (size_t)kx * QW;
+#pragma unroll
+        for (int j = 0; j < CC; ++j)
+#pragma unroll
+          for (int q = 0; q < G; ++q) v[j * G + q] = cmul(v[j * G + q], Qrow[g * CC + j + RR * q]);
+      }
     }
     X::T::inverse(v, tw, scr, g);
     if (act) {
 #pragma unroll
       for (int r = 0; r < RR; ++r) {
-        const int y = g + G * r;
-        if (y < nby) M[y * P + kx] = v[r];
+        if (r < rv) {
+          const int y = g + G * r;
+          if (y < nby) M[y * P + kx] = v[r];
+        }
       }
     }
   }
@@ -240,12 +263,12 @@ __device__ __forceinline__ void fused_rows_cols(const FusedArgs<C>& a, int f, in
 }
 
 // Phase 3: inverse FFT along x of every box row, tilt/surface map, then the
-// epilogue: store (first of two propagations) or boundary mix.
+// epilogue: store the propagated field into obuf (first of two propagations)
+// or apply the boundary mix and write the new (masked) fields.
 template <typename C, int N, bool MIX>
-__device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const StepDesc& sd, int f,
-                                               int region, bool prop_is_b, C* M, C* scr,
-                                               C* obuf, int obuf_pitch,
-                                               const C (&tw)[Team<N>::RR], int team, int g) {
+__device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, int region,
+                                             bool prop_is_b, C* M, C* scr, C* obuf,
+                                             const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
   const int nbx = a.nbx, nby = a.nby;
@@ -255,6 +278,7 @@ __device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const Step
   C* stA = sd.sa >= 0 ? a.state + ((size_t)f * a.nslots + sd.sa) * plane : nullptr;
   C* stB = sd.sb >= 0 ? a.state + ((size_t)f * a.nslots + sd.sb) * plane : nullptr;
   const C* add = (MIX && sd.addA >= 0) ? a.addbuf + (size_t)sd.addA * plane : nullptr;
+  const int rv = (nbx + G - 1) / G;
   C cAA, cAB, cBA, cBB;
   if (MIX) {
     const double2* cf = a.coefs + 4 * sd.coef;
@@ -263,6 +287,7 @@ __device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const Step
   for (int base = 0; base < nby; base += NTEAM) {
     const int y = base + team;
     const bool act = y < nby;
+    if (!__any_sync(0xffffffffu, act)) continue;
     C v[RR];
 #pragma unroll
     for (int j = 0; j < CC; ++j)
@@ -272,18 +297,21 @@ __device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const Step
     if (!act) continue;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
+      if (r >= rv) continue;
       const int x = g + G * r;
       if (x >= nbx) continue;
       const int i = y * nbx + x;
       C p = v[r];
       if (tmap) p = cmul(p, tmap[i]);
       if (!MIX) {
-        obuf[y * obuf_pitch + x] = p;
+        obuf[i] = p;
       } else {
+        // new fields are stored masked (their next propagation masks them anyway)
+        const bool in = a.mask[i] != 0;
         C tA, tB;
         if (prop_is_b) {
           tB = p;
-          if (sd.ra >= 0) tA = obuf[y * obuf_pitch + x];
+          if (sd.ra >= 0) tA = obuf[i];
           else tA = stA ? stA[i] : czero<C>();
         } else {
           tA = p;
@@ -292,67 +320,71 @@ __device__ __forceinline__ void fused_rows_inv(const FusedArgs<C>& a, const Step
         if (stA) {
           C o = cadd(cmul(cAA, tA), cmul(cAB, tB));
           if (add) o = cadd(o, add[i]);
-          stA[i] = o;
+          stA[i] = in ? o : czero<C>();
         }
-        if (stB) stB[i] = cadd(cmul(cBA, tA), cmul(cBB, tB));
+        if (stB) stB[i] = in ? cadd(cmul(cBA, tA), cmul(cBB, tB)) : czero<C>();
       }
     }
   }
 }
 
+// One bounce stage: grid = (steps of the stage, frequencies).
 template <typename R, int N>
 __global__ void __launch_bounds__(kFusedThreads, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
-k_fused_stage(FusedArgs<cplx_t<R>> a, int obuf_smem) {
+k_fused_stage(FusedArgs<cplx_t<R>> a) {
   using C = cplx_t<R>;
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, P = X::P;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nbx = a.nbx, nby = a.nby;
-  C* M = reinterpret_cast<C*>(smem_raw);
-  C* obuf_s = M + nby * P;
-  C* scr_all = obuf_s + (obuf_smem ? nby * nbx : 0);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int nby = a.nby;
+  C* M = reinterpret_cast<C*>(smem_raw + kSmemHeader);
+  C* scr_all = M + nby * P;
   const int tid = threadIdx.x, team = tid / G, g = tid % G;
   C* scr = scr_all + team * X::T::SCR;
   const StepDesc sd = a.steps[blockIdx.x];
   const int f = blockIdx.y;
   C tw[RR];
   team_twiddles<N>(tw, g);
-
+  const int QW = a.fold ? N / 2 : N;
+  auto qptr = [&](int region) -> const C* {
+    return a.phasor + ((size_t)f * a.ntab + region) * (size_t)(QW * QW);
+  };
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
   if (pa && pb) {
-    // first propagation (A) -> obuf (shared memory, or the A slot itself)
-    C* obuf = obuf_smem ? obuf_s : a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * nbx);
-    fused_rows_cols<C, N>(a, f, sd.sa, sd.ra, sd.exitA, M, scr, tw, team, g);
-    fused_rows_inv<C, N, false>(a, sd, f, sd.ra, false, M, scr, obuf, nbx, tw, team, g);
+    // A~ is parked in the A slot itself until the boundary mix
+    C* obuf = a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * a.nbx);
+    fused_phase1<C, N>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, false>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
     __syncthreads();
-    fused_rows_cols<C, N>(a, f, sd.sb, sd.rb, sd.exitB, M, scr, tw, team, g);
-    fused_rows_inv<C, N, true>(a, sd, f, sd.rb, true, M, scr, obuf, nbx, tw, team, g);
+    fused_phase1<C, N>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
   } else if (pa) {
-    fused_rows_cols<C, N>(a, f, sd.sa, sd.ra, sd.exitA, M, scr, tw, team, g);
-    fused_rows_inv<C, N, true>(a, sd, f, sd.ra, false, M, scr, nullptr, nbx, tw, team, g);
+    fused_phase1<C, N>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, true>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
   } else if (pb) {
-    fused_rows_cols<C, N>(a, f, sd.sb, sd.rb, sd.exitB, M, scr, tw, team, g);
-    fused_rows_inv<C, N, true>(a, sd, f, sd.rb, true, M, scr, nullptr, nbx, tw, team, g);
+    fused_phase1<C, N>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
   }
 }
 
 template <int N>
-static size_t fused_smem_for(int nbx, int nby, size_t csz, bool obuf) {
-  const int G = Team<N>::G;
-  const size_t nteam = kFusedThreads / G;
-  return csz * ((size_t)nby * fused_pitch<N>() + (obuf ? (size_t)nby * nbx : 0) +
-                nteam * Team<N>::SCR);
+static size_t fused_smem_for(int nby, size_t csz) {
+  const size_t nteam = kFusedThreads / Team<N>::G;
+  return kSmemHeader + csz * ((size_t)nby * fused_pitch<N>() + nteam * Team<N>::SCR);
 }
 
-static size_t smem_for(int N, int nbx, int nby, size_t csz, bool obuf) {
+static size_t smem_for(int N, int nby, size_t csz) {
   switch (N) {
-    case 8: return fused_smem_for<8>(nbx, nby, csz, obuf);
-    case 16: return fused_smem_for<16>(nbx, nby, csz, obuf);
-    case 32: return fused_smem_for<32>(nbx, nby, csz, obuf);
-    case 64: return fused_smem_for<64>(nbx, nby, csz, obuf);
-    case 128: return fused_smem_for<128>(nbx, nby, csz, obuf);
-    case 256: return fused_smem_for<256>(nbx, nby, csz, obuf);
-    case 512: return fused_smem_for<512>(nbx, nby, csz, obuf);
+    case 8: return fused_smem_for<8>(nby, csz);
+    case 16: return fused_smem_for<16>(nby, csz);
+    case 32: return fused_smem_for<32>(nby, csz);
+    case 64: return fused_smem_for<64>(nby, csz);
+    case 128: return fused_smem_for<128>(nby, csz);
+    case 256: return fused_smem_for<256>(nby, csz);
     default: return (size_t)-1;
   }
 }
@@ -360,34 +392,26 @@ static size_t smem_for(int N, int nbx, int nby, size_t csz, bool obuf) {
 static const size_t kMaxSmem = 227 * 1024;
 
 size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64) {
-  size_t csz = fp64 ? 16 : 8;
-  size_t s = smem_for(N, nbx, nby, csz, true);
-  if (s <= kMaxSmem) return s;
-  return smem_for(N, nbx, nby, csz, false);
+  (void)nbx;
+  return smem_for(N, nby, fp64 ? 16 : 8);
 }
 
 bool fused_supported(int N, int nbx, int nby, bool fp64) {
-  if (N < 8 || N > 512 || (N & (N - 1))) return false;
+  if (N < 8 || N > 256 || (N & (N - 1))) return false;
   if (nbx < 1 || nby < 1 || nbx > N || nby > N) return false;
   return fused_smem_bytes(N, nbx, nby, fp64) <= kMaxSmem;
 }
 
 template <typename R, int N>
 static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
-  const size_t csz = sizeof(cplx_t<R>);
-  size_t smem = smem_for(N, a.nbx, a.nby, csz, true);
-  int obuf = 1;
-  if (smem > kMaxSmem) {
-    smem = smem_for(N, a.nbx, a.nby, csz, false);
-    obuf = 0;
-  }
+  const size_t smem = smem_for(N, a.nby, sizeof(cplx_t<R>));
   if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return (int)e;
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
-  k_fused_stage<R, N><<<grid, kFusedThreads, smem, st>>>(a, obuf);
+  k_fused_stage<R, N><<<grid, kFusedThreads, smem, st>>>(a);
   return (int)cudaGetLastError();
 }
 
@@ -401,7 +425,6 @@ static int launch_fused_dispatch(int N, const FusedArgs<cplx_t<R>>& a, int nstep
     case 64: return launch_fused_t<R, 64>(a, nsteps, st);
     case 128: return launch_fused_t<R, 128>(a, nsteps, st);
     case 256: return launch_fused_t<R, 256>(a, nsteps, st);
-    case 512: return launch_fused_t<R, 512>(a, nsteps, st);
     default: return (int)cudaErrorInvalidValue;
   }
 }

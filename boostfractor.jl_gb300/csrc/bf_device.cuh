@@ -42,6 +42,7 @@ struct FusedArgs {
   double2* exitacc;               // [exit][f][nby][nbx]
   const C* addbuf;                // [add][nby][nbx] (frequency independent)
   const StepDesc* steps;          // this stage
+  int* err;                       // set to 1 if a bounded wait gave up
 };
 
 // Launch the fused stage kernel (templated on the grid size N and the field
@@ -127,5 +128,6 @@ void init_constant_roots();  // host: fill the unit-root tables (once per device
 
 // Kernel launches issued by this library since load (for launch accounting).
 unsigned long long launch_count();
+void note_launch();   // count a launch made outside bf_device.cu
 
 }  // namespace bf

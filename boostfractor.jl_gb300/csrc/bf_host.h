@@ -109,6 +109,8 @@ struct bf_stack {
   bf::RegionGeo* d_geo = nullptr;  // [region]
   Workspace* ws = nullptr;
   unsigned long long geo_version = 0;  // bumps when the geometry changes
+  void* tf_cache = nullptr;            // transformer setup (mode FFT overlaps) of this stack
+  void (*tf_cache_delete)(void*) = nullptr;
 };
 
 namespace bfhost {

@@ -1,0 +1,1030 @@
+// Transformer (mode matching) on the GPU: mode basis, propagation matrices,
+// transfer-matrix chain and the final boundary solve
+// (src/boost_fractor_transformer.jl:23-359).
+//
+// Propagation matrices P[m][m'] = <Psi_m | prop(Psi_m')> (:174-227) by region class:
+//  * air regions without tilt or surface map ("k-space class"): by Parseval,
+//    sum_x conj(Psi_m) IFFT(D FFT(mask Psi_m')) = (1/N^2) sum_k conj(U_m(k)) D(k) Phi_m'(k)
+//    with U = FFT(Psi), Phi = FFT(mask Psi) frequency independent.  D depends on
+//    k only through kx^2 + ky^2, so the sum folds over the mirror images of k:
+//    P = W[nm^2 x K] * D[K x (freqs * regions)], one GEMM for the whole batch;
+//  * disk regions ("pixel class"): P = diag(exp(-i kz_m dz)) sum_x conj(Psi_m) Psi_m'
+//    TS(x) with TS the tilt/surface phase: P = V[nm^2 x Kd] * E[Kd x (freqs*regions)];
+//    air regions with the 1D propagator use the same GEMM with TS = exp(-i k0 dz);
+//  * air regions with a tilt or surface map, or the momentum-space propagator
+//    ("field class"): every mode is propagated on the full grid and overlapped.
+// The chain T <- T G_s blockdiag(P_s, P_s^-1) needs only its bottom block row;
+// the final solve boost = -T22 \ axion_beam runs in FP64.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/boostfractor_gb300.h"
+#include "bf_common.cuh"
+#include "bf_device.cuh"
+#include "bf_host.h"
+#include "bf_linalg.cuh"
+
+namespace bfmodes {
+double besselj_zero(int nu, int m);
+void seed_modes(int M, int L, const std::vector<double>& X, const std::vector<double>& Y, double diskR,
+                std::vector<std::complex<double>>& out, std::vector<std::complex<double>>& kt);
+}  // namespace bfmodes
+
+using bf::RegionGeo;
+
+struct bf_modes {
+  int M = 0, L = 0, nm = 0, nx = 0, ny = 0;
+  std::vector<double> X, Y;
+  std::vector<cd> pat;   // [nm][ny][nx]
+  std::vector<cd> kt;    // [nm]
+  double2* d_pat = nullptr;
+  unsigned long long id = 0;
+};
+
+// engine-wide helpers from bf_api.cu
+int bf_fail(bf_handle* h, int code, const std::string& msg);
+int bf_general_prop(bf_handle* h, const bf_stack* s, int kind, bool fp64, void* buf, void* tmp, int nb,
+                    const double* d_freqs, int region);
+
+#define TCK(call)                                                                            \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return bf_fail(h, BF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+  } while (0)
+#define TCKS(call)              \
+  do {                          \
+    int s_ = (call);            \
+    if (s_ != BF_OK) return s_; \
+  } while (0)
+
+namespace {
+
+constexpr double kC = 299792458.0;
+
+__device__ __forceinline__ double2 dsqrt_c(double x, double y) {
+  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
+  double t = sqrt((fabs(x) + hypot(x, y)) * 0.5);
+  if (x >= 0.0) return make_double2(t, y / (2.0 * t));
+  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
+__device__ __forceinline__ double2 dexp_c(double re, double im) {
+  double s, c;
+  sincos(im, &s, &c);
+  const double m = exp(re);
+  return make_double2(m * c, m * s);
+}
+// k0 = 2 pi / lambda sqrt(eps); a zero imaginary part keeps its sign
+__device__ __forceinline__ double2 k0_c(double lambda, double er, double ei) {
+  double2 s = dsqrt_c(er, ei);
+  const double c = 2.0 * M_PI / lambda;
+  return make_double2(c * s.x, c * s.y);
+}
+
+template <typename C> __device__ __forceinline__ C dto(double2 v);
+template <> __device__ __forceinline__ float2 dto<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <> __device__ __forceinline__ double2 dto<double2>(double2 v) { return v; }
+
+struct RegionT {      // per-region data of a transformer solve
+  double dz, er, ei, tx, ty;
+  int klass;          // 0 k-space, 1 pixel (disk), 2 pixel (air, 1D propagator), 3 field
+  int col;            // column block of the region in its class GEMM
+};
+
+// ---- setup kernels --------------------------------------------------------
+// W[mm'][o] = scale * sum_{k in orbit o} conj(U_m(k)) Phi_m'(k)
+template <typename C>
+__global__ void k_build_w(C* W, const double2* U, const double2* Phi, const int* members, int K, int msz,
+                          int nm, int npix, double scale) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mm = blockIdx.y;
+  if (o >= K) return;
+  const int m = mm / nm, mp = mm % nm;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int q = 0; q < msz; ++q) {
+    const int k = members[(size_t)o * msz + q];
+    if (k < 0) break;
+    const double2 u = U[(size_t)m * npix + k], p = Phi[(size_t)mp * npix + k];
+    acc.x += u.x * p.x + u.y * p.y;
+    acc.y += u.x * p.y - u.y * p.x;
+  }
+  W[(size_t)mm * K + o] = dto<C>(make_double2(acc.x * scale, acc.y * scale));
+}
+
+// V[mm'][s] = conj(Psi_m(x_s)) Psi_m'(x_s) over the support pixels
+template <typename C>
+__global__ void k_build_v(C* V, const double2* pat, const int* supp, int Kd, int nm, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mm = blockIdx.y;
+  if (s >= Kd) return;
+  const int m = mm / nm, mp = mm % nm;
+  const int x = supp[s];
+  const double2 a = pat[(size_t)m * npix + x], b = pat[(size_t)mp * npix + x];
+  V[(size_t)mm * Kd + s] = dto<C>(make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x));
+}
+
+// D[o][f*npar + p] = exp(-i sqrt(k0^2 - kx^2 - ky^2) dz) at the orbit representative
+template <typename C>
+__global__ void k_build_d(C* D, const int2* rep, int K, const double* freqs, int nf, const RegionT* regs,
+                          const int* par_regions, int npar, const double* kX, const double* kY) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;   // f * npar + p
+  if (o >= K) return;
+  const int f = c / npar, p = c % npar;
+  const RegionT g = regs[par_regions[p]];
+  const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
+  const int2 sr = rep[o];
+  const double kx = kX[sr.x], ky = kY[sr.y];
+  const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+  const double re = (k0sq.x - kx * kx) - ky * ky;
+  const double2 kz = dsqrt_c(re, k0sq.y);
+  D[(size_t)o * (nf * npar) + c] = dto<C>(dexp_c(kz.y * g.dz, -kz.x * g.dz));
+}
+
+// E[s][f*npix_regions + q]: tilt/surface phase of pixel class regions
+template <typename C>
+__global__ void k_build_e(C* E, const int* supp, int Kd, const double* freqs, int nf, const RegionT* regs,
+                          const int* pix_regions, int npx, const double* X, const double* Y, int nx,
+                          const double2* surf, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (s >= Kd) return;
+  const int f = c / npx, q = c % npx;
+  const int reg = pix_regions[q];
+  const RegionT g = regs[reg];
+  const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
+  double2 v;
+  if (g.klass == 2) {
+    v = dexp_c(k0.y * g.dz, -k0.x * g.dz);   // propagator1D: exp(-i k0 dz)
+  } else {
+    const int x = supp[s] % nx, y = supp[s] / nx;
+    const double2 a = dexp_c(k0.y * g.tx * X[x], -k0.x * g.tx * X[x]);
+    const double2 b = dexp_c(k0.y * g.ty * Y[y], -k0.x * g.ty * Y[y]);
+    v = bf::cmul(a, b);
+    if (surf) {
+      const double2 sv = surf[(size_t)reg * npix + supp[s]];
+      const double re = k0.x * sv.x - k0.y * sv.y, im = k0.x * sv.y + k0.y * sv.x;
+      v = bf::cmul(v, dexp_c(im, -re));
+    }
+  }
+  E[(size_t)s * (nf * npx) + c] = dto<C>(v);
+}
+
+// P[f][j][m][m'] from a class GEMM output G[mm'][f*ncols + col]; pixel-class
+// disk regions get the propagation diag(exp(-i kz_m dz)) from the left.
+template <typename C>
+__global__ void k_scatter_p(C* P, const C* Gm, int nf, int ncols, const RegionT* regs, const int* cls_regions,
+                            int nd, int nm, const double* freqs, const double2* kt, int left_diag) {
+  const int mm = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.y;
+  if (mm >= nm * nm) return;
+  const int f = c / ncols, q = c % ncols;
+  const int j = cls_regions[q];
+  const RegionT g = regs[j];
+  C v = Gm[(size_t)mm * (nf * ncols) + c];
+  if (left_diag && g.klass == 1) {
+    const int m = mm / nm;
+    const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
+    const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+    const double2 t = kt[m];
+    const double2 ktsq = make_double2(t.x * t.x - t.y * t.y, t.x * t.y + t.y * t.x);
+    const double2 kz = dsqrt_c(k0sq.x - ktsq.x, k0sq.y - ktsq.y);
+    v = bf::cmul(dto<C>(dexp_c(kz.y * g.dz, -kz.x * g.dz)), v);
+  }
+  P[(((size_t)f * nd + j) * nm) * nm + mm] = v;
+}
+
+// field class: P[m][m'] = sum_x conj(Psi_m(x)) Q[m'][x]
+template <typename C>
+__global__ void k_overlap(C* P, const double2* pat, const C* Q, int nm, int npix) {
+  const int mm = blockIdx.x;
+  const int m = mm / nm, mp = mm % nm;
+  __shared__ double2 red[256];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int x = threadIdx.x; x < npix; x += blockDim.x) {
+    const double2 a = pat[(size_t)m * npix + x];
+    const double2 b = bf::to_d(Q[(size_t)mp * npix + x]);
+    acc.x += a.x * b.x + a.y * b.y;
+    acc.y += a.x * b.y - a.y * b.x;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x].x += red[threadIdx.x + s].x;
+      red[threadIdx.x].y += red[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) P[mm] = dto<C>(red[0]);
+}
+
+template <typename C>
+__global__ void k_copy_modes(C* out, const double2* pat, int nm, int npix, int reps) {
+  const size_t total = (size_t)reps * nm * npix;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = dto<C>(pat[i % ((size_t)nm * npix)]);
+}
+
+// ---- batched inversion: Pinv[f][j] = inv(P[f][j]), j in [j0, nd) -----------
+template <typename C>
+__global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int j0, int nm) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  C* W = reinterpret_cast<C*>(sm);
+  double* red_v = reinterpret_cast<double*>(W + 2 * nm * nm);
+  int* red_i = reinterpret_cast<int*>(red_v + 256);
+  const int f = blockIdx.y, j = j0 + blockIdx.x;
+  const size_t off = (((size_t)f * nd + j) * nm) * nm;
+  C* M = Pinv + off;
+  for (int e = threadIdx.x; e < nm * nm; e += blockDim.x) M[e] = P[off + e];
+  __syncthreads();
+  bf::cta_invert(M, W, nm, nullptr, red_v, red_i);
+}
+
+// ---- the chain: one CTA per frequency ---------------------------------------
+struct ChainRegion {
+  double2 a, b, inv2n;   // G = (1/(2 n_r)) [[a I, b I], [b I, a I]]
+  double2 S;             // axion S factor of the step
+};
+
+template <typename C>
+__global__ void __launch_bounds__(256) k_chain(const C* P, const C* Pinv, const ChainRegion* cr, int nd,
+                                               int nm, const double2* emit, C* T21g, C* T22g,
+                                               double2* axg) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  C* U = reinterpret_cast<C*>(sm);
+  C* V = U + nm * nm;
+  double2* ax = reinterpret_cast<double2*>(V + nm * nm);
+  double2* em = ax + nm;
+  const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  C* T21 = T21g + (size_t)f * nm * nm;
+  C* T22 = T22g + (size_t)f * nm * nm;
+  for (int e = tid; e < nm * nm; e += nt) {
+    T21[e] = dto<C>(make_double2(0.0, 0.0));
+    T22[e] = dto<C>(make_double2((e / nm) == (e % nm) ? 1.0 : 0.0, 0.0));
+  }
+  for (int m = tid; m < nm; m += nt) {
+    ax[m] = make_double2(0.0, 0.0);
+    em[m] = emit[m];
+  }
+  __syncthreads();
+  for (int j = 1; j < nd; ++j) {
+    const ChainRegion g = cr[j];
+    // axion_beam += S (T21 + T22) emit   (uses T of the previous step)
+    for (int m = tid; m < nm; m += nt) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int k = 0; k < nm; ++k) {
+        const double2 t = bf::to_d(bf::cadd(T21[m * nm + k], T22[m * nm + k]));
+        acc = bf::cadd(acc, bf::cmul(t, em[k]));
+      }
+      ax[m] = bf::cadd(ax[m], bf::cmul(g.S, acc));
+    }
+    // U = a T21 + b T22, V = b T21 + a T22
+    const C a = dto<C>(g.a), b = dto<C>(g.b), s = dto<C>(g.inv2n);
+    for (int e = tid; e < nm * nm; e += nt) {
+      const C t1 = T21[e], t2 = T22[e];
+      U[e] = bf::cadd(bf::cmul(a, t1), bf::cmul(b, t2));
+      V[e] = bf::cadd(bf::cmul(b, t1), bf::cmul(a, t2));
+    }
+    __syncthreads();
+    const C* Pj = P + (((size_t)f * nd + j) * nm) * nm;
+    const C* Qj = Pinv + (((size_t)f * nd + j) * nm) * nm;
+    // T21 = s U P, T22 = s V Pinv
+    for (int e = tid; e < nm * nm; e += nt) {
+      const int r = e / nm, c = e % nm;
+      C acc1 = dto<C>(make_double2(0.0, 0.0)), acc2 = acc1;
+      for (int k = 0; k < nm; ++k) {
+        const C u = U[r * nm + k], v = V[r * nm + k];
+        const C p = Pj[k * nm + c], q = Qj[k * nm + c];
+        acc1.x += u.x * p.x - u.y * p.y;
+        acc1.y += u.x * p.y + u.y * p.x;
+        acc2.x += v.x * q.x - v.y * q.y;
+        acc2.y += v.x * q.y + v.y * q.x;
+      }
+      T21[e] = bf::cmul(s, acc1);
+      T22[e] = bf::cmul(s, acc2);
+    }
+    __syncthreads();
+  }
+  for (int m = tid; m < nm; m += nt) axg[(size_t)f * nm + m] = ax[m];
+}
+
+// ---- FP64 boundary solve: boost = -T22 \ ax, refl = -T22 \ (T21 reflect) ----
+template <typename C>
+__global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22g, const double2* axg,
+                                                     const double2* reflect, int nm, double2* boost,
+                                                     double2* refl, double* beta2) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  const int w = nm + 2;
+  double2* A = reinterpret_cast<double2*>(sm);   // [nm][nm + 2]
+  double* red_v = reinterpret_cast<double*>(A + nm * w);
+  int* red_i = reinterpret_cast<int*>(red_v + 256);
+  const C* T21 = T21g + (size_t)f * nm * nm;
+  const C* T22 = T22g + (size_t)f * nm * nm;
+  for (int e = tid; e < nm * nm; e += nt) A[(e / nm) * w + (e % nm)] = bf::to_d(T22[e]);
+  for (int m = tid; m < nm; m += nt) {
+    A[m * w + nm] = axg[(size_t)f * nm + m];
+    double2 acc = make_double2(0.0, 0.0);
+    if (reflect)
+      for (int k = 0; k < nm; ++k) acc = bf::cadd(acc, bf::cmul(bf::to_d(T21[m * nm + k]), reflect[k]));
+    A[m * w + nm + 1] = acc;
+  }
+  __syncthreads();
+  // Gaussian elimination with partial pivoting (LAPACK getrf/getrs order)
+  for (int c = 0; c < nm; ++c) {
+    double best = -1.0;
+    int bi = c;
+    for (int r = c + tid; r < nm; r += nt) {
+      const double v = A[r * w + c].x * A[r * w + c].x + A[r * w + c].y * A[r * w + c].y;
+      if (v > best) { best = v; bi = r; }
+    }
+    red_v[tid] = best;
+    red_i[tid] = bi;
+    __syncthreads();
+    for (int s = nt / 2; s > 0; s >>= 1) {
+      if (tid < s && (red_v[tid + s] > red_v[tid] || (red_v[tid + s] == red_v[tid] && red_i[tid + s] < red_i[tid]))) {
+        red_v[tid] = red_v[tid + s];
+        red_i[tid] = red_i[tid + s];
+      }
+      __syncthreads();
+    }
+    const int p = red_i[0];
+    if (p != c)
+      for (int k = tid; k < w; k += nt) {
+        double2 t = A[c * w + k];
+        A[c * w + k] = A[p * w + k];
+        A[p * w + k] = t;
+      }
+    __syncthreads();
+    const double2 piv = A[c * w + c];
+    for (int e = tid; e < (nm - c - 1) * (w - c); e += nt) {
+      const int r = c + 1 + e / (w - c), k = c + e % (w - c);
+      if (k == c) continue;
+      const double d = piv.x * piv.x + piv.y * piv.y;
+      const double2 l = A[r * w + c];
+      const double2 fac = make_double2((l.x * piv.x + l.y * piv.y) / d, (l.y * piv.x - l.x * piv.y) / d);
+      A[r * w + k] = bf::csub(A[r * w + k], bf::cmul(fac, A[c * w + k]));
+    }
+    __syncthreads();
+    for (int r = c + 1 + tid; r < nm; r += nt) A[r * w + c] = make_double2(0.0, 0.0);
+    __syncthreads();
+  }
+  // back substitution for both right-hand sides (serial per column, small)
+  if (tid < 2) {
+    const int col = nm + tid;
+    for (int r = nm - 1; r >= 0; --r) {
+      double2 acc = A[r * w + col];
+      for (int k = r + 1; k < nm; ++k) acc = bf::csub(acc, bf::cmul(A[r * w + k], A[k * w + col]));
+      const double2 piv = A[r * w + r];
+      const double d = piv.x * piv.x + piv.y * piv.y;
+      A[r * w + col] = make_double2((acc.x * piv.x + acc.y * piv.y) / d, (acc.y * piv.x - acc.x * piv.y) / d);
+    }
+  }
+  __syncthreads();
+  for (int m = tid; m < nm; m += nt) {
+    const double2 x = A[m * w + nm];
+    boost[(size_t)f * nm + m] = make_double2(-x.x, -x.y);
+    if (refl) {
+      const double2 y = A[m * w + nm + 1];
+      refl[(size_t)f * nm + m] = make_double2(-y.x, -y.y);
+    }
+  }
+  if (tid == 0 && beta2) {
+    double s = 0.0;
+    for (int m = 0; m < nm; ++m) {
+      const double2 x = A[m * w + nm];
+      s += x.x * x.x + x.y * x.y;
+    }
+    beta2[f] = s;
+  }
+}
+
+// axion_induced_modes / field2modes: c_m = sum conj(Psi_m) B_hat
+__global__ void k_project(double2* out, const double2* pat, const double2* Bn, int nm, int npix) {
+  const int m = blockIdx.x;
+  __shared__ double2 red[256];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int x = threadIdx.x; x < npix; x += blockDim.x) {
+    const double2 a = pat[(size_t)m * npix + x], b = Bn[x];
+    acc.x += a.x * b.x + a.y * b.y;
+    acc.y += a.x * b.y - a.y * b.x;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x].x += red[threadIdx.x + s].x;
+      red[threadIdx.x].y += red[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[m] = red[0];
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+static unsigned long long g_modes_id = 0;
+
+const cd* as_cdp(const double* p) { return reinterpret_cast<const cd*>(p); }
+
+int modes_upload(bf_handle* h, bf_modes* m) {
+  TCKS(bf_dalloc(h, (void**)&m->d_pat, sizeof(cd) * m->pat.size()));
+  TCK(cudaMemcpyAsync(m->d_pat, m->pat.data(), sizeof(cd) * m->pat.size(), cudaMemcpyHostToDevice, h->stream()));
+  TCK(cudaStreamSynchronize(h->stream()));
+  return BF_OK;
+}
+
+unsigned blocks_for(size_t n) { return (unsigned)std::max<size_t>(1, (n + 255) / 256); }
+
+}  // namespace
+
+// Transformer setup cached per (stack, modes, precision): W, V and the orbit
+// and support tables.
+struct TfCache {
+  unsigned long long modes_id = 0, geo_version = ~0ull;
+  int fp64 = -1;
+  int K = 0, msz = 0, Kd = 0, nm = 0;
+  DBuf W, V, rep, supp, U, Phi, members;
+  std::vector<int2> rep_h;
+};
+
+static void tf_cache_delete(void* p) { delete static_cast<TfCache*>(p); }
+
+static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache** out) {
+  if (!s->tf_cache) {
+    s->tf_cache = new TfCache();
+    s->tf_cache_delete = tf_cache_delete;
+  }
+  TfCache& c = *static_cast<TfCache*>(s->tf_cache);
+  *out = &c;
+  if (c.modes_id == md->id && c.geo_version == s->geo_version && c.fp64 == (int)fp64) return BF_OK;
+  cudaStream_t st = h->stream();
+  const int nx = s->nx, ny = s->ny, nm = md->nm;
+  const size_t npix = (size_t)nx * ny;
+  const size_t csz = fp64 ? 16 : 8;
+  c.nm = nm;
+  // orbits of the phasor symmetry in shifted (kX, kY) index space
+  auto antisym = [](const std::vector<double>& k) {
+    const size_t n = k.size();
+    double mx = 0;
+    for (double v : k) mx = std::max(mx, fabs(v));
+    for (size_t i = 0; i < n; ++i)
+      if (fabs(k[i] + k[n - 1 - i]) > 1e-12 * std::max(1.0, mx)) return false;
+    return true;
+  };
+  const bool fx = antisym(s->kX), fy = antisym(s->kY);
+  bool swp = nx == ny;
+  if (swp)
+    for (int i = 0; i < nx; ++i)
+      if (fabs(s->kX[i] - s->kY[i]) > 1e-12 * std::max(1.0, fabs(s->kX[i]))) { swp = false; break; }
+  std::map<std::pair<int, int>, int> orbit_of;
+  std::vector<std::vector<int>> mem;
+  c.rep_h.clear();
+  for (int ky = 0; ky < ny; ++ky)
+    for (int kx = 0; kx < nx; ++kx) {
+      const int sx = (kx + nx / 2) % nx, sy = (ky + ny / 2) % ny;   // fftshift position
+      int a = fx ? std::min(sx, nx - 1 - sx) : sx;
+      int b = fy ? std::min(sy, ny - 1 - sy) : sy;
+      if (swp && b < a) std::swap(a, b);
+      auto key = std::make_pair(a, b);
+      auto it = orbit_of.find(key);
+      int o;
+      if (it == orbit_of.end()) {
+        o = (int)mem.size();
+        orbit_of[key] = o;
+        mem.emplace_back();
+        c.rep_h.push_back(make_int2(sx, sy));
+      } else {
+        o = it->second;
+      }
+      mem[o].push_back(ky * nx + kx);
+    }
+  c.K = (int)mem.size();
+  c.msz = 1;
+  for (auto& v : mem) c.msz = std::max<int>(c.msz, (int)v.size());
+  std::vector<int> members((size_t)c.K * c.msz, -1);
+  for (int o = 0; o < c.K; ++o)
+    for (size_t q = 0; q < mem[o].size(); ++q) members[(size_t)o * c.msz + q] = mem[o][q];
+  TCKS(c.members.alloc(h, sizeof(int) * members.size()));
+  TCK(cudaMemcpyAsync(c.members.p, members.data(), sizeof(int) * members.size(), cudaMemcpyHostToDevice, st));
+  TCKS(c.rep.alloc(h, sizeof(int2) * c.K));
+  TCK(cudaMemcpyAsync(c.rep.p, c.rep_h.data(), sizeof(int2) * c.K, cudaMemcpyHostToDevice, st));
+  // U = FFT(Psi), Phi = FFT(mask Psi), FP64
+  TCKS(c.U.alloc(h, sizeof(double2) * nm * npix));
+  TCKS(c.Phi.alloc(h, sizeof(double2) * nm * npix));
+  TCK(cudaMemcpyAsync(c.U.p, md->d_pat, sizeof(double2) * nm * npix, cudaMemcpyDeviceToDevice, st));
+  TCK(cudaMemcpyAsync(c.Phi.p, md->d_pat, sizeof(double2) * nm * npix, cudaMemcpyDeviceToDevice, st));
+  int e = bf::launch_mul_mask(true, c.Phi.p, nm, nx, ny, s->d_mask_full, st);
+  if (!e) e = bf::launch_line_dft(true, c.U.p, nm, nx, ny, 0, 0, st);
+  if (!e) e = bf::launch_line_dft(true, c.U.p, nm, nx, ny, 1, 0, st);
+  if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 0, 0, st);
+  if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 1, 0, st);
+  if (e) return bf_fail(h, BF_ERR_CUDA, "mode FFTs failed");
+  TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+  {
+    dim3 grid(blocks_for(c.K), nm * nm);
+    const double scale = 1.0 / ((double)nx * (double)ny);
+    if (fp64) { bf::note_launch(); k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
+    else { bf::note_launch(); k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
+    TCK(cudaGetLastError());
+  }
+  // support pixels (any mode non-zero) and V
+  std::vector<int> supp;
+  for (size_t x = 0; x < npix; ++x) {
+    bool nz = false;
+    for (int m = 0; m < nm && !nz; ++m) nz = md->pat[(size_t)m * npix + x] != cd(0.0, 0.0);
+    if (nz) supp.push_back((int)x);
+  }
+  if (supp.empty()) supp.push_back(0);
+  c.Kd = (int)supp.size();
+  TCKS(c.supp.alloc(h, sizeof(int) * supp.size()));
+  TCK(cudaMemcpyAsync(c.supp.p, supp.data(), sizeof(int) * supp.size(), cudaMemcpyHostToDevice, st));
+  TCKS(c.V.alloc(h, csz * (size_t)nm * nm * c.Kd));
+  {
+    dim3 grid(blocks_for(c.Kd), nm * nm);
+    if (fp64) { bf::note_launch(); k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
+    else { bf::note_launch(); k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
+    TCK(cudaGetLastError());
+  }
+  TCK(cudaStreamSynchronize(st));
+  c.U.release();
+  c.Phi.release();
+  c.modes_id = md->id;
+  c.geo_version = s->geo_version;
+  c.fp64 = fp64;
+  return BF_OK;
+}
+
+static double g_tf_gemm_flops = 0.0;   // executed real flops of the class GEMMs of the last solve
+
+static void tf_mark(bf_handle* h, int i) {
+  if (!h->profiling) return;
+  if (!h->ev[i]) cudaEventCreate(&h->ev[i]);
+  cudaEventRecord(h->ev[i], h->stream());
+}
+
+template <typename C>
+static int launch_gemm(bf_handle* h, const C* A, const C* B, C* Cm, int R, int K, int N) {
+  g_tf_gemm_flops += 8.0 * (double)R * (double)K * (double)N;
+  dim3 grid((N + 63) / 64, (R + 63) / 64);
+  bf::note_launch();
+  bf::k_cgemm<C><<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
+  TCK(cudaGetLastError());
+  return BF_OK;
+}
+
+// Propagation matrices of regions [j0, nd) for all frequencies into P[f][j][m][m'].
+template <typename C>
+static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
+                                   const std::vector<RegionT>& regs, int j0, int nf,
+                                   const std::vector<double>& freqs, int prop_kind, bool fp64, DBuf& P) {
+  cudaStream_t st = h->stream();
+  const int nd = s->nd, nm = md->nm, nx = s->nx, ny = s->ny;
+  const size_t npix = (size_t)nx * ny;
+  std::vector<int> kreg, preg, freg;
+  for (int j = j0; j < nd; ++j) {
+    if (regs[j].klass == 0) kreg.push_back(j);
+    else if (regs[j].klass == 3) freg.push_back(j);
+    else preg.push_back(j);
+  }
+  TCKS(P.ensure(h, sizeof(C) * (size_t)nf * nd * nm * nm));
+  DBuf d_regs, d_freq, d_kt, d_list;
+  TCKS(d_regs.alloc(h, sizeof(RegionT) * regs.size()));
+  TCK(cudaMemcpyAsync(d_regs.p, regs.data(), sizeof(RegionT) * regs.size(), cudaMemcpyHostToDevice, st));
+  TCKS(d_freq.alloc(h, sizeof(double) * nf));
+  TCK(cudaMemcpyAsync(d_freq.p, freqs.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, st));
+  TCKS(d_kt.alloc(h, sizeof(cd) * nm));
+  TCK(cudaMemcpyAsync(d_kt.p, md->kt.data(), sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
+  const RegionT* dr = d_regs.as<RegionT>();
+  // k-space class: one GEMM W * D
+  if (!kreg.empty()) {
+    const int npar = (int)kreg.size();
+    DBuf lst, D, G;
+    TCKS(lst.alloc(h, sizeof(int) * npar));
+    TCK(cudaMemcpyAsync(lst.p, kreg.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
+    const int ncol = nf * npar;
+    TCKS(D.alloc(h, sizeof(C) * (size_t)c.K * ncol));
+    TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
+    dim3 gd(blocks_for(c.K), ncol);
+    bf::note_launch();
+    k_build_d<C><<<gd, 256, 0, st>>>(D.as<C>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, dr, lst.as<int>(),
+                                     npar, s->dkX, s->dkY);
+    TCK(cudaGetLastError());
+    TCKS(launch_gemm<C>(h, c.W.as<C>(), D.as<C>(), G.as<C>(), nm * nm, c.K, ncol));
+    dim3 gs(blocks_for((size_t)nm * nm), ncol);
+    bf::note_launch();
+    k_scatter_p<C><<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+                                       d_kt.as<double2>(), 0);
+    TCK(cudaGetLastError());
+    TCK(cudaStreamSynchronize(st));
+  }
+  // pixel class: one GEMM V * E
+  if (!preg.empty()) {
+    const int npx = (int)preg.size();
+    DBuf lst, E, G;
+    TCKS(lst.alloc(h, sizeof(int) * npx));
+    TCK(cudaMemcpyAsync(lst.p, preg.data(), sizeof(int) * npx, cudaMemcpyHostToDevice, st));
+    const int ncol = nf * npx;
+    TCKS(E.alloc(h, sizeof(C) * (size_t)c.Kd * ncol));
+    TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
+    dim3 ge(blocks_for(c.Kd), ncol);
+    bf::note_launch();
+    k_build_e<C><<<ge, 256, 0, st>>>(E.as<C>(), c.supp.as<int>(), c.Kd, d_freq.as<double>(), nf, dr, lst.as<int>(),
+                                     npx, s->dX, s->dY, nx, s->d_surf, (int)npix);
+    TCK(cudaGetLastError());
+    TCKS(launch_gemm<C>(h, c.V.as<C>(), E.as<C>(), G.as<C>(), nm * nm, c.Kd, ncol));
+    dim3 gs(blocks_for((size_t)nm * nm), ncol);
+    bf::note_launch();
+    k_scatter_p<C><<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+                                       d_kt.as<double2>(), 1);
+    TCK(cudaGetLastError());
+    TCK(cudaStreamSynchronize(st));
+  }
+  // field class: propagate every mode, then overlap
+  if (!freg.empty()) {
+    DBuf Q, tmp, fr;
+    TCKS(Q.alloc(h, sizeof(C) * (size_t)nm * npix));
+    TCKS(tmp.alloc(h, sizeof(C) * (size_t)nm * npix));
+    TCKS(fr.alloc(h, sizeof(double) * nm));
+    const int kind = prop_kind == BF_PROP_NOTILTS ? BF_PROP_NOTILTS : prop_kind;
+    for (int f = 0; f < nf; ++f) {
+      std::vector<double> fv(nm, freqs[f]);
+      TCK(cudaMemcpyAsync(fr.p, fv.data(), sizeof(double) * nm, cudaMemcpyHostToDevice, st));
+      for (int j : freg) {
+        bf::note_launch();
+        k_copy_modes<C><<<blocks_for((size_t)nm * npix), 256, 0, st>>>(Q.as<C>(), md->d_pat, nm, (int)npix, 1);
+        TCK(cudaGetLastError());
+        TCKS(bf_general_prop(h, s, kind, fp64, Q.p, tmp.p, nm, fr.as<double>(), j));
+        bf::note_launch();
+        k_overlap<C><<<nm * nm, 256, 0, st>>>(P.as<C>() + (((size_t)f * nd + j) * nm) * nm, md->d_pat, Q.as<C>(), nm,
+                                              (int)npix);
+        TCK(cudaGetLastError());
+      }
+      TCK(cudaStreamSynchronize(st));
+    }
+  }
+  return BF_OK;
+}
+
+static int classify(bf_handle* h, const bf_stack* s, int prop_kind, const std::vector<cd>& eps,
+                    std::vector<RegionT>& regs) {
+  const int nd = s->nd;
+  regs.resize(nd);
+  for (int j = 0; j < nd; ++j) {
+    RegionT& r = regs[j];
+    r.dz = s->distance[j];
+    r.er = eps[j].real();
+    r.ei = eps[j].imag();
+    r.tx = s->tilt_x[j];
+    r.ty = s->tilt_y[j];
+    const bool air = eps[j].real() == 1.0;   // is_air = real(eps) == 1 (transformer.jl:174)
+    const bool flat = (r.tx == 0.0 && r.ty == 0.0 && !(s->d_surf && s->surf_nonzero[j])) || prop_kind == BF_PROP_NOTILTS;
+    if (!air) r.klass = 1;
+    else if (prop_kind == BF_PROP_1D) r.klass = 2;
+    else if ((prop_kind == BF_PROP_3D || prop_kind == BF_PROP_NOTILTS) && flat) r.klass = 0;
+    else r.klass = 3;
+    r.col = 0;
+  }
+  (void)h;
+  return BF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" int bf_modes_create(bf_handle* h, int nx, int ny, const double* X, const double* Y, int three_dim,
+                               int M, int L, double diskR, const double* pattern_input, const double* kT,
+                               bf_modes** out) {
+  if (!h || !out) return BF_ERR_INVALID;
+  *out = nullptr;
+  if (nx < 1 || ny < 1 || !X || !Y) return bf_fail(h, BF_ERR_INVALID, "empty grid");
+  std::unique_ptr<bf_modes> m(new bf_modes());
+  m->nx = nx; m->ny = ny;
+  m->X.assign(X, X + nx);
+  m->Y.assign(Y, Y + ny);
+  const size_t npix = (size_t)nx * ny;
+  if (!three_dim) {
+    // SeedModes(ThreeDim=false): one mode of ones, kt = 0 (transformer.jl:58-63)
+    m->M = 1; m->L = 0; m->nm = 1;
+    m->pat.assign(npix, cd(1.0, 0.0));
+    m->kt.assign(1, cd(0.0, 0.0));
+  } else {
+    if (M < 1 || L < 0) return bf_fail(h, BF_ERR_INVALID, "Mmax >= 1 and Lmax >= 0 required");
+    m->M = M; m->L = L; m->nm = M * (2 * L + 1);
+    if (pattern_input) {
+      // pattern_input (M, 2L+1, nx, ny, 1) column-major, kT (M, 2L+1)
+      if (!kT) return bf_fail(h, BF_ERR_INVALID, "you have to define kTs as well when putting in an input pattern");
+      const int nl = 2 * L + 1;
+      m->pat.assign((size_t)m->nm * npix, cd(0, 0));
+      m->kt.assign(m->nm, cd(0, 0));
+      const cd* pi = as_cdp(pattern_input);
+      const cd* kt = as_cdp(kT);
+      for (int mm = 0; mm < M; ++mm)
+        for (int l = 0; l < nl; ++l) {
+          const int k = mm * nl + l;
+          m->kt[k] = kt[mm + (size_t)M * l];
+          for (int y = 0; y < ny; ++y)
+            for (int x = 0; x < nx; ++x)
+              m->pat[(size_t)k * npix + (size_t)y * nx + x] =
+                  pi[mm + (size_t)M * (l + (size_t)nl * (x + (size_t)nx * y))];
+        }
+    } else {
+      std::vector<double> Xv(X, X + nx), Yv(Y, Y + ny);
+      bfmodes::seed_modes(M, L, Xv, Yv, diskR, m->pat, m->kt);
+    }
+  }
+  if (m->nm > 64) return bf_fail(h, BF_ERR_UNSUPPORTED, "at most 64 modes are supported");
+  TCK(cudaSetDevice(h->device));
+  TCKS(modes_upload(h, m.get()));
+  m->id = ++g_modes_id;
+  *out = m.release();
+  return BF_OK;
+}
+
+extern "C" int bf_modes_destroy(bf_handle* h, bf_modes* m) {
+  if (!h || !m) return BF_ERR_INVALID;
+  cudaStreamSynchronize(h->stream());
+  bf_dfree(h, m->d_pat);
+  delete m;
+  return BF_OK;
+}
+
+extern "C" int bf_modes_get(bf_handle* h, const bf_modes* m, int* nm_out, double* patterns, double* kt) {
+  if (!h || !m) return BF_ERR_INVALID;
+  if (nm_out) *nm_out = m->nm;
+  const size_t npix = (size_t)m->nx * m->ny;
+  const int nl = 2 * m->L + 1;
+  if (patterns) {
+    // (M, 2L+1, nx, ny, 1) column-major
+    cd* o = reinterpret_cast<cd*>(patterns);
+    for (int mm = 0; mm < m->M; ++mm)
+      for (int l = 0; l < nl; ++l)
+        for (int y = 0; y < m->ny; ++y)
+          for (int x = 0; x < m->nx; ++x)
+            o[mm + (size_t)m->M * (l + (size_t)nl * (x + (size_t)m->nx * y))] =
+                m->pat[(size_t)(mm * nl + l) * npix + (size_t)y * m->nx + x];
+  }
+  if (kt) {
+    cd* o = reinterpret_cast<cd*>(kt);
+    for (int mm = 0; mm < m->M; ++mm)
+      for (int l = 0; l < nl; ++l) o[mm + (size_t)m->M * l] = m->kt[mm * nl + l];
+  }
+  return BF_OK;
+}
+
+extern "C" int bf_axion_induced_modes(bf_handle* h, const bf_modes* m, const double* B, double velocity_x,
+                                      double diskR, double f, double* out) {
+  if (!h || !m || !out) return BF_ERR_INVALID;
+  const double* X = m->X.data();
+  const double* Y = m->Y.data();
+  TCK(cudaSetDevice(h->device));
+  const int nx = m->nx, ny = m->ny;
+  const size_t npix = (size_t)nx * ny;
+  std::vector<cd> b(npix, cd(1.0, 0.0));
+  if (B) b.assign(as_cdp(B), as_cdp(B) + npix);
+  if (velocity_x != 0.0) {
+    const double ma = 2.0 * M_PI / (kC / f);
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const double a = -ma * (-velocity_x) * X[x];
+        b[(size_t)y * nx + x] *= cd(std::cos(a), std::sin(a));
+      }
+  }
+  double n2 = 0.0;
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x) {
+      const double xx = X[x] * X[x];
+      const double yy = Y[y] * Y[y];
+      if (!(std::sqrt(xx + yy) <= diskR)) b[(size_t)y * nx + x] = 0.0;
+      n2 += std::norm(b[(size_t)y * nx + x]);
+    }
+  const double nn = std::sqrt(n2);
+  for (auto& v : b) v /= nn;
+  DBuf db, dout;
+  TCKS(db.alloc(h, sizeof(cd) * npix));
+  TCK(cudaMemcpyAsync(db.p, b.data(), sizeof(cd) * npix, cudaMemcpyHostToDevice, h->stream()));
+  TCKS(dout.alloc(h, sizeof(cd) * m->nm));
+  bf::note_launch();
+  k_project<<<m->nm, 256, 0, h->stream()>>>(dout.as<double2>(), m->d_pat, db.as<double2>(), m->nm, (int)npix);
+  TCK(cudaGetLastError());
+  TCK(cudaMemcpyAsync(out, dout.p, sizeof(cd) * m->nm, cudaMemcpyDeviceToHost, h->stream()));
+  TCK(cudaStreamSynchronize(h->stream()));
+  return BF_OK;
+}
+
+extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coeffs, double* field) {
+  if (!h || !m || !coeffs || !field) return BF_ERR_INVALID;
+  const size_t npix = (size_t)m->nx * m->ny;
+  std::vector<cd> acc(npix, cd(0, 0));
+  const cd* c = as_cdp(coeffs);
+  for (int k = 0; k < m->nm; ++k)
+    for (size_t i = 0; i < npix; ++i) acc[i] += c[k] * m->pat[(size_t)k * npix + i];
+  std::copy(acc.begin(), acc.end(), reinterpret_cast<cd*>(field));
+  return BF_OK;
+}
+
+template <typename C>
+static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
+                  const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
+                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm) {
+  cudaStream_t st = h->stream();
+  const int nd = s->nd, nm = md->nm;
+  std::vector<cd> eps(s->eps);
+  if (mirror_1e30)
+    for (auto& e : eps)
+      if (std::isnan(e.real()) || std::isnan(e.imag())) e = cd(1e30, 0.0);   // transformer.jl:289
+  std::vector<RegionT> regs;
+  classify(h, s, prop_kind, eps, regs);
+  std::vector<double> fv(freqs, freqs + nf);
+  DBuf P, Pinv;
+  g_tf_gemm_flops = 0.0;
+  tf_mark(h, 0);
+  const unsigned long long l0 = bf::launch_count();
+  if (pm) {
+    // injected propagation matrices: [nf or 1][nd][nm][nm], each a Julia (nm, nm) column-major matrix
+    std::vector<C> hp((size_t)nf * nd * nm * nm);
+    const cd* src = as_cdp(pm);
+    for (int f = 0; f < nf; ++f)
+      for (int j = 0; j < nd; ++j) {
+        const cd* mj = src + ((size_t)(pm_per_freq ? f : 0) * nd + j) * nm * nm;
+        for (int r = 0; r < nm; ++r)
+          for (int cidx = 0; cidx < nm; ++cidx) {
+            const cd v = mj[r + (size_t)nm * cidx];
+            C o;
+            o.x = (decltype(o.x))v.real();
+            o.y = (decltype(o.x))v.imag();
+            hp[(((size_t)f * nd + j) * nm + r) * nm + cidx] = o;
+          }
+      }
+    TCKS(P.alloc(h, sizeof(C) * hp.size()));
+    TCK(cudaMemcpyAsync(P.p, hp.data(), sizeof(C) * hp.size(), cudaMemcpyHostToDevice, st));
+  } else {
+    TfCache* c = nullptr;
+    TCKS(tf_setup(h, s, md, fp64, &c));
+    TCKS(tf_propagation_matrices<C>(h, s, md, *c, regs, only_matrices ? 0 : 1, nf, fv, prop_kind, fp64, P));
+  }
+  if (only_matrices) {
+    // out_pm: [nf][nd] Julia (nm, nm) column-major matrices
+    std::vector<C> hp((size_t)nf * nd * nm * nm);
+    TCK(cudaMemcpyAsync(hp.data(), P.p, sizeof(C) * hp.size(), cudaMemcpyDeviceToHost, st));
+    TCK(cudaStreamSynchronize(st));
+    cd* o = reinterpret_cast<cd*>(out_pm);
+    for (int f = 0; f < nf; ++f)
+      for (int j = 0; j < nd; ++j)
+        for (int r = 0; r < nm; ++r)
+          for (int cidx = 0; cidx < nm; ++cidx) {
+            const C v = hp[(((size_t)f * nd + j) * nm + r) * nm + cidx];
+            o[((size_t)f * nd + j) * nm * nm + r + (size_t)nm * cidx] = cd(v.x, v.y);
+          }
+    return BF_OK;
+  }
+  tf_mark(h, 1);
+  // The inverses, the chain and the boundary solve run in FP64 for either
+  // precision: near a resonance T22 is ill-conditioned and FP32 chains lose
+  // the 1e-4 bar on beta^2 (the propagation matrices themselves may be FP32).
+  using D2 = double2;
+  DBuf P64;
+  const D2* Pd;
+  if (sizeof(C) == sizeof(D2)) {
+    Pd = reinterpret_cast<const D2*>(P.p);
+  } else {
+    TCKS(P64.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
+    if (bf::launch_convert(P.p, false, P64.p, true, (size_t)nf * nd * nm * nm, st))
+      return bf_fail(h, BF_ERR_CUDA, "convert P");
+    Pd = P64.as<D2>();
+  }
+  TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
+  {
+    const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
+    TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(nd - 1, nf);
+    bf::note_launch();
+    k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
+    TCK(cudaGetLastError());
+  }
+  // chain coefficients: step j uses n_left = sqrt(eps[j]), n_right = sqrt(eps[j-1])
+  std::vector<ChainRegion> cr(nd);
+  for (int j = 1; j < nd; ++j) {
+    const cd nl = std::sqrt(eps[j]), nr = std::sqrt(eps[j - 1]);
+    cr[j].a = make_double2((nr + nl).real(), (nr + nl).imag());
+    cr[j].b = make_double2((nr - nl).real(), (nr - nl).imag());
+    const cd inv = 1.0 / (2.0 * nr);
+    cr[j].inv2n = make_double2(inv.real(), inv.imag());
+    // axion_S_factor(n1 = sqrt(eps[j-1]), n0 = sqrt(eps[j])) = (1/n1^2 - 1/n0^2)/2
+    const cd S = (1.0 / (nr * nr) - 1.0 / (nl * nl)) / 2.0;
+    cr[j].S = make_double2(S.real(), S.imag());
+  }
+  std::vector<cd> em(nm);
+  if (emit) {
+    em.assign(as_cdp(emit), as_cdp(emit) + nm);
+  } else {
+    // default emit = axion_induced_modes(coords, modes; B=nothing, diskR) (transformer.jl:285)
+    TCKS(bf_axion_induced_modes(h, md, nullptr, 0.0, s->diskR, 10e9, reinterpret_cast<double*>(em.data())));
+  }
+  DBuf d_cr, d_em, T21, T22, ax, d_refl, boost, refl, b2;
+  TCKS(d_cr.alloc(h, sizeof(ChainRegion) * nd));
+  TCK(cudaMemcpyAsync(d_cr.p, cr.data(), sizeof(ChainRegion) * nd, cudaMemcpyHostToDevice, st));
+  TCKS(d_em.alloc(h, sizeof(cd) * nm));
+  TCK(cudaMemcpyAsync(d_em.p, em.data(), sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
+  TCKS(T21.alloc(h, sizeof(D2) * (size_t)nf * nm * nm));
+  TCKS(T22.alloc(h, sizeof(D2) * (size_t)nf * nm * nm));
+  TCKS(ax.alloc(h, sizeof(double2) * (size_t)nf * nm));
+  {
+    const size_t smem = sizeof(D2) * 2 * nm * nm + sizeof(double2) * 2 * nm;
+    TCK(cudaFuncSetAttribute(k_chain<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bf::note_launch();
+    k_chain<D2><<<nf, 256, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
+                                       T21.as<D2>(), T22.as<D2>(), ax.as<double2>());
+    TCK(cudaGetLastError());
+  }
+  if (reflect) {
+    TCKS(d_refl.alloc(h, sizeof(cd) * nm));
+    TCK(cudaMemcpyAsync(d_refl.p, reflect, sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
+  }
+  TCKS(boost.alloc(h, sizeof(cd) * (size_t)nf * nm));
+  if (reflect) TCKS(refl.alloc(h, sizeof(cd) * (size_t)nf * nm));
+  TCKS(b2.alloc(h, sizeof(double) * nf));
+  {
+    const size_t smem = sizeof(double2) * nm * (nm + 2) + 256 * (sizeof(double) + sizeof(int));
+    TCK(cudaFuncSetAttribute(k_final_solve<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bf::note_launch();
+    k_final_solve<D2><<<nf, 256, smem, st>>>(T21.as<D2>(), T22.as<D2>(), ax.as<double2>(),
+                                             reflect ? d_refl.as<double2>() : nullptr, nm, boost.as<double2>(),
+                                             reflect ? refl.as<double2>() : nullptr, b2.as<double>());
+    TCK(cudaGetLastError());
+  }
+  tf_mark(h, 2);
+  if (h->profiling) {
+    TCK(cudaEventSynchronize(h->ev[2]));
+    float t01 = 0, t12 = 0, t02 = 0;
+    cudaEventElapsedTime(&t01, h->ev[0], h->ev[1]);
+    cudaEventElapsedTime(&t12, h->ev[1], h->ev[2]);
+    cudaEventElapsedTime(&t02, h->ev[0], h->ev[2]);
+    h->prof[0] = t02;      // whole solve
+    h->prof[1] = t01;      // propagation matrices (class GEMMs)
+    h->prof[2] = t12;      // inverses, chain, boundary solve
+    h->prof[3] = 0;
+    h->prof[4] = 0;
+    h->prof[5] = (double)(bf::launch_count() - l0);
+    h->prof[6] = g_tf_gemm_flops;
+    h->prof[7] = nf;
+    h->prof_valid = 1;
+  }
+  if (out_boost) TCK(cudaMemcpyAsync(out_boost, boost.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
+  if (out_refl && reflect) TCK(cudaMemcpyAsync(out_refl, refl.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
+  if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+  TCK(cudaStreamSynchronize(st));
+  return BF_OK;
+}
+
+static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
+                    int precision) {
+  if (!h) return BF_ERR_INVALID;
+  if (!s || !md) return bf_fail(h, BF_ERR_INVALID, "null stack or modes");
+  if (md->nx != s->nx || md->ny != s->ny) return bf_fail(h, BF_ERR_INVALID, "modes and stack grids differ");
+  if (nf < 1 || !freqs) return bf_fail(h, BF_ERR_INVALID, "need at least one frequency");
+  for (int i = 0; i < nf; ++i)
+    if (!(freqs[i] > 0) || !std::isfinite(freqs[i])) return bf_fail(h, BF_ERR_INVALID, "bad frequency");
+  if (prop_kind < 0 || prop_kind > 3) return bf_fail(h, BF_ERR_INVALID, "unknown propagator kind");
+  if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED) return bf_fail(h, BF_ERR_INVALID, "unknown precision");
+  return BF_OK;
+}
+
+extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
+                              int precision, const double* emit, const double* reflect,
+                              const double* propagation_matrices, int pm_per_freq, double* out_boost,
+                              double* out_refl, double* out_beta2) {
+  TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
+  TCK(cudaSetDevice(h->device));
+  if (precision == BF_PREC_FP64)
+    return tf_run<double2>(h, s, md, nf, freqs, prop_kind, true, emit, reflect, propagation_matrices, pm_per_freq,
+                           out_boost, out_refl, out_beta2, 1, 0, nullptr);
+  return tf_run<float2>(h, s, md, nf, freqs, prop_kind, false, emit, reflect, propagation_matrices, pm_per_freq,
+                        out_boost, out_refl, out_beta2, 1, 0, nullptr);
+}
+
+extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,
+                                            int prop_kind, int precision, double* out) {
+  TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
+  if (!out) return bf_fail(h, BF_ERR_INVALID, "null output");
+  TCK(cudaSetDevice(h->device));
+  if (precision == BF_PREC_FP64)
+    return tf_run<double2>(h, s, md, nf, freqs, prop_kind, true, nullptr, nullptr, nullptr, 0, nullptr, nullptr,
+                           nullptr, 0, 1, out);
+  return tf_run<float2>(h, s, md, nf, freqs, prop_kind, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
+                        0, 1, out);
+}

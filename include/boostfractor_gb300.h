@@ -166,6 +166,49 @@ int bf_dancer(bf_handle* h, int nd, const double* distance, const double* r,
               int returnsum, int immediatesum, double beta2_scale,
               double* out, double* out_beta2);
 
+/* ---- transformer: mode basis -------------------------------------------- */
+/* SeedModes(coords; ThreeDim, Mmax=M, Lmax=L, diskR, pattern_input, kT_arr):
+ * three_dim = 0 gives one mode of ones (the 1D model); otherwise Bessel disk
+ * modes J_l(j_{|l|,m} r/R) exp(-i l phi), zero outside r > diskR, unit
+ * normalised, in the reference's flat order (m-1)(2L+1)+l+L, or the caller's
+ * pattern_input (M, 2L+1, nx, ny, 1) complex with kT (M, 2L+1) complex.
+ * At most 64 modes.  Replaces src/boost_fractor_transformer.jl:46-107. */
+int bf_modes_create(bf_handle* h, int nx, int ny, const double* X, const double* Y, int three_dim,
+                    int M, int L, double diskR, const double* pattern_input, const double* kT,
+                    bf_modes** out);
+int bf_modes_destroy(bf_handle* h, bf_modes* m);
+/* Copy the mode patterns (M, 2L+1, nx, ny, 1) and mode_kt (M, 2L+1) out
+ * (either pointer may be NULL); *nm receives M(2L+1). */
+int bf_modes_get(bf_handle* h, const bf_modes* m, int* nm, double* patterns, double* kt);
+/* Mode coefficients of the masked (r <= diskR), unit-normalised field B
+ * ((nx, ny) complex, NULL = uniform), with the axion velocity phase when
+ * velocity_x != 0; out: nm complex.  Replaces axion_induced_modes and
+ * field2modes (src/boost_fractor_transformer.jl:115-156). */
+int bf_axion_induced_modes(bf_handle* h, const bf_modes* m, const double* B, double velocity_x,
+                           double diskR, double f, double* out);
+/* Field (nx, ny) complex of nm mode coefficients.  Replaces modes2field (:161-167). */
+int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coeffs, double* field);
+
+/* ---- transformer: propagation matrices and the transfer-matrix solve ----- */
+/* Propagation (mode-mixing) matrices of every region for nf frequencies;
+ * out: nf x nd Julia (nm, nm) complex column-major matrices.  The stack's
+ * permittivities are used as given (a NaN mirror gives NaN, as in the
+ * reference).  Replaces calc_propagation_matrices / propagation_matrix
+ * (src/boost_fractor_transformer.jl:174-227, 274-280). */
+int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs,
+                                 int prop_kind, int precision, double* out);
+/* transformer for nf frequencies of one resident stack (mirror eps NaN taken
+ * as 1e30).  emit / reflect: nm complex or NULL (emit NULL = the default
+ * axion-induced modes of the stack's diskR); propagation_matrices: NULL, or
+ * (pm_per_freq ? nf : 1) x nd Julia (nm, nm) matrices to use instead of
+ * computing them.  Outputs: out_boost[f] (nm complex), out_refl[f] (nm complex,
+ * when reflect is given), out_beta2[f] = sum |boost|^2.
+ * Replaces src/boost_fractor_transformer.jl:238-359. */
+int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs,
+                   int prop_kind, int precision, const double* emit, const double* reflect,
+                   const double* propagation_matrices, int pm_per_freq, double* out_boost,
+                   double* out_refl, double* out_beta2);
+
 #ifdef __cplusplus
 }
 #endif

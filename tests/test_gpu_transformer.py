@@ -1,0 +1,149 @@
+"""GPU parity of the transformer path (mode basis, propagation matrices,
+transfer-matrix chain, FP64 boundary solve) against the CPU oracle and the
+reference's golden vectors.
+
+Tolerances: FP64 path 1e-10 relative; mixed path 1e-4 relative in beta^2.
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import bf_oracle as O
+from tests.golden import reference_goldens as G
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+FP64_TOL = 1e-10
+MIXED_BETA2_TOL = 1e-4
+DEPS = np.arange(0, 3 * math.pi, 1.0)
+
+
+@pytest.fixture(scope="module")
+def B():
+    import build as _b
+    _b.build()
+    import bfgb300
+    return bfgb300
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def _dist(d):
+    return np.array([0.0, math.pi * 3e-2 / (2 * math.pi), d * 1e-2 / (2 * math.pi), 0.0])
+
+
+def test_modes_match_oracle(B):
+    from bfgb300 import workloads as W
+    X = W.symmetric_grid(48)
+    cb = B.SeedCoordinateSystem(X=X, Y=X)
+    co = O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=4, Lmax=2, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=4, Lmax=2, diskR=0.15)
+    assert rel(mb.mode_patterns, mo.mode_patterns) < 1e-12
+    assert rel(mb.mode_kt, mo.mode_kt) < 1e-13
+
+
+def test_transformer_goldens_on_gpu(B):
+    """test/runtests.jl:122-171,217 through the GPU (FP64 path)."""
+    c = B.SeedCoordinateSystem()
+    eps = np.array([np.nan, 1, 9, 1], dtype=complex)
+    sb = B.SeedSetupBoundaries(c, diskno=1, distance=np.array([0, 0.15, 0.05, 0]) * 1e-2, epsilon=eps)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=10, Lmax=0, diskR=0.15)
+    out = []
+    for d in DEPS:
+        sb.distance = _dist(d)
+        b = B.transformer(sb, c, modes, prop=B.propagator, f=10e9, diskR=0.15)
+        out.append(np.sum(np.abs(b) ** 2))
+    assert rel(out, G.TRANSFORMER_BETA2) < G.RTOL
+    fld = B.modes2field(B.field2modes(None, c, modes, diskR=0.15), c, modes)
+    assert abs(fld.flatten(order="F")[4999] - G.MODES_FIELD_5000) / abs(G.MODES_FIELD_5000) < G.RTOL
+    assert sb.eps[0] == 1e30                     # mutated like the reference (:289)
+    pm = B.calc_propagation_matrices(sb, c, modes)
+    assert abs(pm[0][3, 5] - G.PROPMAT_1_4_6) / abs(G.PROPMAT_1_4_6) < G.RTOL
+
+
+def _stack(ndisk, n, seed, tilt_air=False, surf=False):
+    from bfgb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    nd = 2 * ndisk + 2
+    tx = np.zeros(nd); ty = np.zeros(nd)
+    for k in range(ndisk):
+        tx[2 + 2 * k] = rng.uniform(-5e-4, 5e-4)
+        ty[2 + 2 * k] = rng.uniform(-5e-4, 5e-4)
+    if tilt_air:
+        tx[1] = 3e-4
+    distance, eps, tx, ty = W.booster(ndisk, rng.uniform(7.5e-3, 8.5e-3, ndisk), tilt_x=tx, tilt_y=ty)
+    X = W.symmetric_grid(n)
+    s = None
+    if surf:
+        s = np.zeros((nd, n, n))
+        for k in range(ndisk):
+            s[2 + 2 * k] = 1e-5 * rng.standard_normal((n, n))
+    return distance, eps, tx, ty, X, s
+
+
+@pytest.mark.parametrize("n,ndisk,M,L,tilt_air,surf", [(32, 1, 4, 0, False, False), (48, 2, 3, 1, False, True),
+                                                       (32, 2, 3, 0, True, False)])
+def test_transformer_fp64_vs_oracle(B, n, ndisk, M, L, tilt_air, surf):
+    distance, eps, tx, ty, X, s = _stack(ndisk, n, seed=n + M, tilt_air=tilt_air, surf=surf)
+    kw = dict(diskno=ndisk, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty)
+    if s is not None:
+        kw["relative_surfaces"] = s
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=M, Lmax=L, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=M, Lmax=L, diskR=0.15)
+    for f in (19.6e9, 20.4e9):
+        sbb, sbo = B.SeedSetupBoundaries(cb, **kw), O.seed_setup_boundaries(co, **kw)
+        rng = np.random.default_rng(1)
+        refl_in = rng.standard_normal(mb.nm) + 1j * rng.standard_normal(mb.nm)
+        ref_b, ref_r = O.transformer(sbo, co, mo, f=f, reflect=refl_in)
+        got_b, got_r = B.transformer(sbb, cb, mb, f=f, reflect=refl_in)
+        assert rel(got_b, ref_b) < FP64_TOL and rel(got_r, ref_r) < FP64_TOL
+        pmo = O.calc_propagation_matrices(sbo, co, mo, f=f)
+        pmb = B.calc_propagation_matrices(sbb, cb, mb, f=f)
+        for j in range(1, len(pmo)):
+            assert rel(pmb[j], pmo[j]) < FP64_TOL, j
+
+
+def test_transformer_batched_mixed_and_injected(B):
+    distance, eps, tx, ty, X, s = _stack(3, 64, seed=7, surf=True)
+    kw = dict(diskno=3, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=6, Lmax=0, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=6, Lmax=0, diskR=0.15)
+    freqs = np.linspace(19.5e9, 20.5e9, 5)
+    b64 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs)
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    for k, f in enumerate(freqs):
+        ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
+        assert rel(b64[k], ref) < FP64_TOL
+        r2 = np.sum(np.abs(ref) ** 2)
+        assert abs(np.sum(np.abs(b32[k]) ** 2) - r2) / r2 < MIXED_BETA2_TOL
+    # injected matrices (transformer.jl:335-337) give the same boost
+    sbo = O.seed_setup_boundaries(co, **kw)
+    sbo.eps[0] = 1e30
+    pm = O.calc_propagation_matrices(sbo, co, mo, f=freqs[2])
+    got = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs[2], propagation_matrices=pm)
+    assert rel(got, O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=freqs[2], propagation_matrices=pm)) < FP64_TOL
+
+
+def test_transformer_1d_vs_analytical1d(B):
+    d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
+    c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
+    m1 = B.SeedModes(c1, ThreeDim=False)
+    for k in range(int(d["ncases"])):
+        nd, eps_d, spac, freqs, gold = int(d[f"nd_{k}"]), float(d[f"eps_{k}"]), d[f"spacings_{k}"], d[f"freqs_{k}"], d[f"beta2_{k}"]
+        dist, eps = [0.0], [np.nan]
+        for i in range(nd):
+            dist += [spac[i], 1e-3]
+            eps += [1.0, eps_d]
+        dist += [0.0]; eps += [1.0]
+        sb = B.SeedSetupBoundaries(c1, diskno=nd, distance=np.array(dist), epsilon=np.array(eps, dtype=complex))
+        got = np.abs(B.transformer(sb, c1, m1, f=freqs, prop=B.propagator1D)[:, 0]) ** 2
+        assert np.allclose(got, gold, rtol=1e-6), k
