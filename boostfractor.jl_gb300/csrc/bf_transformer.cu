@@ -24,6 +24,7 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/boostfractor_gb300.h"
@@ -92,6 +93,8 @@ __device__ __forceinline__ double2 k0_c(double lambda, double er, double ei) {
 template <typename C> __device__ __forceinline__ C dto(double2 v);
 template <> __device__ __forceinline__ float2 dto<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 template <> __device__ __forceinline__ double2 dto<double2>(double2 v) { return v; }
+// double-float storage (hi/lo FP32 pairs) of the overlap operands of the mixed path
+template <> __device__ __forceinline__ float4 dto<float4>(double2 v) { return bf::df_split(v); }
 
 struct RegionT {      // per-region data of a transformer solve
   double dz, er, ei, tx, ty;
@@ -180,9 +183,10 @@ __global__ void k_build_e(C* E, const int* supp, int Kd, const double* freqs, in
 
 // P[f][j][m][m'] from a class GEMM output G[mm'][f*ncols + col]; pixel-class
 // disk regions get the propagation diag(exp(-i kz_m dz)) from the left.
-template <typename C>
-__global__ void k_scatter_p(C* P, const C* Gm, int nf, int ncols, const RegionT* regs, const int* cls_regions,
-                            int nd, int nm, const double* freqs, const double2* kt, int left_diag) {
+__global__ void k_scatter_p(double2* P, const double2* Gm, int nf, int ncols, const RegionT* regs,
+                            const int* cls_regions, int nd, int nm, const double* freqs, const double2* kt,
+                            int left_diag) {
+  using C = double2;
   const int mm = blockIdx.x * blockDim.x + threadIdx.x;
   const int c = blockIdx.y;
   if (mm >= nm * nm) return;
@@ -475,7 +479,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
-  const size_t csz = fp64 ? 16 : 8;
+  const size_t csz = 16;   // double2 or a double-float float4
   c.nm = nm;
   // orbits of the phasor symmetry in shifted (kX, kY) index space
   auto antisym = [](const std::vector<double>& k) {
@@ -539,7 +543,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
     dim3 grid(blocks_for(c.K), nm * nm);
     const double scale = 1.0 / ((double)nx * (double)ny);
     if (fp64) { bf::note_launch(); k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
-    else { bf::note_launch(); k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
+    else { bf::note_launch(); k_build_w<float4><<<grid, 256, 0, st>>>(c.W.as<float4>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
     TCK(cudaGetLastError());
   }
   // support pixels (any mode non-zero) and V
@@ -557,7 +561,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   {
     dim3 grid(blocks_for(c.Kd), nm * nm);
     if (fp64) { bf::note_launch(); k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
-    else { bf::note_launch(); k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
+    else { bf::note_launch(); k_build_v<float4><<<grid, 256, 0, st>>>(c.V.as<float4>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
     TCK(cudaGetLastError());
   }
   TCK(cudaStreamSynchronize(st));
@@ -577,21 +581,31 @@ static void tf_mark(bf_handle* h, int i) {
   cudaEventRecord(h->ev[i], h->stream());
 }
 
-template <typename C>
-static int launch_gemm(bf_handle* h, const C* A, const C* B, C* Cm, int R, int K, int N) {
+// Class GEMM G = A * B with FP64 output: FP64 operands, or double-float
+// operands (mixed path) on the FP32 pipes.
+template <typename S>
+static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R, int K, int N) {
   g_tf_gemm_flops += 8.0 * (double)R * (double)K * (double)N;
   dim3 grid((N + 63) / 64, (R + 63) / 64);
   bf::note_launch();
-  bf::k_cgemm<C><<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
+  if constexpr (std::is_same<S, double2>::value)
+    bf::k_cgemm<double2><<<grid, 256, 0, h->stream()>>>(reinterpret_cast<const double2*>(A),
+                                                        reinterpret_cast<const double2*>(B), Cm, R, K, N);
+  else
+    bf::k_cgemm_df<<<grid, 256, 0, h->stream()>>>(reinterpret_cast<const float4*>(A),
+                                                  reinterpret_cast<const float4*>(B), Cm, R, K, N);
   TCK(cudaGetLastError());
   return BF_OK;
 }
 
-// Propagation matrices of regions [j0, nd) for all frequencies into P[f][j][m][m'].
-template <typename C>
+// Propagation matrices of regions [j0, nd) for all frequencies into
+// P[f][j][m][m'] (FP64).  S is the operand storage of the class GEMMs:
+// double2 (FP64 path) or float4 (double-float, mixed path).
+template <typename S>
 static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
                                    const std::vector<RegionT>& regs, int j0, int nf,
-                                   const std::vector<double>& freqs, int prop_kind, bool fp64, DBuf& P) {
+                                   const std::vector<double>& freqs, int prop_kind, DBuf& P) {
+  using C = double2;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm, nx = s->nx, ny = s->ny;
   const size_t npix = (size_t)nx * ny;
@@ -617,18 +631,18 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(lst.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(lst.p, kreg.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npar;
-    TCKS(D.alloc(h, sizeof(C) * (size_t)c.K * ncol));
+    TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
     dim3 gd(blocks_for(c.K), ncol);
     bf::note_launch();
-    k_build_d<C><<<gd, 256, 0, st>>>(D.as<C>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, dr, lst.as<int>(),
+    k_build_d<S><<<gd, 256, 0, st>>>(D.as<S>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, dr, lst.as<int>(),
                                      npar, s->dkX, s->dkY);
     TCK(cudaGetLastError());
-    TCKS(launch_gemm<C>(h, c.W.as<C>(), D.as<C>(), G.as<C>(), nm * nm, c.K, ncol));
+    TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
     dim3 gs(blocks_for((size_t)nm * nm), ncol);
     bf::note_launch();
-    k_scatter_p<C><<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
-                                       d_kt.as<double2>(), 0);
+    k_scatter_p<<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+                                    d_kt.as<double2>(), 0);
     TCK(cudaGetLastError());
     TCK(cudaStreamSynchronize(st));
   }
@@ -639,22 +653,22 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(lst.alloc(h, sizeof(int) * npx));
     TCK(cudaMemcpyAsync(lst.p, preg.data(), sizeof(int) * npx, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npx;
-    TCKS(E.alloc(h, sizeof(C) * (size_t)c.Kd * ncol));
+    TCKS(E.alloc(h, sizeof(S) * (size_t)c.Kd * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
     dim3 ge(blocks_for(c.Kd), ncol);
     bf::note_launch();
-    k_build_e<C><<<ge, 256, 0, st>>>(E.as<C>(), c.supp.as<int>(), c.Kd, d_freq.as<double>(), nf, dr, lst.as<int>(),
+    k_build_e<S><<<ge, 256, 0, st>>>(E.as<S>(), c.supp.as<int>(), c.Kd, d_freq.as<double>(), nf, dr, lst.as<int>(),
                                      npx, s->dX, s->dY, nx, s->d_surf, (int)npix);
     TCK(cudaGetLastError());
-    TCKS(launch_gemm<C>(h, c.V.as<C>(), E.as<C>(), G.as<C>(), nm * nm, c.Kd, ncol));
+    TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
     dim3 gs(blocks_for((size_t)nm * nm), ncol);
     bf::note_launch();
-    k_scatter_p<C><<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
-                                       d_kt.as<double2>(), 1);
+    k_scatter_p<<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+                                    d_kt.as<double2>(), 1);
     TCK(cudaGetLastError());
     TCK(cudaStreamSynchronize(st));
   }
-  // field class: propagate every mode, then overlap
+  // field class: propagate every mode (FP64), then overlap
   if (!freg.empty()) {
     DBuf Q, tmp, fr;
     TCKS(Q.alloc(h, sizeof(C) * (size_t)nm * npix));
@@ -668,7 +682,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
         bf::note_launch();
         k_copy_modes<C><<<blocks_for((size_t)nm * npix), 256, 0, st>>>(Q.as<C>(), md->d_pat, nm, (int)npix, 1);
         TCK(cudaGetLastError());
-        TCKS(bf_general_prop(h, s, kind, fp64, Q.p, tmp.p, nm, fr.as<double>(), j));
+        TCKS(bf_general_prop(h, s, kind, true, Q.p, tmp.p, nm, fr.as<double>(), j));
         bf::note_launch();
         k_overlap<C><<<nm * nm, 256, 0, st>>>(P.as<C>() + (((size_t)f * nd + j) * nm) * nm, md->d_pat, Q.as<C>(), nm,
                                               (int)npix);
@@ -837,7 +851,9 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
   return BF_OK;
 }
 
-template <typename C>
+// One transformer solve (or, with only_matrices, the propagation matrices).
+// fp64 selects FP64 class-GEMM operands; otherwise double-float operands on
+// the FP32 pipes.  Propagation matrices, inverses, chain and solve are FP64.
 static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
                   const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
                   double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm) {
@@ -856,7 +872,7 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
   const unsigned long long l0 = bf::launch_count();
   if (pm) {
     // injected propagation matrices: [nf or 1][nd][nm][nm], each a Julia (nm, nm) column-major matrix
-    std::vector<C> hp((size_t)nf * nd * nm * nm);
+    std::vector<double2> hp((size_t)nf * nd * nm * nm);
     const cd* src = as_cdp(pm);
     for (int f = 0; f < nf; ++f)
       for (int j = 0; j < nd; ++j) {
@@ -864,30 +880,29 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
         for (int r = 0; r < nm; ++r)
           for (int cidx = 0; cidx < nm; ++cidx) {
             const cd v = mj[r + (size_t)nm * cidx];
-            C o;
-            o.x = (decltype(o.x))v.real();
-            o.y = (decltype(o.x))v.imag();
-            hp[(((size_t)f * nd + j) * nm + r) * nm + cidx] = o;
+            hp[(((size_t)f * nd + j) * nm + r) * nm + cidx] = make_double2(v.real(), v.imag());
           }
       }
-    TCKS(P.alloc(h, sizeof(C) * hp.size()));
-    TCK(cudaMemcpyAsync(P.p, hp.data(), sizeof(C) * hp.size(), cudaMemcpyHostToDevice, st));
+    TCKS(P.alloc(h, sizeof(double2) * hp.size()));
+    TCK(cudaMemcpyAsync(P.p, hp.data(), sizeof(double2) * hp.size(), cudaMemcpyHostToDevice, st));
   } else {
     TfCache* c = nullptr;
     TCKS(tf_setup(h, s, md, fp64, &c));
-    TCKS(tf_propagation_matrices<C>(h, s, md, *c, regs, only_matrices ? 0 : 1, nf, fv, prop_kind, fp64, P));
+    const int j0 = only_matrices ? 0 : 1;
+    if (fp64) TCKS(tf_propagation_matrices<double2>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
+    else TCKS(tf_propagation_matrices<float4>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
   }
   if (only_matrices) {
     // out_pm: [nf][nd] Julia (nm, nm) column-major matrices
-    std::vector<C> hp((size_t)nf * nd * nm * nm);
-    TCK(cudaMemcpyAsync(hp.data(), P.p, sizeof(C) * hp.size(), cudaMemcpyDeviceToHost, st));
+    std::vector<double2> hp((size_t)nf * nd * nm * nm);
+    TCK(cudaMemcpyAsync(hp.data(), P.p, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
     cd* o = reinterpret_cast<cd*>(out_pm);
     for (int f = 0; f < nf; ++f)
       for (int j = 0; j < nd; ++j)
         for (int r = 0; r < nm; ++r)
           for (int cidx = 0; cidx < nm; ++cidx) {
-            const C v = hp[(((size_t)f * nd + j) * nm + r) * nm + cidx];
+            const double2 v = hp[(((size_t)f * nd + j) * nm + r) * nm + cidx];
             o[((size_t)f * nd + j) * nm * nm + r + (size_t)nm * cidx] = cd(v.x, v.y);
           }
     return BF_OK;
@@ -897,16 +912,7 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
   // precision: near a resonance T22 is ill-conditioned and FP32 chains lose
   // the 1e-4 bar on beta^2 (the propagation matrices themselves may be FP32).
   using D2 = double2;
-  DBuf P64;
-  const D2* Pd;
-  if (sizeof(C) == sizeof(D2)) {
-    Pd = reinterpret_cast<const D2*>(P.p);
-  } else {
-    TCKS(P64.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
-    if (bf::launch_convert(P.p, false, P64.p, true, (size_t)nf * nd * nm * nm, st))
-      return bf_fail(h, BF_ERR_CUDA, "convert P");
-    Pd = P64.as<D2>();
-  }
+  const D2* Pd = P.as<D2>();
   TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
   {
     const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
@@ -1010,11 +1016,8 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
                               double* out_refl, double* out_beta2) {
   TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
   TCK(cudaSetDevice(h->device));
-  if (precision == BF_PREC_FP64)
-    return tf_run<double2>(h, s, md, nf, freqs, prop_kind, true, emit, reflect, propagation_matrices, pm_per_freq,
-                           out_boost, out_refl, out_beta2, 1, 0, nullptr);
-  return tf_run<float2>(h, s, md, nf, freqs, prop_kind, false, emit, reflect, propagation_matrices, pm_per_freq,
-                        out_boost, out_refl, out_beta2, 1, 0, nullptr);
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, emit, reflect, propagation_matrices,
+                pm_per_freq, out_boost, out_refl, out_beta2, 1, 0, nullptr);
 }
 
 extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,
@@ -1022,9 +1025,6 @@ extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes*
   TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
   if (!out) return bf_fail(h, BF_ERR_INVALID, "null output");
   TCK(cudaSetDevice(h->device));
-  if (precision == BF_PREC_FP64)
-    return tf_run<double2>(h, s, md, nf, freqs, prop_kind, true, nullptr, nullptr, nullptr, 0, nullptr, nullptr,
-                           nullptr, 0, 1, out);
-  return tf_run<float2>(h, s, md, nf, freqs, prop_kind, false, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
-                        0, 1, out);
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, nullptr, nullptr, nullptr, 0, nullptr,
+                nullptr, nullptr, 0, 1, out);
 }

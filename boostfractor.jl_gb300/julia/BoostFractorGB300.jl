@@ -1,0 +1,176 @@
+# BoostFractorGB300: the GB300 solvers behind BoostFractor.jl's public API.
+#
+# Thin ccall wrappers over libbfgb300.so (include/boostfractor_gb300.h).  The
+# methods take the reference's own types (SetupBoundaries, CoordinateSystem,
+# Modes) and keyword arguments, so a caller switches by replacing
+# `BoostFractor.cheerleader(...)` with `BoostFractorGB300.cheerleader(...)`.
+# Arrays are passed as they are: Julia's column-major ComplexF64 layout is the
+# ABI's layout.
+module BoostFractorGB300
+
+using BoostFractor: SetupBoundaries, CoordinateSystem, Modes,
+                    propagator, propagatorNoTilts, propagatorMomentumSpace, propagator1D
+
+const lib = get(ENV, "BFGB300_LIB", joinpath(@__DIR__, "..", "lib", "libbfgb300.so"))
+
+const BF_PROP = Dict(propagator => 0, propagatorNoTilts => 1, propagatorMomentumSpace => 2,
+                     propagator1D => 3)
+const BF_PREC = Dict(:fp64 => 0, :mixed => 1)
+
+mutable struct Handle
+    ptr::Ptr{Cvoid}
+end
+
+function check(h::Handle, rc::Cint)
+    rc == 0 && return nothing
+    msg = unsafe_string(ccall((:bf_last_error, lib), Cstring, (Ptr{Cvoid},), h.ptr))
+    rc == 1 && throw(ArgumentError(msg))
+    error("libbfgb300 error $rc: $msg")
+end
+
+function Handle(device::Integer = 0; hbm_budget::Integer = 0)
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:bf_create, lib), Cint, (Cint, Culonglong, Ptr{Ptr{Cvoid}}), device, hbm_budget, ref)
+    rc == 0 || error("bf_create failed ($rc)")
+    h = Handle(ref[])
+    finalizer(x -> ccall((:bf_destroy, lib), Cint, (Ptr{Cvoid},), x.ptr), h)
+    return h
+end
+
+const DEFAULT = Ref{Union{Nothing, Handle}}(nothing)
+default_handle() = something(DEFAULT[], (DEFAULT[] = Handle(0)))
+
+# resident stack (bf_stack_create)
+function stack(h::Handle, bdry::SetupBoundaries, coords::CoordinateSystem, diskR)
+    nd = length(bdry.distance)
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    surf = any(!iszero, bdry.relative_surfaces) ? ComplexF64.(bdry.relative_surfaces) : C_NULL
+    check(h, ccall((:bf_stack_create, lib), Cint,
+        (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{ComplexF64}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Float64,
+         Ptr{Ptr{Cvoid}}),
+        h.ptr, nd, Float64.(bdry.distance), ComplexF64.(bdry.r), ComplexF64.(bdry.eps),
+        Float64.(bdry.relative_tilt_x), Float64.(bdry.relative_tilt_y), surf,
+        length(coords.X), length(coords.Y), collect(Float64, coords.X), collect(Float64, coords.Y),
+        collect(Float64, coords.kX), collect(Float64, coords.kY), diskR, ref))
+    return ref[]
+end
+stack_destroy(h::Handle, s) = ccall((:bf_stack_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), h.ptr, s)
+
+"""
+    cheerleader(amin, nmax, bdry, coords; f=10.0e9, prop=propagator, emit=nothing,
+                reflect=nothing, diskR=0.1, returnboth=false, precision=:fp64)
+
+src/boost_fractor_recurprop.jl:226 on the GPU.  `f` may be a vector: the
+frequencies are solved as one batch and the result gains a trailing frequency
+dimension.
+"""
+function cheerleader(amin, nmax, bdry::SetupBoundaries, coords::CoordinateSystem; f=10.0e9,
+                     prop=propagator, emit=nothing, reflect=nothing, diskR=0.1, returnboth=false,
+                     precision=:fp64, handle=default_handle())
+    freqs = Float64.(collect(f))
+    nx, ny, nf = length(coords.X), length(coords.Y), length(freqs)
+    right = Array{ComplexF64}(undef, nx, ny, nf)
+    left = returnboth ? Array{ComplexF64}(undef, nx, ny, nf) : C_NULL
+    s = stack(handle, bdry, coords, diskR)
+    try
+        check(handle, ccall((:bf_stack_cheerleader, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Float64, Cint, Cint, Cint, Ptr{ComplexF64},
+             Ptr{ComplexF64}, Cint, Float64, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Float64}),
+            handle.ptr, s, nf, freqs, amin, nmax, BF_PROP[prop], BF_PREC[precision],
+            emit === nothing ? C_NULL : ComplexF64.(emit), reflect === nothing ? C_NULL : ComplexF64.(reflect),
+            returnboth, 0.0, 0, right, left, C_NULL))
+    finally
+        stack_destroy(handle, s)
+    end
+    r = f isa Number ? right[:, :, 1] : right
+    returnboth || return r
+    return (f isa Number ? left[:, :, 1] : left), r
+end
+
+"""
+    dancer(amin, nmax, sbdry, coords; f=10.0e9, prop=propagator, emit=nothing,
+           reflect=nothing, diskR=0.1, returnsum=true, immediatesum=true, precision=:fp64)
+
+src/boost_fractor_recurprop.jl:25 on the GPU.
+"""
+function dancer(amin, nmax, sbdry::SetupBoundaries, coords::CoordinateSystem; f=10.0e9,
+                prop=propagator, emit=nothing, reflect=nothing, diskR=0.1, returnsum=true,
+                immediatesum=true, precision=:fp64, handle=default_handle())
+    freqs = Float64.(collect(f))
+    nx, ny, nf = length(coords.X), length(coords.Y), length(freqs)
+    nslots = (returnsum || immediatesum) ? 1 : nmax + 1
+    out = Array{ComplexF64}(undef, nx, ny, nslots, nf)
+    s = stack(handle, sbdry, coords, diskR)
+    try
+        check(handle, ccall((:bf_stack_dancer, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Float64, Cint, Cint, Cint, Ptr{ComplexF64},
+             Ptr{ComplexF64}, Cint, Cint, Float64, Cint, Ptr{ComplexF64}, Ptr{Float64}),
+            handle.ptr, s, nf, freqs, amin, nmax, BF_PROP[prop], BF_PREC[precision],
+            emit === nothing ? C_NULL : ComplexF64.(emit), reflect === nothing ? C_NULL : ComplexF64.(reflect),
+            returnsum, immediatesum, 0.0, 0, out, C_NULL))
+    finally
+        stack_destroy(handle, s)
+    end
+    r = nslots == 1 ? out[:, :, 1, :] : out
+    return f isa Number ? selectdim(r, ndims(r), 1) |> collect : r
+end
+
+"""
+    propagate!(E0, dz, diskR, eps, tilt_x, tilt_y, surface, lambda, coords; prop=propagator)
+
+The `prop=` plug-in as one GPU call (src/boost_fractor.jl:137-227).
+"""
+function propagate!(E0::Matrix{ComplexF64}, dz, diskR, eps, tilt_x, tilt_y, surface, lambda,
+                    coords::CoordinateSystem; prop=propagator, precision=:fp64, handle=default_handle())
+    surf = surface isa AbstractArray && any(!iszero, surface) ? ComplexF64.(surface) : C_NULL
+    check(handle, ccall((:bf_propagate, lib), Cint,
+        (Ptr{Cvoid}, Cint, Cint, Ptr{ComplexF64}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+         Ptr{Float64}, Float64, Float64, Float64, Float64, Float64, Float64, Ptr{ComplexF64}, Float64),
+        handle.ptr, BF_PROP[prop], BF_PREC[precision], E0, size(E0, 1), size(E0, 2),
+        collect(Float64, coords.X), collect(Float64, coords.Y), collect(Float64, coords.kX),
+        collect(Float64, coords.kY), dz, diskR, real(eps), imag(eps), tilt_x, tilt_y, surf, lambda))
+    return E0
+end
+
+"""
+    transformer(bdry, coords, modes; f=10.0e9, prop=propagator, propagation_matrices=[],
+                diskR=0.15, emit=nothing, reflect=nothing, precision=:fp64)
+
+src/boost_fractor_transformer.jl:285 on the GPU (NaN permittivities of `bdry`
+become 1e30 in place, like the reference).  `modes` is the reference's Modes;
+its patterns are uploaded as `pattern_input`.
+"""
+function transformer(bdry::SetupBoundaries, coords::CoordinateSystem, modes::Modes; f=10.0e9,
+                     prop=propagator, propagation_matrices=Matrix{ComplexF64}[], diskR=0.15,
+                     emit=nothing, reflect=nothing, precision=:fp64, handle=default_handle())
+    bdry.eps[isnan.(bdry.eps)] .= 1e30
+    freqs = Float64.(collect(f))
+    nf, nm = length(freqs), modes.M * (2modes.L + 1)
+    mref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(handle, ccall((:bf_modes_create, lib), Cint,
+        (Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Float64,
+         Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Ptr{Cvoid}}),
+        handle.ptr, length(coords.X), length(coords.Y), collect(Float64, coords.X),
+        collect(Float64, coords.Y), 1, modes.M, modes.L, diskR, modes.mode_patterns, modes.mode_kt, mref))
+    s = stack(handle, bdry, coords, diskR)
+    boost = Array{ComplexF64}(undef, nm, nf)
+    refl = reflect === nothing ? C_NULL : Array{ComplexF64}(undef, nm, nf)
+    pm = isempty(propagation_matrices) ? C_NULL : reduce(hcat, vec.(propagation_matrices))
+    try
+        check(handle, ccall((:bf_transformer, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint, Ptr{ComplexF64},
+             Ptr{ComplexF64}, Ptr{ComplexF64}, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Float64}),
+            handle.ptr, s, mref[], nf, freqs, BF_PROP[prop], BF_PREC[precision],
+            emit === nothing ? C_NULL : ComplexF64.(emit), reflect === nothing ? C_NULL : ComplexF64.(reflect),
+            pm, 0, boost, refl, C_NULL))
+    finally
+        stack_destroy(handle, s)
+        ccall((:bf_modes_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), handle.ptr, mref[])
+    end
+    b = f isa Number ? boost[:, 1] : boost
+    reflect === nothing && return b
+    return b, (f isa Number ? refl[:, 1] : refl)
+end
+
+end # module
