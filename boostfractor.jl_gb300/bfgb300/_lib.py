@@ -21,6 +21,7 @@ BF_PROP_3D = 0
 BF_PROP_NOTILTS = 1
 BF_PROP_MOMENTUM = 2
 BF_PROP_1D = 3
+BF_NOALLOC_MAX_N = 256
 
 BF_PREC_FP64 = 0
 BF_PREC_MIXED = 1
@@ -47,6 +48,8 @@ _SIGS = {
     "bf_fresnel_reflectivities": (_c_int, [_c_int, _p_dbl, _p_dbl]),
     "bf_propagate": (_c_int, [_vp, _c_int, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl,
                               _p_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
+    "bf_propagate_noalloc": (_c_int, [_vp, _c_int, _vp, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl,
+                                      _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
     "bf_stack_create": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                  _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, ctypes.POINTER(_vp)]),
     "bf_stack_destroy": (_c_int, [_vp, _vp]),

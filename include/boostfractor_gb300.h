@@ -107,6 +107,26 @@ int bf_propagate(bf_handle* h, int prop_kind, int precision,
                  double dz, double diskR, double eps_re, double eps_im,
                  double tilt_x, double tilt_y, const double* surface, double lambda);
 
+/* ---- propagation without allocation -------------------------------------- */
+/* No counterpart in the reference.  The operation of bf_propagate at FP64 on a
+ * field E_dev ((nx, ny) complex128, column-major) that already lives in device
+ * memory, propagated in place on the handle's stream; the call does not wait
+ * for the result.  Every piece of workspace is one static device array per
+ * device, so the call makes no cudaMalloc / cudaFree and no other allocation:
+ * for callers with a pre-sized device pool, or that must not stall the device
+ * with cudaFree's implicit synchronisation.
+ *   - nx, ny <= BF_NOALLOC_MAX_N; larger grids return BF_ERR_INVALID.
+ *   - The first call on a device does the set-up (cudaGetSymbolAddress of the
+ *     scratch, first launch of each kernel); make it before any stream capture.
+ *   - One scratch per device for the whole process: overlapping calls (other
+ *     streams, other threads) race on it; serialise them.
+ * X, Y, kX, kY, surface are host arrays as in bf_propagate. */
+#define BF_NOALLOC_MAX_N 256
+int bf_propagate_noalloc(bf_handle* h, int prop_kind, double* E_dev, int nx, int ny,
+                         const double* X, const double* Y, const double* kX, const double* kY,
+                         double dz, double diskR, double eps_re, double eps_im,
+                         double tilt_x, double tilt_y, const double* surface, double lambda);
+
 /* ---- resident disk stacks ------------------------------------------------ */
 /* Upload a SetupBoundaries (src/boost_fractor.jl:63-71) and a CoordinateSystem
  * (:21-28) once; the stack stays in HBM until bf_stack_destroy.
