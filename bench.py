@@ -328,8 +328,9 @@ def run_ours(args):
 
 
 def run_transformer(args):
-    """Transformer mode-matching arm: 20 disks with surface maps, 64 modes on a
-    256x256 grid, 1024 frequencies per request (one request per step)."""
+    """Transformer mode-matching arm: 20 disks with surface maps, 64
+    Laguerre-Gauss modes on a 256x256 grid, 1024 frequencies per request (one
+    request per step)."""
     import torch
     torch.cuda.set_device(0)
     import build as _b
@@ -349,7 +350,8 @@ def run_transformer(args):
               relative_tilt_x=w["relative_tilt_x"], relative_tilt_y=w["relative_tilt_y"],
               relative_surfaces=w["relative_surfaces"])
     t0 = time.perf_counter()
-    modes = B.SeedModes(c, ThreeDim=True, Mmax=w["M"], Lmax=w["L"], diskR=w["diskR"], handle=h)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=w["M"], Lmax=w["L"], diskR=w["diskR"],
+                        pattern_input=w["pattern_input"], kT_arr=w["kT_arr"], handle=h)
     t_modes = time.perf_counter() - t0
     sb = B.SeedSetupBoundaries(c, **kw)
     sb.eps[np.isnan(sb.eps)] = 1e30
@@ -395,7 +397,7 @@ def run_transformer(args):
     ms = e0.elapsed_time(e1) / args.steps
     N = len(w["X"])
     peak_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
-    line = {"metric": f"beta2 freq-points/s (transformer, 20 disks + surface maps, {nm} modes, {N}x{N}, {nf} freqs)",
+    line = {"metric": f"beta2 freq-points/s (transformer, 20 disks + surface maps, {nm} LG modes, {N}x{N}, {nf} freqs)",
             "value": nf / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c64 overlap GEMMs (FP32), f64 phases, inverses, chain and boundary solve",

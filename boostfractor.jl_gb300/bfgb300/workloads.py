@@ -79,18 +79,63 @@ def surface_roughness(X, Y, ngaps, rng, mag=1e-5, trunc=1e-4, xi=0.02, diskR=0.1
     return init
 
 
-def config3_transformer(seed=3, n=256, ndisk=20, nf=1024, modes=64, f_lo=19e9, f_hi=21e9):
+def lg_orders(n_modes):
+    """(p, l) of the n_modes lowest-order Laguerre-Gauss modes, ordered by the
+    order N = 2p + |l|, then by l (-N, -N+2, ..., N)."""
+    out = []
+    N = 0
+    while len(out) < n_modes:
+        for l in range(-N, N + 1, 2):
+            out.append(((N - abs(l)) // 2, l))
+        N += 1
+    return out[:n_modes]
+
+
+def lg_modes(X, Y, n_modes=64, waist=0.03, diskR=0.15):
+    """Laguerre-Gauss modes LG_p^l(r) e^{-i l phi} at the waist, as the
+    reference's `pattern_input` and `kT_arr` of SeedModes
+    (src/boost_fractor_transformer.jl:46, :99-104): patterns (n_modes, 1, nx,
+    ny, 1) cut to r <= diskR and normalised to sum |pattern|^2 = 1, and the
+    paraxial transverse wavenumber kT = 2 sqrt(N + 1) / waist of each mode
+    (the Gouy phase (N + 1) z / z_R written as kz = sqrt(k^2 - kT^2) to first
+    order), N = 2p + |l|.
+
+    With the 3 cm waist every one of the 64 lowest orders (N <= 10) lies
+    inside the 0.15 m disk and propagates in air above 10 GHz (kT <= 221 rad/m),
+    so the transfer-matrix chain through a 20-disk stack stays well conditioned.
+    """
+    from scipy.special import eval_genlaguerre
+    X = np.asarray(X, dtype=np.float64)
+    Y = np.asarray(Y, dtype=np.float64)
+    RR = np.sqrt(X[:, None] ** 2 + Y[None, :] ** 2)
+    Phi = np.arctan2(np.broadcast_to(Y[None, :], RR.shape), np.broadcast_to(X[:, None], RR.shape))
+    u = 2.0 * RR ** 2 / waist ** 2
+    orders = lg_orders(n_modes)
+    pats = np.zeros((n_modes, 1, len(X), len(Y), 1), dtype=np.complex128)
+    kt = np.zeros((n_modes, 1), dtype=np.complex128)
+    for i, (p, l) in enumerate(orders):
+        a = abs(l)
+        field = u ** (a / 2.0) * eval_genlaguerre(p, a, u) * np.exp(-u / 2.0) * np.exp(-1j * l * Phi)
+        field[RR > diskR] = 0.0
+        pats[i, 0, :, :, 0] = field / np.sqrt(np.sum(np.abs(field) ** 2))
+        kt[i, 0] = 2.0 * np.sqrt(2 * p + a + 1.0) / waist
+    return pats, kt
+
+
+def config3_transformer(seed=3, n=256, ndisk=20, nf=1024, modes=64, f_lo=19e9, f_hi=21e9, waist=0.03):
     """Transformer mode matching: the 20-disk geometry of the cheerleader
     workload on a 256x256 grid, per-disk surface maps (GRF, rms 10 um,
-    correlation length 2 cm), 64 Bessel disk modes (M=64, L=0), 1024
-    frequencies 19-21 GHz."""
+    correlation length 2 cm), 64 Laguerre-Gauss modes (the 64 lowest orders,
+    waist 3 cm, given as pattern_input with M=64, L=0), 1024 frequencies
+    19-21 GHz."""
     w = config2_cheerleader(seed=seed, n=n, ndisk=ndisk, nf=nf, f_lo=f_lo, f_hi=f_hi)
     rng = np.random.default_rng(seed + 1000)
     nd = len(w["distance"])
     surf = np.zeros((nd, n, n))
     surf[2:nd - 1:2] = surface_roughness(w["X"], w["Y"], ndisk, rng)
-    w.update(name=f"transformer-{ndisk}disk-{n}-{modes}modes", solver="transformer", relative_surfaces=surf,
-             M=modes, L=0)
+    pats, kt = lg_modes(w["X"], w["Y"], modes, waist, w["diskR"])
+    w.update(name=f"transformer-{ndisk}disk-{n}-{modes}LGmodes", solver="transformer", relative_surfaces=surf,
+             M=modes, L=0, pattern_input=pats, kT_arr=kt)
     return w
 
 

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -62,17 +63,46 @@ int bf_fail(bf_handle* h, int code, const std::string& msg) { return fail(h, cod
     if (s_ != BF_OK) return s_; \
   } while (0)
 
+// Device memory comes from one stream-ordered pool per device (allocations
+// and frees are ordered on the handle's stream).  Unlike cudaMalloc/cudaFree,
+// neither waits for the rest of the device, so handles working on different
+// streams (the serving engine's workers) do not serialise each other.  Freed
+// blocks stay in the pool for the next request; bf_destroy trims the pool.
+static cudaMemPool_t device_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  if (device < 0 || device >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!pools[device]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+  }
+  return pools[device];
+}
+
 int bf_dalloc(bf_handle* h, void** p, size_t bytes) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
+  std::lock_guard<std::mutex> lock(h->alloc_mu);
   if (h->budget && h->used + bytes > h->budget)
     return fail(h, BF_ERR_NOMEM, "device allocation of " + std::to_string(bytes) +
                                      " bytes exceeds the handle's HBM budget");
-  cudaError_t e = cudaMalloc(p, bytes);
+  cudaMemPool_t pool = device_pool(h->device);
+  cudaError_t e = pool ? cudaMallocFromPoolAsync(p, bytes, pool, h->stream()) : cudaMalloc(p, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     *p = nullptr;
-    return fail(h, BF_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return fail(h, BF_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
   }
   h->allocs[*p] = bytes;
   h->used += bytes;
@@ -81,12 +111,14 @@ int bf_dalloc(bf_handle* h, void** p, size_t bytes) {
 
 void bf_dfree(bf_handle* h, void* p) {
   if (!p) return;
+  std::lock_guard<std::mutex> lock(h->alloc_mu);
   auto it = h->allocs.find(p);
   if (it != h->allocs.end()) {
     h->used -= it->second;
     h->allocs.erase(it);
   }
-  cudaFree(p);
+  if (device_pool(h->device)) cudaFreeAsync(p, h->stream());
+  else cudaFree(p);
 }
 
 static int upload(bf_handle* h, DBuf& b, const void* src, size_t bytes) {
@@ -184,10 +216,16 @@ extern "C" int bf_create(int device, unsigned long long hbm_budget_bytes, bf_han
     delete h;
     return BF_ERR_CUDA;
   }
-  static bool roots_ready[64] = {false};
-  if (device < 64 && !roots_ready[device]) {
-    bf::init_constant_roots();
-    roots_ready[device] = true;
+  {
+    // the constant root tables are per device; write them once, even when
+    // several threads create handles at the same time
+    static std::mutex mu;
+    static bool roots_ready[64] = {false};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device < 64 && !roots_ready[device]) {
+      bf::init_constant_roots();
+      roots_ready[device] = true;
+    }
   }
   if (bf_dalloc(h, (void**)&h->d_scalar, 64) != BF_OK) {
     cudaStreamDestroy(h->own_stream);
@@ -202,8 +240,14 @@ extern "C" int bf_destroy(bf_handle* h) {
   if (!h) return BF_ERR_INVALID;
   cudaSetDevice(h->device);
   cudaStreamSynchronize(h->stream());
-  for (auto& kv : h->allocs) cudaFree(kv.first);
+  cudaMemPool_t pool = device_pool(h->device);
+  for (auto& kv : h->allocs) {
+    if (pool) cudaFreeAsync(kv.first, h->stream());
+    else cudaFree(kv.first);
+  }
   h->allocs.clear();
+  cudaStreamSynchronize(h->stream());
+  if (pool) cudaMemPoolTrimTo(pool, 0);
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   cudaStreamDestroy(h->own_stream);
@@ -385,6 +429,51 @@ extern "C" int bf_stack_destroy(bf_handle* h, bf_stack* s) {
   stack_free(h, s);
   delete s;
   return BF_OK;
+}
+
+static size_t dbuf_bytes(const DBuf& b) { return b.p ? b.n : 0; }
+
+size_t bf_stack_device_bytes(const bf_stack* s) {
+  if (!s) return 0;
+  const size_t npix = (size_t)s->nx * s->ny;
+  size_t b = sizeof(double) * 2 * ((size_t)s->nx + s->ny) + npix + (size_t)s->nbx * s->nby +
+             sizeof(RegionGeo) * s->nd;
+  if (s->d_surf) b += sizeof(double2) * s->nd * npix;
+  if (const Workspace* w = s->ws) {
+    for (const DBuf* d : {&w->freq, &w->reg, &w->phasor, &w->tidx, &w->tregs, &w->tilt, &w->init, &w->state,
+                          &w->add, &w->coef, &w->exitacc, &w->steps, &w->tmp, &w->beta, &w->exit_full[0],
+                          &w->exit_full[1], &w->direct[0], &w->direct[1]})
+      b += dbuf_bytes(*d);
+  }
+  if (s->tf_cache && s->tf_cache_bytes) b += s->tf_cache_bytes(s->tf_cache);
+  return b;
+}
+
+void bf_stack_trim(bf_stack* s) {
+  if (!s) return;
+  delete s->ws;
+  s->ws = nullptr;
+  if (s->tf_cache && s->tf_cache_delete) s->tf_cache_delete(s->tf_cache);
+  s->tf_cache = nullptr;
+}
+
+size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, int prop_kind, int precision) {
+  const size_t npix = (size_t)s->nx * s->ny, plane = (size_t)s->nbx * s->nby;
+  const size_t nd = (size_t)s->nd, F = (size_t)std::max(nf, 1);
+  const size_t csz = precision == BF_PREC_FP64 ? 16 : 8;
+  if (solver == 2) {
+    // resident overlaps (orbit-folded k-space W, pixel V), per solve: P and
+    // its inverses/chain (FP64), the class GEMM operands and products
+    const size_t m2 = (size_t)nm * nm;
+    const size_t K = s->kx_sym ? ((size_t)s->nx / 2 + 1) * ((size_t)s->ny / 2 + 1) : npix;
+    const size_t cache = s->tf_cache ? 0 : 16 * m2 * (K + npix) + 32 * nm * npix;
+    return cache + F * nd * (16 * 4 * m2 + 16 * (K + npix) + 16 * m2) + 16 * npix * nm * 2;
+  }
+  if (prop_kind == BF_PROP_1D) return F * (16 * 4 * nd * npix + 64);
+  const size_t slots = 2 * nd + 2;
+  const size_t fused = F * (csz * (slots * plane + nd * npix + nd * plane) + 16 * (2 * plane + 3 * npix));
+  const size_t full = F * (csz * (slots + 1) * npix + 16 * 3 * npix);
+  return std::max(fused, full) + F * 64;
 }
 
 extern "C" int bf_stack_set_distance(bf_handle* h, bf_stack* s, const double* distance) {

@@ -24,7 +24,10 @@
 
 namespace bf {
 
-static unsigned long long g_launches = 0;
+// Kernel launches made by the calling host thread (one handle's call runs on
+// one thread, so per-call differences are exact even with several handles
+// working concurrently).
+static thread_local unsigned long long g_launches = 0;
 unsigned long long launch_count() { return g_launches; }
 void note_launch() { ++g_launches; }
 #define COUNT_LAUNCH() (++g_launches)

@@ -6,6 +6,7 @@
 #pragma once
 
 #include <complex>
+#include <mutex>
 #include <cstdint>
 #include <string>
 #include <unordered_map>
@@ -33,6 +34,9 @@ struct bf_handle {
   int prof_valid = 0;
   unsigned long long prof_launch0 = 0;
   cudaStream_t stream() const { return user_stream ? user_stream : own_stream; }
+  // allocs/used may be changed by another thread that trims a stack whose
+  // workspace this handle allocated (the serving engine's eviction)
+  std::mutex alloc_mu;
 };
 
 int bf_dalloc(bf_handle* h, void** p, size_t bytes);
@@ -111,7 +115,19 @@ struct bf_stack {
   unsigned long long geo_version = 0;  // bumps when the geometry changes
   void* tf_cache = nullptr;            // transformer setup (mode FFT overlaps) of this stack
   void (*tf_cache_delete)(void*) = nullptr;
+  size_t (*tf_cache_bytes)(const void*) = nullptr;
 };
+
+// Device bytes held by a stack: geometry, bounce-loop workspace and the
+// transformer's cached overlaps.
+size_t bf_stack_device_bytes(const bf_stack* s);
+// Release a stack's workspace and transformer cache (the geometry stays); the
+// next solve rebuilds them.  The stack must be idle.
+void bf_stack_trim(bf_stack* s);
+// Upper bound of the device bytes one solve adds to a stack (workspace,
+// per-call buffers, outputs): solver 0 cheerleader, 1 dancer, 2 transformer
+// with nm modes.
+size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, int prop_kind, int precision);
 
 namespace bfhost {
 

@@ -19,6 +19,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <map>
@@ -441,7 +442,7 @@ __global__ void k_project(double2* out, const double2* pat, const double2* Bn, i
 // ---------------------------------------------------------------------------
 namespace {
 
-static unsigned long long g_modes_id = 0;
+static std::atomic<unsigned long long> g_modes_id{0};
 
 const cd* as_cdp(const double* p) { return reinterpret_cast<const cd*>(p); }
 
@@ -467,15 +468,25 @@ struct TfCache {
 };
 
 static void tf_cache_delete(void* p) { delete static_cast<TfCache*>(p); }
+static size_t tf_cache_bytes(const void* p) {
+  const TfCache* c = static_cast<const TfCache*>(p);
+  size_t b = 0;
+  for (const DBuf* d : {&c->W, &c->V, &c->rep, &c->supp, &c->U, &c->Phi, &c->members}) b += d->p ? d->n : 0;
+  return b;
+}
 
 static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache** out) {
   if (!s->tf_cache) {
     s->tf_cache = new TfCache();
     s->tf_cache_delete = tf_cache_delete;
+    s->tf_cache_bytes = tf_cache_bytes;
   }
   TfCache& c = *static_cast<TfCache*>(s->tf_cache);
   *out = &c;
-  if (c.modes_id == md->id && c.geo_version == s->geo_version && c.fp64 == (int)fp64) return BF_OK;
+  // W and V depend on the modes, the grid and the disk mask only, none of
+  // which a stack changes after creation (bf_stack_set_distance moves the
+  // disks), so gap updates of an optimiser reuse them.
+  if (c.modes_id == md->id && c.fp64 == (int)fp64) return BF_OK;
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -573,7 +584,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   return BF_OK;
 }
 
-static double g_tf_gemm_flops = 0.0;   // executed real flops of the class GEMMs of the last solve
+static thread_local double g_tf_gemm_flops = 0.0;   // executed real flops of the class GEMMs of this thread's last solve
 
 static void tf_mark(bf_handle* h, int i) {
   if (!h->profiling) return;

@@ -133,6 +133,56 @@ def test_transformer_batched_mixed_and_injected(B):
     assert rel(got, O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=freqs[2], propagation_matrices=pm)) < FP64_TOL
 
 
+def test_transformer_lg_pattern_input_vs_oracle(B):
+    """Laguerre-Gauss modes through pattern_input/kT_arr (transformer.jl:46,
+    :99-104) on a reduced stack with surface maps: FP64 boost within 1e-10,
+    mixed beta^2 within 1e-4."""
+    from bfgb300 import workloads as W
+    distance, eps, tx, ty, _, _ = _stack(4, 64, seed=41)
+    X = W.symmetric_grid(64, width=0.4)
+    rng = np.random.default_rng(42)
+    nd = len(distance)
+    s = np.zeros((nd, 64, 64))
+    s[2:nd - 1:2] = W.surface_roughness(X, X, 4, rng)
+    pats, kt = W.lg_modes(X, X, 16, 0.03, 0.15)
+    kw = dict(diskno=4, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=16, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=16, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    freqs = np.array([19.2e9, 20.0e9, 20.9e9])
+    b64 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs)
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    for k, f in enumerate(freqs):
+        ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
+        assert rel(b64[k], ref) < FP64_TOL
+        r2 = np.sum(np.abs(ref) ** 2)
+        assert abs(np.sum(np.abs(b32[k]) ** 2) - r2) / r2 < MIXED_BETA2_TOL
+
+
+def test_transformer_full_size_lg_vs_oracle_fixture(B):
+    """The full transformer workload (20 disks with surface maps, 64
+    Laguerre-Gauss modes, 256x256) at three of its frequencies against the
+    oracle's boost stored by tests/golden/make_c3_fixture.py: FP64 within 1e-10,
+    mixed beta^2 within 1e-4."""
+    import os
+    from bfgb300 import workloads as W
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "c3_lg_oracle.npz"))
+    w = W.config3_transformer()
+    assert np.array_equal(w["freqs"][fx["freq_index"]], fx["freqs"])
+    c = B.SeedCoordinateSystem(X=w["X"], Y=w["Y"])
+    kw = dict(diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"], epsilon=w["eps"],
+              relative_tilt_x=w["relative_tilt_x"], relative_tilt_y=w["relative_tilt_y"],
+              relative_surfaces=w["relative_surfaces"])
+    m = B.SeedModes(c, ThreeDim=True, Mmax=w["M"], Lmax=w["L"], diskR=w["diskR"],
+                    pattern_input=w["pattern_input"], kT_arr=w["kT_arr"])
+    b64 = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"])
+    b32 = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"], precision="mixed")
+    for k in range(len(fx["freqs"])):
+        assert rel(b64[k], fx["boost"][k]) < FP64_TOL
+        assert abs(np.sum(np.abs(b32[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
+
+
 def test_transformer_1d_vs_analytical1d(B):
     d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
     c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
