@@ -15,6 +15,7 @@ keep the reference behaviour):
     (complex64 fields, FP64 phase arguments and exit accumulation);
   * ``handle``: a :class:`Handle` (one per host thread; a default one is made).
 """
+import ctypes
 import math
 import threading
 
@@ -28,7 +29,7 @@ __all__ = [
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
-    "calc_propagation_matrices", "transformer",
+    "calc_propagation_matrices", "transformer", "Server",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -555,3 +556,106 @@ def transformer(bdry, coords, modes, f=10.0e9, velocity_x=0.0, prop=propagator, 
     if reflect is None:
         return boost
     return boost, refl
+
+
+_SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,
+            "transformer": _lib.BF_SOLVER_TRANSFORMER}
+
+
+class Server:
+    """A request loop over resident stacks (bf_server_create / bf_submit /
+    bf_wait).  Requests on different stacks run concurrently on ``n_workers``
+    streams, admitted by device footprint against ``hbm_budget_bytes``
+    (0 = the device's free memory).  ``dry_run`` schedules without device
+    work (a request takes ``nmax`` microseconds and holds ``footprint_bytes``),
+    for exercising the scheduler without a GPU."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0, n_workers=4, dry_run=False):
+        L = _lib.lib()
+        p = _lib._vp()
+        rc = L.bf_server_create(int(device), int(hbm_budget_bytes), int(n_workers),
+                                _lib.BF_SERVER_DRYRUN if dry_run else 0, ctypes.byref(p))
+        if rc != _lib.BF_OK:
+            raise BFError(rc, "bf_server_create failed")
+        self._p = p
+        self._live = {}   # id -> (request struct, freqs, outputs): kept alive until completion
+
+    def _check(self, rc):
+        if rc != _lib.BF_OK:
+            msg = _lib.lib().bf_server_last_error(self._p)
+            raise BFError(rc, msg.decode() if msg else "")
+
+    def submit(self, stack, freqs, solver="cheerleader", modes=None, distance=None, nmax=400, prop=None,
+               precision="mixed", beta2_scale=0.0, want_boost=False, footprint_bytes=0):
+        """Queue one solve; returns its id.  ``stack`` is a Stack (or, dry-run, any
+        non-zero integer token), ``distance`` the stack's new region distances."""
+        fr = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+        nm = modes.nm if modes is not None else 0
+        b2 = np.empty(len(fr))
+        boost = np.empty((len(fr), nm), dtype=np.complex128) if want_boost and nm else None
+        dist = None if distance is None else np.ascontiguousarray(distance, dtype=np.float64)
+        q = _lib.BFRequest()
+        q.solver = _SOLVERS[solver] if isinstance(solver, str) else int(solver)
+        q.stack = stack._s if isinstance(stack, Stack) else _lib._vp(int(stack))
+        q.modes = modes._m if modes is not None else None
+        q.nf = len(fr)
+        q.freqs = _lib.ptr(fr)
+        q.distance = _lib.ptr(dist)
+        q.nmax = int(nmax)
+        q.prop_kind = _prop_kind(prop if prop is not None else propagator)
+        q.precision = _prec(precision)
+        q.beta2_scale = float(beta2_scale)
+        q.out_beta2 = _lib.ptr(b2)
+        q.out_boost = _lib.ptr(None if boost is None else boost.view(np.float64))
+        q.footprint_bytes = int(footprint_bytes)
+        rid = _lib._ull()
+        self._check(_lib.lib().bf_submit(self._p, ctypes.byref(q), ctypes.byref(rid)))
+        self._live[rid.value] = (q, fr, dist, b2, boost)
+        return rid.value
+
+    def _result(self, rid, st, t):
+        _, _, _, b2, boost = self._live.pop(rid)
+        if st.value != _lib.BF_OK:
+            msg = _lib.lib().bf_server_last_error(self._p)
+            raise BFError(st.value, msg.decode() if msg else "")
+        return {"beta2": b2, "boost": boost, "t_submit": t[0], "t_start": t[1], "t_done": t[2]}
+
+    def wait(self, rid, timeout_ms=-1):
+        """Result dict of request ``rid`` (beta2, boost, times); TimeoutError if it
+        is still pending after ``timeout_ms``."""
+        st = _lib._c_int()
+        t = np.zeros(3)
+        rc = _lib.lib().bf_wait(self._p, rid, int(timeout_ms), ctypes.byref(st), _lib.ptr(t))
+        if rc == _lib.BF_ERR_TIMEOUT:
+            raise TimeoutError(f"request {rid} still pending")
+        self._check(rc)
+        return self._result(rid, st, t)
+
+    def poll(self, rid):
+        """None while pending, else the result dict."""
+        st = _lib._c_int()
+        t = np.zeros(3)
+        self._check(_lib.lib().bf_poll(self._p, rid, ctypes.byref(st), _lib.ptr(t)))
+        if st.value == _lib.BF_PENDING:
+            return None
+        return self._result(rid, st, t)
+
+    def stats(self, solver=None):
+        out = np.zeros(10)
+        k = -1 if solver is None else (_SOLVERS[solver] if isinstance(solver, str) else int(solver))
+        self._check(_lib.lib().bf_server_stats(self._p, k, _lib.ptr(out)))
+        keys = ["completed", "failed", "freq_points", "p50_ms", "p99_ms", "mean_ms", "max_ms", "wall_s",
+                "batched", "evictions"]
+        return dict(zip(keys, out.tolist()))
+
+    def close(self):
+        if getattr(self, "_p", None):
+            _lib.lib().bf_server_destroy(self._p)
+            self._p = None
+            self._live.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -34,6 +34,21 @@ _p_dbl = ctypes.POINTER(ctypes.c_double)
 _vp = ctypes.c_void_p
 _ull = ctypes.c_ulonglong
 
+BF_SOLVER_CHEERLEADER = 0
+BF_SOLVER_DANCER = 1
+BF_SOLVER_TRANSFORMER = 2
+BF_PENDING = -1
+BF_SERVER_DRYRUN = 1
+
+
+class BFRequest(ctypes.Structure):
+    """struct bf_request of include/boostfractor_gb300.h."""
+    _fields_ = [("solver", _c_int), ("stack", _vp), ("modes", _vp), ("nf", _c_int), ("freqs", _p_dbl),
+                ("distance", _p_dbl), ("nmax", _c_int), ("prop_kind", _c_int), ("precision", _c_int),
+                ("beta2_scale", _c_dbl), ("out_beta2", _p_dbl), ("out_boost", _p_dbl),
+                ("footprint_bytes", _ull)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/boostfractor_gb300.h
 _SIGS = {
     "bf_version": (_c_int, []),
@@ -50,6 +65,13 @@ _SIGS = {
                               _p_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
     "bf_propagate_noalloc": (_c_int, [_vp, _c_int, _vp, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl,
                                       _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
+    "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),
+    "bf_server_destroy": (_c_int, [_vp]),
+    "bf_submit": (_c_int, [_vp, ctypes.POINTER(BFRequest), ctypes.POINTER(_ull)]),
+    "bf_poll": (_c_int, [_vp, _ull, ctypes.POINTER(_c_int), _p_dbl]),
+    "bf_wait": (_c_int, [_vp, _ull, _c_int, ctypes.POINTER(_c_int), _p_dbl]),
+    "bf_server_stats": (_c_int, [_vp, _c_int, _p_dbl]),
+    "bf_server_last_error": (ctypes.c_char_p, [_vp]),
     "bf_stack_create": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                  _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, ctypes.POINTER(_vp)]),
     "bf_stack_destroy": (_c_int, [_vp, _vp]),

@@ -62,62 +62,67 @@ __global__ void __launch_bounds__(256) k_cgemm(const C* __restrict__ A, const C*
     }
 }
 
-// ---- double-float (FP32 hi/lo pair) complex GEMM -----------------------------
-// A complex number is a float4 (re_hi, re_lo, im_hi, im_lo) with re = re_hi +
-// re_lo exactly representable to ~48 bits.  Products use the FMA-exact error
-// of hi*hi plus the cross terms; sums use TwoSum, so a long, cancelling
-// contraction keeps ~1e-14 relative accuracy on the FP32 pipes.
-__device__ __forceinline__ float4 df_split(double2 v) {
-  const float rh = (float)v.x, ih = (float)v.y;
-  return make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
-}
-__device__ __forceinline__ double2 df_join(float4 v) {
-  return make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
-}
-// (sh, sl) += (xh + xl) * (yh + yl)
-__device__ __forceinline__ void df_mac(float& sh, float& sl, float xh, float xl, float yh, float yl) {
-  const float p = xh * yh;
-  float e = fmaf(xh, yh, -p);
-  e = fmaf(xh, yl, e);
-  e = fmaf(xl, yh, e);
-  const float t = sh + p;
-  const float z = t - sh;
-  const float err = (sh - (t - z)) + (p - z);
-  sl += err + e;
-  sh = t;
+// ---- complex64 operands, chunked double-float accumulation -------------------
+// C[R][Ncol] (complex128) = A[R][K] * B[K][Ncol], A and B complex64.  Each
+// thread sums TK = 16 consecutive products of an output in FP32 (error
+// ~16 u of that chunk's terms) and folds the chunk into a (hi, lo) FP32 pair
+// with TwoSum, so the rounding of a long contraction does not grow with K:
+// the result carries the complex64 rounding of the operands (random, ~6e-8 of
+// each term) and no accumulation drift.  64x64 tile per CTA of 256 threads, a
+// 4x4 block per thread; the next K tile is prefetched into registers while
+// the current one is multiplied.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float t = hi + x;
+  const float z = t - hi;
+  lo += (hi - (t - z)) + (x - z);
+  hi = t;
 }
 
-// C[R][Ncol] (complex128) = A[R][K] * B[K][Ncol], A and B double-float complex.
-__global__ void __launch_bounds__(256) k_cgemm_df(const float4* __restrict__ A, const float4* __restrict__ B,
-                                                  double2* __restrict__ Cout, int R, int K, int Ncol) {
-  constexpr int TM = 64, TN = 64, TK = 8;
-  __shared__ float4 As[TK][TM + 1];
-  __shared__ float4 Bs[TK][TN];
+__global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__ A, const float2* __restrict__ B,
+                                                       double2* __restrict__ Cout, int R, int K, int Ncol) {
+  constexpr int TM = 64, TN = 64, TK = 16;
+  __shared__ float2 As[TK][TM + 1];
+  __shared__ float2 Bs[TK][TN];
   const int tid = threadIdx.x;
   const int tr = tid / 16, tc = tid % 16;
   const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TN;
-  // accumulators: real and imaginary parts as (hi, lo)
-  float rh[4][4], rl[4][4], ih[4][4], il[4][4];
+  float hr[4][4], lr[4][4], hi[4][4], li[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) rh[i][j] = rl[i][j] = ih[i][j] = il[i][j] = 0.0f;
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int k0 = 0; k0 < K; k0 += TK) {
-    for (int e = tid; e < TM * TK; e += 256) {
+    for (int j = 0; j < 4; ++j) hr[i][j] = lr[i][j] = hi[i][j] = li[i][j] = 0.0f;
+  // each thread stages 4 A and 4 B elements per tile
+  float2 pa[4], pb[4];
+  auto fetch = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = tid + 256 * q;
       const int rr = e / TK, kk = e % TK;
       const int gr = r0 + rr, gk = k0 + kk;
-      As[kk][rr] = (gr < R && gk < K) ? A[(size_t)gr * K + gk] : z4;
+      pa[q] = (gr < R && gk < K) ? A[(size_t)gr * K + gk] : make_float2(0.f, 0.f);
+      const int kb = e / TN, cc = e % TN;
+      const int gkb = k0 + kb, gc = c0 + cc;
+      pb[q] = (gkb < K && gc < Ncol) ? B[(size_t)gkb * Ncol + gc] : make_float2(0.f, 0.f);
     }
-    for (int e = tid; e < TK * TN; e += 256) {
-      const int kk = e / TN, cc = e % TN;
-      const int gk = k0 + kk, gc = c0 + cc;
-      Bs[kk][cc] = (gk < K && gc < Ncol) ? B[(size_t)gk * Ncol + gc] : z4;
+  };
+  fetch(0);
+  for (int k0 = 0; k0 < K; k0 += TK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = tid + 256 * q;
+      As[e % TK][e / TK] = pa[q];
+      Bs[e / TN][e % TN] = pb[q];
     }
     __syncthreads();
-#pragma unroll 2
+    if (k0 + TK < K) fetch(k0 + TK);
+    float ar[4][4], ai[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) ar[i][j] = ai[i][j] = 0.0f;
+#pragma unroll
     for (int kk = 0; kk < TK; ++kk) {
-      float4 a[4], b[4];
+      float2 a[4], b[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) a[i] = As[kk][tr * 4 + i];
 #pragma unroll
@@ -126,13 +131,19 @@ __global__ void __launch_bounds__(256) k_cgemm_df(const float4* __restrict__ A, 
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          // re += ar br - ai bi ; im += ar bi + ai br
-          df_mac(rh[i][j], rl[i][j], a[i].x, a[i].y, b[j].x, b[j].y);
-          df_mac(rh[i][j], rl[i][j], -a[i].z, -a[i].w, b[j].z, b[j].w);
-          df_mac(ih[i][j], il[i][j], a[i].x, a[i].y, b[j].z, b[j].w);
-          df_mac(ih[i][j], il[i][j], a[i].z, a[i].w, b[j].x, b[j].y);
+          ar[i][j] = fmaf(a[i].x, b[j].x, ar[i][j]);
+          ar[i][j] = fmaf(-a[i].y, b[j].y, ar[i][j]);
+          ai[i][j] = fmaf(a[i].x, b[j].y, ai[i][j]);
+          ai[i][j] = fmaf(a[i].y, b[j].x, ai[i][j]);
         }
     }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        two_sum_acc(hr[i][j], lr[i][j], ar[i][j]);
+        two_sum_acc(hi[i][j], li[i][j], ai[i][j]);
+      }
     __syncthreads();
   }
 #pragma unroll
@@ -142,7 +153,7 @@ __global__ void __launch_bounds__(256) k_cgemm_df(const float4* __restrict__ A, 
       const int gr = r0 + tr * 4 + i, gc = c0 + tc + 16 * j;
       if (gr < R && gc < Ncol)
         Cout[(size_t)gr * Ncol + gc] =
-            make_double2((double)rh[i][j] + (double)rl[i][j], (double)ih[i][j] + (double)il[i][j]);
+            make_double2((double)hr[i][j] + (double)lr[i][j], (double)hi[i][j] + (double)li[i][j]);
     }
 }
 

@@ -1,0 +1,479 @@
+// Serving engine: a request loop over resident disk stacks.
+//
+// The reference's callers solve one candidate geometry per call: the
+// optimiser utilities (examples/transformer_optim_utilities.jl:11-144) move
+// the disks and call transformer again, and frequency sweeps run @distributed
+// over single-frequency calls.  Here a server accepts such solves as requests
+// (bf_submit), keeps every stack's geometry and workspace resident on the
+// device, and runs admitted requests concurrently on its workers' streams:
+//   * workers: n_workers host threads, each owning one bf_handle (one stream);
+//     a stack's workspace lives with the worker that grew it (its "home") until
+//     the workspace is released, so a stack never pays a reallocation for
+//     changing streams;
+//   * admission: the request's footprint + the bytes resident in served stacks
+//     + the running requests' footprints must fit the budget; idle stacks'
+//     workspaces are released least recently used first to make room; a queued
+//     request that does not fit is passed over by smaller ones at most
+//     kMaxPassOver times, after which nothing else starts until it fits;
+//   * order and batching: one request per stack at a time, in submission order;
+//     queued requests on the same stack with the same solver settings and no
+//     geometry change join the first one's frequency batch (one solve);
+//   * completion: beta^2 (and the transformer boost) are copied to the caller's
+//     buffers, then the status becomes final; bf_poll / bf_wait report it.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/boostfractor_gb300.h"
+#include "bf_host.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+constexpr int kMaxPassOver = 8;
+constexpr int kMaxBatchFreqs = 4096;
+
+struct Req {
+  unsigned long long id = 0;
+  bf_request r{};
+  std::vector<double> freqs, distance;
+  size_t est = 0;
+  int nm = 0;
+  int status = BF_PENDING;
+  int passed_over = 0;
+  int in_batch = 0;  // solved as part of an earlier request's batch
+  double t_submit = 0, t_start = 0, t_done = 0;
+};
+
+struct StackInfo {
+  int home = -1;      // worker holding the stack's workspace, -1 = none
+  bool busy = false;
+  double last_used = 0;
+  size_t resident = 0;
+};
+
+struct Batch {
+  std::vector<Req*> reqs;
+  size_t need = 0;
+};
+
+}  // namespace
+
+struct bf_server {
+  int device = 0, flags = 0;
+  unsigned long long budget = 0;
+  std::vector<bf_handle*> hs;
+  std::vector<std::thread> th;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Req*> queue;
+  std::unordered_map<unsigned long long, Req*> reqs;
+  std::unordered_map<bf_stack*, StackInfo> stacks;
+  size_t resident = 0, inflight = 0;
+  unsigned long long next_id = 1;
+  bool stop = false;
+  std::string err;
+  Clock::time_point t0;
+  // statistics (per solver)
+  std::vector<double> lat[3];
+  double fpts[3] = {0, 0, 0};
+  unsigned long long failed[3] = {0, 0, 0}, batched[3] = {0, 0, 0};
+  unsigned long long evictions = 0;
+  double t_first = -1.0, t_last = 0.0;
+  double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+  bool dry() const { return flags & BF_SERVER_DRYRUN; }
+};
+
+namespace {
+
+int server_fail(bf_server* s, int code, const std::string& msg) {
+  s->err = msg;
+  return code;
+}
+
+// Release the workspace of idle stacks, least recently used first, until
+// `need` more bytes fit the budget.  Caller holds the lock.
+bool make_room(bf_server* S, size_t need, const bf_stack* keep) {
+  while (S->resident + S->inflight + need > S->budget) {
+    bf_stack* victim = nullptr;
+    double oldest = 1e300;
+    for (auto& kv : S->stacks)
+      if (kv.first != keep && !kv.second.busy && kv.second.resident > 0 && kv.second.last_used < oldest) {
+        oldest = kv.second.last_used;
+        victim = kv.first;
+      }
+    if (!victim) return false;
+    StackInfo& vi = S->stacks[victim];
+    if (!S->dry()) bf_stack_trim(victim);
+    S->resident -= vi.resident;
+    vi.resident = 0;
+    vi.home = -1;
+    S->evictions++;
+  }
+  return true;
+}
+
+bool mergeable(const Req* a, const Req* b) {
+  return b->distance.empty() && a->r.solver == b->r.solver && a->r.modes == b->r.modes &&
+         a->r.nmax == b->r.nmax && a->r.prop_kind == b->r.prop_kind && a->r.precision == b->r.precision &&
+         a->r.beta2_scale == b->r.beta2_scale;
+}
+
+// The next batch worker w may start, or an empty batch.  Caller holds the lock.
+Batch pick(bf_server* S, int w) {
+  Batch b;
+  for (size_t qi = 0; qi < S->queue.size(); ++qi) {
+    Req* R = S->queue[qi];
+    StackInfo& si = S->stacks[R->r.stack];
+    if (si.busy || (si.home >= 0 && si.home != w)) continue;
+    // the workspace the stack already holds is reused by the solve
+    const size_t need = R->est > si.resident ? R->est - si.resident : 0;
+    if (!make_room(S, need, R->r.stack)) {
+      if (++R->passed_over > kMaxPassOver) return b;  // hold the line for it
+      continue;
+    }
+    // take R and the queued requests on the same stack that can join its batch
+    b.reqs.push_back(R);
+    b.need = need;
+    int nf = R->r.nf;
+    std::vector<size_t> taken = {qi};
+    for (size_t qj = qi + 1; qj < S->queue.size(); ++qj) {
+      Req* Q = S->queue[qj];
+      if (Q->r.stack != R->r.stack) continue;
+      if (!mergeable(R, Q) || nf + Q->r.nf > kMaxBatchFreqs) break;
+      if (S->resident + S->inflight + b.need + Q->est > S->budget) break;
+      b.reqs.push_back(Q);
+      b.need += Q->est;
+      nf += Q->r.nf;
+      Q->in_batch = 1;
+      taken.push_back(qj);
+    }
+    for (auto it = taken.rbegin(); it != taken.rend(); ++it) S->queue.erase(S->queue.begin() + (long)*it);
+    si.busy = true;
+    si.home = w;
+    S->inflight += b.need;
+    return b;
+  }
+  return b;
+}
+
+double default_scale(const bf_stack* s) {
+  const double dx = s->nx > 1 ? s->X[1] - s->X[0] : 1.0;
+  const double dy = s->ny > 1 ? s->Y[1] - s->Y[0] : 1.0;
+  return dx * dy / (M_PI * s->diskR * s->diskR);
+}
+
+// Run one batch on worker w's handle (no lock held).  Returns the status for
+// every request of the batch and fills their outputs.
+int run_batch(bf_server* S, int w, Batch& b, std::string& err) {
+  Req* R0 = b.reqs[0];
+  if (S->dry()) {
+    std::this_thread::sleep_for(std::chrono::microseconds((long long)R0->r.nmax * (long long)b.reqs.size()));
+    for (Req* R : b.reqs) std::fill(R->r.out_beta2, R->r.out_beta2 + R->r.nf, 0.0);
+    return BF_OK;
+  }
+  bf_handle* h = S->hs[w];
+  bf_stack* st = R0->r.stack;
+  int rc = BF_OK;
+  if (!R0->distance.empty()) rc = bf_stack_set_distance(h, st, R0->distance.data());
+  if (rc != BF_OK) { err = h->err; return rc; }
+  std::vector<double> freqs;
+  for (Req* R : b.reqs) freqs.insert(freqs.end(), R->freqs.begin(), R->freqs.end());
+  const int nf = (int)freqs.size();
+  std::vector<double> b2(nf, 0.0);
+  const bf_request& q = R0->r;
+  if (q.solver == BF_SOLVER_TRANSFORMER) {
+    bool want = false;
+    for (Req* R : b.reqs) want |= R->r.out_boost != nullptr;
+    std::vector<double> boost(want ? (size_t)nf * R0->nm * 2 : 0);
+    rc = bf_transformer(h, st, q.modes, nf, freqs.data(), q.prop_kind, q.precision, nullptr, nullptr, nullptr, 0,
+                        want ? boost.data() : nullptr, nullptr, b2.data());
+    if (rc == BF_OK && want) {
+      size_t off = 0;
+      for (Req* R : b.reqs) {
+        const size_t n = (size_t)R->r.nf * R0->nm * 2;
+        if (R->r.out_boost) std::memcpy(R->r.out_boost, boost.data() + off, sizeof(double) * n);
+        off += n;
+      }
+    }
+  } else {
+    const double scale = q.beta2_scale != 0.0 ? q.beta2_scale : default_scale(st);
+    if (q.solver == BF_SOLVER_CHEERLEADER)
+      rc = bf_stack_cheerleader(h, st, nf, freqs.data(), 0.0, q.nmax, q.prop_kind, q.precision, nullptr, nullptr, 0,
+                                scale, 0, nullptr, nullptr, b2.data());
+    else
+      rc = bf_stack_dancer(h, st, nf, freqs.data(), 0.0, q.nmax, q.prop_kind, q.precision, nullptr, nullptr, 1, 1,
+                           scale, 0, nullptr, b2.data());
+  }
+  if (rc != BF_OK) { err = h->err; return rc; }
+  size_t off = 0;
+  for (Req* R : b.reqs) {
+    std::copy(b2.begin() + (long)off, b2.begin() + (long)off + R->r.nf, R->r.out_beta2);
+    off += R->r.nf;
+  }
+  return BF_OK;
+}
+
+void worker(bf_server* S, int w) {
+  if (!S->dry()) cudaSetDevice(S->device);
+  std::unique_lock<std::mutex> lock(S->mu);
+  for (;;) {
+    Batch b;
+    S->cv_work.wait(lock, [&] {
+      if (S->stop) return true;
+      b = pick(S, w);
+      return !b.reqs.empty();
+    });
+    if (b.reqs.empty()) return;  // stopping
+    const double t_start = S->now();
+    for (Req* R : b.reqs) R->t_start = t_start;
+    lock.unlock();
+    std::string err;
+    const int rc = run_batch(S, w, b, err);
+    bf_stack* st = b.reqs[0]->r.stack;
+    const size_t res = S->dry() ? (size_t)std::max<unsigned long long>(b.reqs[0]->r.footprint_bytes, 1)
+                                : bf_stack_device_bytes(st);
+    lock.lock();
+    const double t_done = S->now();
+    StackInfo& si = S->stacks[st];
+    S->inflight -= b.need;
+    S->resident -= si.resident;
+    si.resident = res;
+    S->resident += res;
+    si.busy = false;
+    si.last_used = t_done;
+    if (rc != BF_OK) S->err = err;
+    for (Req* R : b.reqs) {
+      R->t_done = t_done;
+      R->status = rc;
+      const int k = R->r.solver;
+      if (rc == BF_OK) {
+        S->lat[k].push_back(1e3 * (t_done - R->t_submit));
+        S->fpts[k] += R->r.nf;
+      } else {
+        S->failed[k]++;
+      }
+      if (R->in_batch) S->batched[k]++;
+      R->freqs.clear();
+      R->freqs.shrink_to_fit();
+    }
+    S->t_last = std::max(S->t_last, t_done);
+    S->cv_done.notify_all();
+    S->cv_work.notify_all();
+  }
+}
+
+double percentile(std::vector<double> v, double p) {
+  if (v.empty()) return 0.0;
+  std::sort(v.begin(), v.end());
+  size_t k = (size_t)std::ceil(p * (double)v.size());
+  k = k == 0 ? 0 : k - 1;
+  return v[std::min(k, v.size() - 1)];
+}
+
+int finish(bf_server* S, std::unordered_map<unsigned long long, Req*>::iterator it, int* status, double* times) {
+  Req* R = it->second;
+  if (status) *status = R->status;
+  if (times) {
+    times[0] = R->t_submit;
+    times[1] = R->t_start;
+    times[2] = R->t_done;
+  }
+  if (R->status != BF_PENDING) {
+    delete R;
+    S->reqs.erase(it);
+  }
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_workers, int flags,
+                                bf_server** out) {
+  if (!out || n_workers < 1 || n_workers > 64) return BF_ERR_INVALID;
+  *out = nullptr;
+  bf_server* S = new bf_server();
+  S->device = device;
+  S->flags = flags;
+  S->t0 = Clock::now();
+  S->budget = hbm_budget_bytes;
+  if (!S->dry()) {
+    if (cudaSetDevice(device) != cudaSuccess) {
+      cudaGetLastError();
+      delete S;
+      return BF_ERR_CUDA;
+    }
+    if (!S->budget) {
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        delete S;
+        return BF_ERR_CUDA;
+      }
+      S->budget = fr;
+    }
+    for (int w = 0; w < n_workers; ++w) {
+      bf_handle* h = nullptr;
+      const int rc = bf_create(device, 0, &h);
+      if (rc != BF_OK) {
+        for (bf_handle* x : S->hs) bf_destroy(x);
+        delete S;
+        return rc;
+      }
+      S->hs.push_back(h);
+    }
+  } else if (!S->budget) {
+    S->budget = ~0ull;
+  }
+  for (int w = 0; w < n_workers; ++w) S->th.emplace_back(worker, S, w);
+  *out = S;
+  return BF_OK;
+}
+
+extern "C" int bf_server_destroy(bf_server* S) {
+  if (!S) return BF_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lock(S->mu);
+    S->stop = true;
+    for (Req* R : S->queue) {
+      R->status = BF_ERR_INVALID;
+      R->t_done = S->now();
+    }
+    S->queue.clear();
+    S->cv_work.notify_all();
+    S->cv_done.notify_all();
+  }
+  for (auto& t : S->th) t.join();
+  if (!S->dry())
+    for (auto& kv : S->stacks) bf_stack_trim(kv.first);
+  for (bf_handle* h : S->hs) bf_destroy(h);
+  for (auto& kv : S->reqs) delete kv.second;
+  delete S;
+  return BF_OK;
+}
+
+extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* id) {
+  if (!S || !q || !id) return BF_ERR_INVALID;
+  *id = 0;
+  if (q->solver < BF_SOLVER_CHEERLEADER || q->solver > BF_SOLVER_TRANSFORMER)
+    return server_fail(S, BF_ERR_INVALID, "unknown solver");
+  if (!q->stack || q->nf < 1 || !q->freqs || !q->out_beta2)
+    return server_fail(S, BF_ERR_INVALID, "request needs a stack, frequencies and out_beta2");
+  if (q->nf > kMaxBatchFreqs) return server_fail(S, BF_ERR_INVALID, "more than 4096 frequencies in one request");
+  for (int i = 0; i < q->nf; ++i)
+    if (!(q->freqs[i] > 0.0) || !std::isfinite(q->freqs[i]))
+      return server_fail(S, BF_ERR_INVALID, "frequencies must be finite and positive");
+  if (q->solver == BF_SOLVER_TRANSFORMER && !q->modes)
+    return server_fail(S, BF_ERR_INVALID, "a transformer request needs a mode basis");
+  if (q->solver != BF_SOLVER_TRANSFORMER && q->nmax < 0) return server_fail(S, BF_ERR_INVALID, "nmax < 0");
+  if (q->precision != BF_PREC_FP64 && q->precision != BF_PREC_MIXED)
+    return server_fail(S, BF_ERR_INVALID, "unknown precision");
+  if (S->dry() && !q->footprint_bytes)
+    return server_fail(S, BF_ERR_INVALID, "a dry-run request needs footprint_bytes");
+  Req* R = new Req();
+  R->r = *q;
+  R->freqs.assign(q->freqs, q->freqs + q->nf);
+  if (!S->dry()) {
+    if (q->distance) {
+      R->distance.assign(q->distance, q->distance + q->stack->nd);
+      for (double d : R->distance)
+        if (!std::isfinite(d)) {
+          delete R;
+          return server_fail(S, BF_ERR_INVALID, "non-finite distance");
+        }
+    }
+    if (q->solver == BF_SOLVER_TRANSFORMER && bf_modes_get(S->hs[0], q->modes, &R->nm, nullptr, nullptr) != BF_OK) {
+      delete R;
+      return server_fail(S, BF_ERR_INVALID, "invalid mode basis");
+    }
+    R->est = q->footprint_bytes ? (size_t)q->footprint_bytes
+                                : bf_solve_bytes_estimate(q->stack, q->solver, q->nf, R->nm, q->prop_kind, q->precision);
+  } else {
+    if (q->distance) R->distance.assign(1, 0.0);  // marks a geometry change (no stack to read)
+    R->est = (size_t)q->footprint_bytes;
+  }
+  std::lock_guard<std::mutex> lock(S->mu);
+  if (S->stop) {
+    delete R;
+    return server_fail(S, BF_ERR_INVALID, "server is shutting down");
+  }
+  if (R->est > S->budget) {
+    const size_t est = R->est;
+    delete R;
+    return server_fail(S, BF_ERR_NOMEM, "request footprint of " + std::to_string(est) +
+                                            " bytes exceeds the server's HBM budget");
+  }
+  R->id = S->next_id++;
+  R->t_submit = S->now();
+  if (S->t_first < 0) S->t_first = R->t_submit;
+  S->stacks.emplace(q->stack, StackInfo());
+  S->reqs[R->id] = R;
+  S->queue.push_back(R);
+  *id = R->id;
+  S->cv_work.notify_all();
+  return BF_OK;
+}
+
+extern "C" int bf_poll(bf_server* S, unsigned long long id, int* status, double* times) {
+  if (!S) return BF_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) return server_fail(S, BF_ERR_INVALID, "unknown request id");
+  return finish(S, it, status, times);
+}
+
+extern "C" int bf_wait(bf_server* S, unsigned long long id, int timeout_ms, int* status, double* times) {
+  if (!S) return BF_ERR_INVALID;
+  std::unique_lock<std::mutex> lock(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end()) return server_fail(S, BF_ERR_INVALID, "unknown request id");
+  Req* R = it->second;
+  auto done = [&] { return R->status != BF_PENDING; };
+  if (timeout_ms < 0) S->cv_done.wait(lock, done);
+  else if (!S->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), done)) {
+    if (status) *status = BF_PENDING;
+    return BF_ERR_TIMEOUT;
+  }
+  return finish(S, S->reqs.find(id), status, times);
+}
+
+extern "C" int bf_server_stats(bf_server* S, int solver, double* out) {
+  if (!S || !out || solver < -1 || solver > 2) return BF_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  std::vector<double> lat;
+  double fp = 0, nf_ = 0, nb = 0;
+  for (int k = 0; k < 3; ++k)
+    if (solver < 0 || solver == k) {
+      lat.insert(lat.end(), S->lat[k].begin(), S->lat[k].end());
+      fp += S->fpts[k];
+      nf_ += (double)S->failed[k];
+      nb += (double)S->batched[k];
+    }
+  double mean = 0, mx = 0;
+  for (double v : lat) {
+    mean += v;
+    mx = std::max(mx, v);
+  }
+  if (!lat.empty()) mean /= (double)lat.size();
+  out[0] = (double)lat.size();
+  out[1] = nf_;
+  out[2] = fp;
+  out[3] = percentile(lat, 0.50);
+  out[4] = percentile(lat, 0.99);
+  out[5] = mean;
+  out[6] = mx;
+  out[7] = S->t_first < 0 ? 0.0 : S->t_last - S->t_first;
+  out[8] = nb;
+  out[9] = (double)S->evictions;
+  return BF_OK;
+}
+
+extern "C" const char* bf_server_last_error(const bf_server* S) { return S ? S->err.c_str() : ""; }

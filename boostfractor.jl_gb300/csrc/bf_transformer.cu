@@ -94,8 +94,6 @@ __device__ __forceinline__ double2 k0_c(double lambda, double er, double ei) {
 template <typename C> __device__ __forceinline__ C dto(double2 v);
 template <> __device__ __forceinline__ float2 dto<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 template <> __device__ __forceinline__ double2 dto<double2>(double2 v) { return v; }
-// double-float storage (hi/lo FP32 pairs) of the overlap operands of the mixed path
-template <> __device__ __forceinline__ float4 dto<float4>(double2 v) { return bf::df_split(v); }
 
 struct RegionT {      // per-region data of a transformer solve
   double dz, er, ei, tx, ty;
@@ -490,7 +488,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
-  const size_t csz = 16;   // double2 or a double-float float4
+  const size_t csz = fp64 ? 16 : 8;   // double2 or float2 operands
   c.nm = nm;
   // orbits of the phasor symmetry in shifted (kX, kY) index space
   auto antisym = [](const std::vector<double>& k) {
@@ -554,7 +552,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
     dim3 grid(blocks_for(c.K), nm * nm);
     const double scale = 1.0 / ((double)nx * (double)ny);
     if (fp64) { bf::note_launch(); k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
-    else { bf::note_launch(); k_build_w<float4><<<grid, 256, 0, st>>>(c.W.as<float4>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
+    else { bf::note_launch(); k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
     TCK(cudaGetLastError());
   }
   // support pixels (any mode non-zero) and V
@@ -572,7 +570,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   {
     dim3 grid(blocks_for(c.Kd), nm * nm);
     if (fp64) { bf::note_launch(); k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
-    else { bf::note_launch(); k_build_v<float4><<<grid, 256, 0, st>>>(c.V.as<float4>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
+    else { bf::note_launch(); k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
     TCK(cudaGetLastError());
   }
   TCK(cudaStreamSynchronize(st));
@@ -592,26 +590,24 @@ static void tf_mark(bf_handle* h, int i) {
   cudaEventRecord(h->ev[i], h->stream());
 }
 
-// Class GEMM G = A * B with FP64 output: FP64 operands, or double-float
-// operands (mixed path) on the FP32 pipes.
+// Class GEMM G = A * B with FP64 output: FP64 operands (FP64 path), or
+// complex64 operands with chunked double-float accumulation (mixed path).
 template <typename S>
 static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R, int K, int N) {
   g_tf_gemm_flops += 8.0 * (double)R * (double)K * (double)N;
   dim3 grid((N + 63) / 64, (R + 63) / 64);
   bf::note_launch();
   if constexpr (std::is_same<S, double2>::value)
-    bf::k_cgemm<double2><<<grid, 256, 0, h->stream()>>>(reinterpret_cast<const double2*>(A),
-                                                        reinterpret_cast<const double2*>(B), Cm, R, K, N);
+    bf::k_cgemm<double2><<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
   else
-    bf::k_cgemm_df<<<grid, 256, 0, h->stream()>>>(reinterpret_cast<const float4*>(A),
-                                                  reinterpret_cast<const float4*>(B), Cm, R, K, N);
+    bf::k_cgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
   TCK(cudaGetLastError());
   return BF_OK;
 }
 
 // Propagation matrices of regions [j0, nd) for all frequencies into
 // P[f][j][m][m'] (FP64).  S is the operand storage of the class GEMMs:
-// double2 (FP64 path) or float4 (double-float, mixed path).
+// double2 (FP64 path) or float2 (mixed path).
 template <typename S>
 static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
                                    const std::vector<RegionT>& regs, int j0, int nf,
@@ -901,7 +897,7 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
     TCKS(tf_setup(h, s, md, fp64, &c));
     const int j0 = only_matrices ? 0 : 1;
     if (fp64) TCKS(tf_propagation_matrices<double2>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
-    else TCKS(tf_propagation_matrices<float4>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
+    else TCKS(tf_propagation_matrices<float2>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
   }
   if (only_matrices) {
     // out_pm: [nf][nd] Julia (nm, nm) column-major matrices

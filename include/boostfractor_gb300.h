@@ -229,6 +229,77 @@ int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double*
                    const double* propagation_matrices, int pm_per_freq, double* out_boost,
                    double* out_refl, double* out_beta2);
 
+/* ---- serving: a request loop over resident stacks ------------------------ */
+/* No counterpart in the reference, whose callers (the optimiser utilities,
+ * examples/transformer_optim_utilities.jl:11-144, and @distributed frequency
+ * sweeps) call transformer / cheerleader once per candidate geometry.  A server
+ * owns n_workers handles (one stream each).  Requests name a resident stack
+ * (and mode basis); requests that arrive while others run are admitted as
+ * workers and HBM budget free up, and run concurrently on the workers' streams.
+ *   - Admission: a request's device footprint (workspace + per-solve buffers,
+ *     an upper bound unless footprint_bytes is given) plus the bytes resident
+ *     in served stacks plus the running requests' footprints must fit
+ *     hbm_budget_bytes (0 = the device's free memory at creation).  Idle
+ *     stacks' workspaces are released, least recently used first, to make
+ *     room.  A request that cannot fit even alone fails at bf_submit with
+ *     BF_ERR_NOMEM.
+ *   - Order: requests on one stack run one at a time in submission order;
+ *     queued requests on a stack that have the same solver settings and no
+ *     geometry change are solved together as one frequency batch.
+ *   - Each request reports its own beta^2 (and boost), identical to a solve of
+ *     the same stack alone.
+ * The stacks and mode bases must outlive the server (bf_server_destroy
+ * releases the workspaces it grew on them). */
+typedef struct bf_server bf_server;
+
+#define BF_SOLVER_CHEERLEADER 0
+#define BF_SOLVER_DANCER      1
+#define BF_SOLVER_TRANSFORMER 2
+
+#define BF_PENDING (-1)          /* request status: queued or running */
+#define BF_SERVER_DRYRUN 1       /* schedule without device work: a request
+                                    "runs" for nmax microseconds and occupies
+                                    footprint_bytes; for testing the scheduler
+                                    on machines without a GPU */
+
+typedef struct bf_request {
+  int solver;                  /* BF_SOLVER_* */
+  bf_stack* stack;             /* resident stack (bf_stack_create) */
+  bf_modes* modes;             /* transformer: resident mode basis; else NULL */
+  int nf;                      /* frequency count */
+  const double* freqs;         /* nf frequencies [Hz], copied by bf_submit */
+  const double* distance;      /* NULL, or nd new region distances set on the stack
+                                  before the solve (an optimiser step), copied */
+  int nmax;                    /* RFP: nmax + 1 bounce iterations */
+  int prop_kind;               /* BF_PROP_* */
+  int precision;               /* BF_PREC_* */
+  double beta2_scale;          /* RFP: as in bf_stack_cheerleader; 0 = dx dy / (pi diskR^2) */
+  double* out_beta2;           /* host, nf doubles, written before completion is reported */
+  double* out_boost;           /* transformer: host nf x nm complex, or NULL */
+  unsigned long long footprint_bytes;  /* 0 = the server's estimate */
+} bf_request;
+
+int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_workers, int flags,
+                     bf_server** out);
+/* Cancels queued requests (status BF_ERR_INVALID), waits for running ones,
+ * releases the workspaces grown on served stacks and the workers. */
+int bf_server_destroy(bf_server* s);
+int bf_submit(bf_server* s, const bf_request* req, unsigned long long* id);
+/* Non-blocking: *status = BF_PENDING, or the request's final status (BF_OK or
+ * an error code).  Reporting a final status releases the id.  times (NULL or
+ * 3 doubles): submit, start and completion time in seconds since the server's
+ * creation. */
+int bf_poll(bf_server* s, unsigned long long id, int* status, double* times);
+/* Blocks up to timeout_ms (< 0: no limit); BF_ERR_TIMEOUT if the request is
+ * still pending then (the id stays valid). */
+int bf_wait(bf_server* s, unsigned long long id, int timeout_ms, int* status, double* times);
+/* out[10] for requests of one solver (BF_SOLVER_*) or all (-1): completed,
+ * failed, frequency points, latency p50 / p99 / mean / max [ms], seconds from
+ * the first submission to the last completion, requests solved as part of
+ * another's batch, stack workspaces released for admission. */
+int bf_server_stats(bf_server* s, int solver, double* out);
+const char* bf_server_last_error(const bf_server* s);
+
 #ifdef __cplusplus
 }
 #endif

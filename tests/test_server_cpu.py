@@ -1,0 +1,131 @@
+"""The serving engine's scheduler (bf_server_*), exercised without a GPU.
+
+In dry-run mode a request "runs" for nmax microseconds and holds
+footprint_bytes of device memory, so admission, ordering, batching, overlap
+and timeouts are observable from the returned submit/start/done times.
+Stacks are opaque tokens here.
+"""
+import time
+
+import numpy as np
+import pytest
+
+MB = 1 << 20
+
+
+@pytest.fixture
+def B():
+    import build as _b
+    _b.build()
+    import bfgb300
+    return bfgb300
+
+
+def times(r):
+    return r["t_submit"], r["t_start"], r["t_done"]
+
+
+def test_all_requests_complete_with_outputs(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=3, dry_run=True)
+    try:
+        ids = [srv.submit(0x1000 + 16 * (k % 5), np.linspace(1e10, 2e10, 7), nmax=2000, footprint_bytes=MB)
+               for k in range(20)]
+        res = [srv.wait(i, timeout_ms=20000) for i in ids]
+        assert all(r["beta2"].shape == (7,) and np.all(r["beta2"] == 0.0) for r in res)
+        st = srv.stats()
+        assert st["completed"] == 20 and st["failed"] == 0 and st["freq_points"] == 140
+        assert st["p99_ms"] >= st["p50_ms"] > 0.0
+        with pytest.raises(B.BFError):   # a reported id is released
+            srv.poll(ids[0])
+    finally:
+        srv.close()
+
+
+def test_one_stack_runs_in_submission_order(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=4, dry_run=True)
+    try:
+        # distance changes keep the requests from joining one batch
+        ids = [srv.submit(0x2000, [1e10], nmax=3000, distance=[0.0], footprint_bytes=MB) for _ in range(5)]
+        res = [srv.wait(i, timeout_ms=20000) for i in ids]
+        for a, b in zip(res, res[1:]):
+            assert b["t_start"] >= a["t_done"]
+        assert srv.stats()["batched"] == 0
+    finally:
+        srv.close()
+
+
+def test_queued_requests_on_a_stack_join_one_batch(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        first = srv.submit(0x3000, [1e10], nmax=50000, footprint_bytes=MB)
+        time.sleep(0.01)   # the first one is running; the next three queue behind it
+        rest = [srv.submit(0x3000, [1e10, 1.1e10], nmax=1000, footprint_bytes=MB) for _ in range(3)]
+        r0 = srv.wait(first, timeout_ms=20000)
+        rr = [srv.wait(i, timeout_ms=20000) for i in rest]
+        assert all(r["t_start"] >= r0["t_done"] for r in rr)
+        assert len({r["t_start"] for r in rr}) == 1          # one solve
+        assert srv.stats()["batched"] == 2
+    finally:
+        srv.close()
+
+
+def test_requests_on_different_stacks_overlap(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=4, dry_run=True)
+    try:
+        t0 = time.perf_counter()
+        ids = [srv.submit(0x4000 + 16 * k, [1e10], nmax=100000, footprint_bytes=MB) for k in range(4)]
+        res = [srv.wait(i, timeout_ms=20000) for i in ids]
+        wall = time.perf_counter() - t0
+        assert wall < 0.35            # 4 x 0.1 s of work on 4 workers
+        starts = sorted(r["t_start"] for r in res)
+        assert starts[-1] < min(r["t_done"] for r in res)   # all four were running together
+    finally:
+        srv.close()
+
+
+def test_admission_by_footprint_and_eviction(B):
+    # 100 MB budget, 60 MB requests on three stacks: at most one runs or stays resident at a time
+    srv = B.Server(hbm_budget_bytes=100 * MB, n_workers=3, dry_run=True)
+    try:
+        ids = [srv.submit(0x5000 + 16 * k, [1e10], nmax=20000, footprint_bytes=60 * MB) for k in range(3)]
+        res = sorted((srv.wait(i, timeout_ms=20000) for i in ids), key=lambda r: r["t_start"])
+        for a, b in zip(res, res[1:]):
+            assert b["t_start"] >= a["t_done"]
+        assert srv.stats()["evictions"] >= 2
+    finally:
+        srv.close()
+
+
+def test_request_beyond_budget_is_refused(B):
+    srv = B.Server(hbm_budget_bytes=100 * MB, n_workers=1, dry_run=True)
+    try:
+        with pytest.raises(B.BFError) as e:
+            srv.submit(0x6000, [1e10], nmax=10, footprint_bytes=200 * MB)
+        assert e.value.code == 2   # BF_ERR_NOMEM
+        with pytest.raises(B.BFError):
+            srv.submit(0x6000, [-1.0], nmax=10, footprint_bytes=MB)   # invalid frequency
+    finally:
+        srv.close()
+
+
+def test_wait_times_out_then_completes(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=1, dry_run=True)
+    try:
+        rid = srv.submit(0x7000, [1e10], nmax=300000, footprint_bytes=MB)
+        with pytest.raises(TimeoutError):
+            srv.wait(rid, timeout_ms=20)
+        assert srv.poll(rid) is None or True   # may still be pending; the id stays valid
+        r = srv.wait(rid, timeout_ms=20000)
+        assert r["t_done"] - r["t_start"] >= 0.29
+    finally:
+        srv.close()
+
+
+def test_close_cancels_queued_requests(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=1, dry_run=True)
+    srv.submit(0x8000, [1e10], nmax=100000, footprint_bytes=MB)
+    for _ in range(5):
+        srv.submit(0x8000, [1e10], nmax=100000, distance=[0.0], footprint_bytes=MB)
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 0.5   # only the running one is waited for
