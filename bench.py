@@ -417,6 +417,177 @@ def run_transformer(args):
     h.close()
 
 
+# --------------------------------------------------------------------------
+# uneven batch and serving (the request loop of bf_server)
+# --------------------------------------------------------------------------
+def _build_request_stack(B, W, h, req):
+    c = B.SeedCoordinateSystem(X=req["X"], Y=req["X"])
+    sb = B.SeedSetupBoundaries(c, diskno=req["ndisk"], distance=req["distance"], epsilon=req["eps"],
+                               relative_tilt_x=req["relative_tilt_x"], relative_tilt_y=req["relative_tilt_y"])
+    sb.eps[np.isnan(sb.eps)] = 1e30
+    st = B.Stack(sb, c, req["diskR"], handle=h)
+    modes = None
+    if req["solver"] == "transformer":
+        pats, kt = W.lg_modes(c.X, c.Y, req["M"], req["waist"], req["diskR"])
+        modes = B.SeedModes(c, ThreeDim=True, Mmax=req["M"], Lmax=0, diskR=req["diskR"], pattern_input=pats,
+                            kT_arr=kt, handle=h)
+    return st, modes
+
+
+def _solve_plain(B, h, st, modes, req, precision="mixed"):
+    """One request through the direct C ABI on handle h: beta^2 per frequency."""
+    from bfgb300 import _lib
+    fr = np.ascontiguousarray(req["freqs"], dtype=np.float64)
+    if req["solver"] == "transformer":
+        b2 = np.empty(len(fr))
+        h.check(_lib.lib().bf_transformer(h.ptr, st._s, modes._m, len(fr), _lib.ptr(fr), _lib.BF_PROP_3D,
+                                          B._prec(precision), None, None, None, 0, None, None, _lib.ptr(b2)))
+        return b2
+    return st.dancer(fr, nmax=req["nmax"], precision=precision)[1]
+
+
+def _server_line(metric, value, n_done, wall, extra):
+    line = {"metric": metric, "value": value, "unit": UNIT, "n_gpus": 1, "steps": int(n_done), "warmup": 0,
+            "ms_per_step": 1000.0 * wall / max(n_done, 1), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 fields / overlap GEMM operands, f64 phases and solves",
+            "data": "synthetic (seeded stacks, no dataset)"}
+    line.update(extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_uneven(args):
+    """Uneven batch: a seeded sample of the 4096-stack distribution (disk count
+    U{5..80}, grid {64,128,256}, U{64..1024} frequencies, half dancer / half
+    transformer) solved through the serving engine (all requests submitted at
+    once, 4 worker streams) and one after another on one handle ("plain");
+    each request's beta^2 must be the same both ways."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    reqs = W.config4_uneven()[:args.requests]
+    h = B.Handle(0)
+    plain_set = [_build_request_stack(B, W, h, r) for r in reqs]
+    batch_set = [_build_request_stack(B, W, h, r) for r in reqs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain = [_solve_plain(B, h, st, m, r) for (st, m), r in zip(plain_set, reqs)]
+    t_plain = time.perf_counter() - t0
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    clock = ClockSampler(0)
+    clock.start()
+    t0 = time.perf_counter()
+    ids = [srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision="mixed")
+           for (st, m), r in zip(batch_set, reqs)]
+    res = [srv.wait(i) for i in ids]
+    t_batch = time.perf_counter() - t0
+    clocks = clock.stop()
+    worst = max(float(np.max(np.abs(r["beta2"] - p) / np.abs(p))) for r, p in zip(res, plain))
+    fpts = sum(len(r["freqs"]) for r in reqs)
+    st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
+    srv.close()
+    for st, m in plain_set + batch_set:
+        if m is not None:
+            m.close()
+        st.close()
+    h.close()
+    _server_line(
+        "beta2 freq-points/s (uneven batch of disk stacks: 5-80 disks, 64/128/256 grids, 64-1024 freqs, "
+        "dancer + transformer)", fpts / t_batch, len(reqs), t_batch,
+        {"config": {"workload": f"uneven-batch-{len(reqs)}-of-4096-stacks", "requests": len(reqs),
+                    "dancers": sum(r["solver"] == "dancer" for r in reqs), "workers": args.workers,
+                    "dancer_bounces": reqs[0]["nmax"] + 1, "transformer_modes": reqs[0]["M"],
+                    "hbm_budget_gb": 180, "l2": "no flush: per-request working sets > L2"},
+         "plain_freqpts_per_s": fpts / t_plain, "batched_over_plain": t_plain / t_batch,
+         "beta2_max_rel_diff_batched_vs_plain": worst,
+         "latency_ms": {"p50": st_all["p50_ms"], "p99": st_all["p99_ms"], "max": st_all["max_ms"]},
+         "per_solver": {"dancer": st_d, "transformer": st_t}, "evictions": st_all["evictions"],
+         "clocks": clocks})
+
+
+def run_serve(args, optimiser_class=False):
+    """Serving loop: 32 disk-position optimiser clients, each with its own
+    resident stack; every step moves the gaps by N(0, 10 um) (bf_request.distance),
+    submits, waits for beta^2 and thinks for an exponential time of mean
+    32/2000 s (2000 requests/s offered when the service is instant).  Stacks
+    follow the uneven-batch distribution, or, with optimiser_class, are all
+    20-disk, 256-frequency transformer requests (8 Laguerre-Gauss modes,
+    128x128 over 1 m)."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    nclients = 32
+    if optimiser_class:
+        reqs = []
+        for k in range(nclients):
+            rng = np.random.default_rng(500 + k)
+            distance, eps, tx, ty = W.booster(20, rng.uniform(7.5e-3, 8.5e-3, 20))
+            reqs.append(dict(solver="transformer", ndisk=20, n=128, nf=256, distance=distance, eps=eps,
+                             relative_tilt_x=tx, relative_tilt_y=ty, X=W.symmetric_grid(128), diskR=0.15,
+                             freqs=np.linspace(19.5e9, 20.5e9, 256), nmax=0, M=8, waist=0.03))
+    else:
+        reqs = W.config4_uneven(seed=5, count=nclients)
+    h = B.Handle(0)
+    stacks = [_build_request_stack(B, W, h, r) for r in reqs]
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    # one warm-up step per client (builds the resident overlaps / plans), untimed
+    for (st, m), r in zip(stacks, reqs):
+        srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision="mixed"))
+    srv.close()
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    deadline = time.perf_counter() + args.serve_seconds
+    errors = []
+
+    def client(k):
+        rng = np.random.default_rng(1000 + k)
+        st, m = stacks[k]
+        r = reqs[k]
+        d = np.array(r["distance"])
+        try:
+            while time.perf_counter() < deadline:
+                d = W.optimiser_step(d, rng)
+                srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, distance=d, nmax=r["nmax"],
+                                    precision="mixed"))
+                time.sleep(rng.exponential(nclients / 2000.0))
+        except Exception as e:  # reported in the JSON line
+            errors.append(repr(e))
+
+    clock = ClockSampler(0)
+    clock.start()
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=client, args=(k,)) for k in range(nclients)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    wall = time.perf_counter() - t0
+    clocks = clock.stop()
+    st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
+    srv.close()
+    for st, m in stacks:
+        if m is not None:
+            m.close()
+        st.close()
+    h.close()
+    name = ("20-disk 256-frequency transformer requests (8 LG modes, 128x128)" if optimiser_class
+            else "stacks of the uneven-batch distribution")
+    _server_line(
+        f"beta2 freq-points/s and p50/p99 latency, 32 optimiser clients, {name}",
+        st_all["freq_points"] / wall, st_all["completed"], wall,
+        {"config": {"workload": "serve-optimiser-class" if optimiser_class else "serve-uneven-mix",
+                    "clients": nclients, "think_mean_ms": 1000.0 * nclients / 2000.0, "seconds": args.serve_seconds,
+                    "workers": args.workers, "hbm_budget_gb": 180, "gap_step_um": 10},
+         "latency_ms": {"p50": st_all["p50_ms"], "p99": st_all["p99_ms"], "mean": st_all["mean_ms"],
+                        "max": st_all["max_ms"]},
+         "requests_per_s": st_all["completed"] / wall, "per_solver": {"dancer": st_d, "transformer": st_t},
+         "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -460,10 +631,18 @@ def main():
     ap.add_argument("--nmax", type=int, default=None, help="override nmax (testing only)")
     ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="cheerleader", choices=["cheerleader", "transformer"])
+    ap.add_argument("--workload", default="cheerleader",
+                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt"])
+    ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
+    ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
+    ap.add_argument("--serve-seconds", type=float, default=30.0)
     args = ap.parse_args()
     if args.workload == "transformer" and args.impl == "ours":
         run_transformer(args)
+    elif args.workload == "uneven" and args.impl == "ours":
+        run_uneven(args)
+    elif args.workload in ("serve", "serve-opt") and args.impl == "ours":
+        run_serve(args, optimiser_class=args.workload == "serve-opt")
     elif args.impl == "reference":
         run_reference(args)
     else:

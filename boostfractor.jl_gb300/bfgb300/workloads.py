@@ -148,3 +148,35 @@ def fresnel_r(eps):
         a, b = np.sqrt(e[i - 1]), np.sqrt(e[i])
         r.append((a - b) / (a + b))
     return np.array(r, dtype=np.complex128)
+
+
+def config4_uneven(seed=4, count=4096, nmax=100, modes=16, waist=0.03):
+    """Uneven batch: `count` seeded disk stacks, disk count U{5..80}, grid
+    N in {64, 128, 256} over 1 m, frequency count U{64..1024} in 19.5-20.5 GHz,
+    gaps U(6, 10) mm, eps in {9.4, 24}, 1 mm disks, half dancer (nmax + 1
+    bounces, mixed precision) and half transformer (`modes` Laguerre-Gauss
+    modes of waist 3 cm, mixed precision).  Returns a list of request dicts;
+    the stacks are untilted and flat."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(count):
+        ndisk = int(rng.integers(5, 81))
+        n = int(rng.choice([64, 128, 256]))
+        nf = int(rng.integers(64, 1025))
+        eps_disk = float(rng.choice([9.4, 24.0]))
+        solver = "dancer" if rng.random() < 0.5 else "transformer"
+        gaps = rng.uniform(6e-3, 10e-3, ndisk)
+        distance, eps, tx, ty = booster(ndisk, gaps, eps_disk=eps_disk)
+        out.append(dict(name=f"c4-{k}", solver=solver, ndisk=ndisk, n=n, nf=nf, distance=distance, eps=eps,
+                        relative_tilt_x=tx, relative_tilt_y=ty, X=symmetric_grid(n), diskR=0.15,
+                        freqs=np.linspace(19.5e9, 20.5e9, nf), nmax=nmax, M=modes, waist=waist,
+                        precision="mixed"))
+    return out
+
+
+def optimiser_step(distance, rng, sigma=10e-6):
+    """One disk-position optimiser step: every gap (regions 1, 3, ..., nd-3)
+    moves by N(0, sigma)."""
+    d = np.array(distance, dtype=np.float64)
+    d[1:-1:2] += rng.normal(0.0, sigma, len(d[1:-1:2]))
+    return d
