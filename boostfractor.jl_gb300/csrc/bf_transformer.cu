@@ -95,6 +95,20 @@ template <typename C> __device__ __forceinline__ C dto(double2 v);
 template <> __device__ __forceinline__ float2 dto<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 template <> __device__ __forceinline__ double2 dto<double2>(double2 v) { return v; }
 
+// exp(re + i im) stored as C.  double2: FP64 throughout.  float2: the
+// argument (FP64) is reduced to [-pi, pi] in FP64, then sincos/exp run in FP32;
+// the result carries the complex64 rounding of the stored operand (~1e-7) and
+// no loss from large phase arguments, at the FP32 rate instead of the FP64 one.
+template <typename C> __device__ __forceinline__ C cexp_as(double re, double im);
+template <> __device__ __forceinline__ double2 cexp_as<double2>(double re, double im) { return dexp_c(re, im); }
+template <> __device__ __forceinline__ float2 cexp_as<float2>(double re, double im) {
+  const double r = im - 6.283185307179586 * rint(im * 0.15915494309189535);
+  float sn, cs;
+  sincosf((float)r, &sn, &cs);
+  const float m = expf((float)re);
+  return make_float2(m * cs, m * sn);
+}
+
 struct RegionT {      // per-region data of a transformer solve
   double dz, er, ei, tx, ty;
   int klass;          // 0 k-space, 1 pixel (disk), 2 pixel (air, 1D propagator), 3 field
@@ -148,7 +162,7 @@ __global__ void k_build_d(C* D, const int2* rep, int K, const double* freqs, int
   const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
   const double re = (k0sq.x - kx * kx) - ky * ky;
   const double2 kz = dsqrt_c(re, k0sq.y);
-  D[(size_t)o * (nf * npar) + c] = dto<C>(dexp_c(kz.y * g.dz, -kz.x * g.dz));
+  D[(size_t)o * (nf * npar) + c] = cexp_as<C>(kz.y * g.dz, -kz.x * g.dz);
 }
 
 // E[s][f*npix_regions + q]: tilt/surface phase of pixel class regions
@@ -163,6 +177,25 @@ __global__ void k_build_e(C* E, const int* supp, int Kd, const double* freqs, in
   const int reg = pix_regions[q];
   const RegionT g = regs[reg];
   const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
+  if constexpr (std::is_same<C, float2>::value) {
+    double re, im;
+    if (g.klass == 2) {
+      re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
+      im = -k0.x * g.dz;
+    } else {
+      const int x = supp[s] % nx, y = supp[s] / nx;
+      const double t = g.tx * X[x] + g.ty * Y[y];
+      re = k0.y * t;
+      im = -k0.x * t;
+      if (surf) {
+        const double2 sv = surf[(size_t)reg * npix + supp[s]];
+        re += k0.x * sv.y + k0.y * sv.x;
+        im -= k0.x * sv.x - k0.y * sv.y;
+      }
+    }
+    E[(size_t)s * (nf * npx) + c] = cexp_as<C>(re, im);
+    return;
+  }
   double2 v;
   if (g.klass == 2) {
     v = dexp_c(k0.y * g.dz, -k0.x * g.dz);   // propagator1D: exp(-i k0 dz)
@@ -182,7 +215,8 @@ __global__ void k_build_e(C* E, const int* supp, int Kd, const double* freqs, in
 
 // P[f][j][m][m'] from a class GEMM output G[mm'][f*ncols + col]; pixel-class
 // disk regions get the propagation diag(exp(-i kz_m dz)) from the left.
-__global__ void k_scatter_p(double2* P, const double2* Gm, int nf, int ncols, const RegionT* regs,
+template <typename PT>
+__global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const RegionT* regs,
                             const int* cls_regions, int nd, int nm, const double* freqs, const double2* kt,
                             int left_diag) {
   using C = double2;
@@ -202,12 +236,12 @@ __global__ void k_scatter_p(double2* P, const double2* Gm, int nf, int ncols, co
     const double2 kz = dsqrt_c(k0sq.x - ktsq.x, k0sq.y - ktsq.y);
     v = bf::cmul(dto<C>(dexp_c(kz.y * g.dz, -kz.x * g.dz)), v);
   }
-  P[(((size_t)f * nd + j) * nm) * nm + mm] = v;
+  P[(((size_t)f * nd + j) * nm) * nm + mm] = dto<PT>(v);
 }
 
 // field class: P[m][m'] = sum_x conj(Psi_m(x)) Q[m'][x]
-template <typename C>
-__global__ void k_overlap(C* P, const double2* pat, const C* Q, int nm, int npix) {
+template <typename PT, typename C>
+__global__ void k_overlap(PT* P, const double2* pat, const C* Q, int nm, int npix) {
   const int mm = blockIdx.x;
   const int m = mm / nm, mp = mm % nm;
   __shared__ double2 red[256];
@@ -227,7 +261,7 @@ __global__ void k_overlap(C* P, const double2* pat, const C* Q, int nm, int npix
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) P[mm] = dto<C>(red[0]);
+  if (threadIdx.x == 0) P[mm] = dto<PT>(red[0]);
 }
 
 template <typename C>
@@ -318,6 +352,163 @@ __global__ void __launch_bounds__(256) k_chain(const C* P, const C* Pinv, const 
     __syncthreads();
   }
   for (int m = tid; m < nm; m += nt) axg[(size_t)f * nm + m] = ax[m];
+}
+
+// ---- the chain in double-float (mixed path) -----------------------------------
+// T21 and T22 accumulate 2(nd-1) matrix products; near a resonance the final
+// solve amplifies their relative error by cond(T22) ~ 1e3-1e4, so complex64
+// storage of T (rounding ~6e-8 per step) misses the 1e-4 bar on beta^2 while
+// complex64 P and inverse(P) do not.  Here T is a (hi, lo) FP32 pair per
+// component (~48 bits): products of its hi part with the complex64 P are made
+// exact with FMA error terms and summed with TwoSum, its lo part is summed in
+// FP32, and the scalar steps use double-float arithmetic -- all on the FP32
+// pipes.  One CTA per frequency; U, V, P_j and inverse(P_j) in shared memory.
+struct DFc { float rh, rl, ih, il; };   // complex double-float
+
+__device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float z = s - a;
+  e = (a - (s - z)) + (b - z);
+}
+__device__ __forceinline__ void df_fast_two_sum(float& hi, float& lo) {
+  const float s = hi + lo;
+  lo = lo - (s - hi);
+  hi = s;
+}
+// (sh, sl) += a * b, the product exact
+__device__ __forceinline__ void df_acc_prod(float& sh, float& sl, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  float s, t;
+  df_two_sum(sh, p, s, t);
+  sh = s;
+  sl += t + e;
+}
+__device__ __forceinline__ DFc dfc_from(double2 v) {
+  DFc r;
+  r.rh = (float)v.x;
+  r.rl = (float)(v.x - (double)r.rh);
+  r.ih = (float)v.y;
+  r.il = (float)(v.y - (double)r.ih);
+  return r;
+}
+__device__ __forceinline__ double2 dfc_to_d(DFc v) {
+  return make_double2((double)v.rh + (double)v.rl, (double)v.ih + (double)v.il);
+}
+// x * y in double-float (x, y double-float; error ~1e-14 relative)
+__device__ __forceinline__ DFc dfc_mul(DFc x, DFc y) {
+  DFc r;
+  float sh = 0.f, sl = 0.f;
+  df_acc_prod(sh, sl, x.rh, y.rh);
+  df_acc_prod(sh, sl, -x.ih, y.ih);
+  sl += x.rh * y.rl + x.rl * y.rh - x.ih * y.il - x.il * y.ih;
+  df_fast_two_sum(sh, sl);
+  r.rh = sh;
+  r.rl = sl;
+  sh = 0.f;
+  sl = 0.f;
+  df_acc_prod(sh, sl, x.rh, y.ih);
+  df_acc_prod(sh, sl, x.ih, y.rh);
+  sl += x.rh * y.il + x.rl * y.ih + x.ih * y.rl + x.il * y.rh;
+  df_fast_two_sum(sh, sl);
+  r.ih = sh;
+  r.il = sl;
+  return r;
+}
+__device__ __forceinline__ DFc dfc_add(DFc x, DFc y) {
+  DFc r;
+  float e;
+  df_two_sum(x.rh, y.rh, r.rh, e);
+  r.rl = e + x.rl + y.rl;
+  df_fast_two_sum(r.rh, r.rl);
+  df_two_sum(x.ih, y.ih, r.ih, e);
+  r.il = e + x.il + y.il;
+  df_fast_two_sum(r.ih, r.il);
+  return r;
+}
+
+__global__ void __launch_bounds__(256) k_chain_df(const float2* P, const float2* Pinv, const ChainRegion* cr,
+                                                  int nd, int nm, const double2* emit, DFc* T21g, DFc* T22g,
+                                                  double2* axg, double2* T21out, double2* T22out) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int n2 = nm * nm;
+  DFc* U = reinterpret_cast<DFc*>(sm);
+  DFc* V = U + n2;
+  float2* Ps = reinterpret_cast<float2*>(V + n2);
+  float2* Qs = Ps + n2;
+  double2* ax = reinterpret_cast<double2*>(Qs + n2);
+  DFc* em = reinterpret_cast<DFc*>(ax + nm);
+  const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  DFc* T21 = T21g + (size_t)f * n2;
+  DFc* T22 = T22g + (size_t)f * n2;
+  const DFc zero = {0.f, 0.f, 0.f, 0.f}, one = {1.f, 0.f, 0.f, 0.f};
+  for (int e = tid; e < n2; e += nt) {
+    T21[e] = zero;
+    T22[e] = (e / nm) == (e % nm) ? one : zero;
+  }
+  for (int m = tid; m < nm; m += nt) {
+    ax[m] = make_double2(0.0, 0.0);
+    em[m] = dfc_from(emit[m]);
+  }
+  __syncthreads();
+  for (int j = 1; j < nd; ++j) {
+    const ChainRegion g = cr[j];
+    // axion_beam += S (T21 + T22) emit   (T of the previous step)
+    for (int m = tid; m < nm; m += nt) {
+      DFc acc = zero;
+      for (int k = 0; k < nm; ++k) acc = dfc_add(acc, dfc_mul(dfc_add(T21[m * nm + k], T22[m * nm + k]), em[k]));
+      const double2 v = dfc_to_d(acc);
+      ax[m] = bf::cadd(ax[m], bf::cmul(g.S, v));
+    }
+    // U = a T21 + b T22, V = b T21 + a T22; stage P_j and inverse(P_j)
+    const DFc a = dfc_from(g.a), b = dfc_from(g.b), sc = dfc_from(g.inv2n);
+    for (int e = tid; e < n2; e += nt) {
+      const DFc t1 = T21[e], t2 = T22[e];
+      U[e] = dfc_add(dfc_mul(a, t1), dfc_mul(b, t2));
+      V[e] = dfc_add(dfc_mul(b, t1), dfc_mul(a, t2));
+    }
+    const float2* Pj = P + (((size_t)f * nd + j) * nm) * nm;
+    const float2* Qj = Pinv + (((size_t)f * nd + j) * nm) * nm;
+    for (int e = tid; e < n2; e += nt) {
+      Ps[e] = Pj[e];
+      Qs[e] = Qj[e];
+    }
+    __syncthreads();
+    // T21 = s U P, T22 = s V inverse(P)
+    for (int e = tid; e < n2; e += nt) {
+      const int r = e / nm, c = e % nm;
+      float r1h = 0.f, r1l = 0.f, i1h = 0.f, i1l = 0.f, r2h = 0.f, r2l = 0.f, i2h = 0.f, i2l = 0.f;
+      for (int k = 0; k < nm; ++k) {
+        const DFc u = U[r * nm + k], v = V[r * nm + k];
+        const float2 p = Ps[k * nm + c], q = Qs[k * nm + c];
+        df_acc_prod(r1h, r1l, u.rh, p.x);
+        df_acc_prod(r1h, r1l, -u.ih, p.y);
+        df_acc_prod(i1h, i1l, u.rh, p.y);
+        df_acc_prod(i1h, i1l, u.ih, p.x);
+        r1l = fmaf(u.rl, p.x, fmaf(-u.il, p.y, r1l));
+        i1l = fmaf(u.rl, p.y, fmaf(u.il, p.x, i1l));
+        df_acc_prod(r2h, r2l, v.rh, q.x);
+        df_acc_prod(r2h, r2l, -v.ih, q.y);
+        df_acc_prod(i2h, i2l, v.rh, q.y);
+        df_acc_prod(i2h, i2l, v.ih, q.x);
+        r2l = fmaf(v.rl, q.x, fmaf(-v.il, q.y, r2l));
+        i2l = fmaf(v.rl, q.y, fmaf(v.il, q.x, i2l));
+      }
+      df_fast_two_sum(r1h, r1l);
+      df_fast_two_sum(i1h, i1l);
+      df_fast_two_sum(r2h, r2l);
+      df_fast_two_sum(i2h, i2l);
+      const DFc acc1 = {r1h, r1l, i1h, i1l}, acc2 = {r2h, r2l, i2h, i2l};
+      T21[e] = dfc_mul(sc, acc1);
+      T22[e] = dfc_mul(sc, acc2);
+    }
+    __syncthreads();
+  }
+  for (int m = tid; m < nm; m += nt) axg[(size_t)f * nm + m] = ax[m];
+  for (int e = tid; e < n2; e += nt) {
+    T21out[(size_t)f * n2 + e] = dfc_to_d(T21[e]);
+    T22out[(size_t)f * n2 + e] = dfc_to_d(T22[e]);
+  }
 }
 
 // ---- FP64 boundary solve: boost = -T22 \ ax, refl = -T22 \ (T21 reflect) ----
@@ -606,8 +797,8 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
 }
 
 // Propagation matrices of regions [j0, nd) for all frequencies into
-// P[f][j][m][m'] (FP64).  S is the operand storage of the class GEMMs:
-// double2 (FP64 path) or float2 (mixed path).
+// P[f][j][m][m'] stored as S, which is also the operand storage of the class
+// GEMMs: double2 (FP64 path) or float2 (mixed path).
 template <typename S>
 static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
                                    const std::vector<RegionT>& regs, int j0, int nf,
@@ -622,7 +813,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     else if (regs[j].klass == 3) freg.push_back(j);
     else preg.push_back(j);
   }
-  TCKS(P.ensure(h, sizeof(C) * (size_t)nf * nd * nm * nm));
+  TCKS(P.ensure(h, sizeof(S) * (size_t)nf * nd * nm * nm));
   DBuf d_regs, d_freq, d_kt, d_list;
   TCKS(d_regs.alloc(h, sizeof(RegionT) * regs.size()));
   TCK(cudaMemcpyAsync(d_regs.p, regs.data(), sizeof(RegionT) * regs.size(), cudaMemcpyHostToDevice, st));
@@ -648,7 +839,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
     dim3 gs(blocks_for((size_t)nm * nm), ncol);
     bf::note_launch();
-    k_scatter_p<<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
                                     d_kt.as<double2>(), 0);
     TCK(cudaGetLastError());
     TCK(cudaStreamSynchronize(st));
@@ -670,7 +861,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
     dim3 gs(blocks_for((size_t)nm * nm), ncol);
     bf::note_launch();
-    k_scatter_p<<<gs, 256, 0, st>>>(P.as<C>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
+    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
                                     d_kt.as<double2>(), 1);
     TCK(cudaGetLastError());
     TCK(cudaStreamSynchronize(st));
@@ -691,7 +882,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
         TCK(cudaGetLastError());
         TCKS(bf_general_prop(h, s, kind, true, Q.p, tmp.p, nm, fr.as<double>(), j));
         bf::note_launch();
-        k_overlap<C><<<nm * nm, 256, 0, st>>>(P.as<C>() + (((size_t)f * nd + j) * nm) * nm, md->d_pat, Q.as<C>(), nm,
+        k_overlap<S, C><<<nm * nm, 256, 0, st>>>(P.as<S>() + (((size_t)f * nd + j) * nm) * nm, md->d_pat, Q.as<C>(), nm,
                                               (int)npix);
         TCK(cudaGetLastError());
       }
@@ -861,9 +1052,14 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
 // One transformer solve (or, with only_matrices, the propagation matrices).
 // fp64 selects FP64 class-GEMM operands; otherwise double-float operands on
 // the FP32 pipes.  Propagation matrices, inverses, chain and solve are FP64.
-static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
-                  const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
-                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm) {
+// PT: storage of the propagation matrices, their inverses and the chain:
+// double2 (FP64 path) or float2 (mixed path); the boundary solve is FP64.
+template <typename PT>
+static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
+                    const double* emit, const double* reflect, const double* pm, int pm_per_freq,
+                    double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
+                    double* out_pm) {
+  constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
   std::vector<cd> eps(s->eps);
@@ -890,19 +1086,33 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
             hp[(((size_t)f * nd + j) * nm + r) * nm + cidx] = make_double2(v.real(), v.imag());
           }
       }
-    TCKS(P.alloc(h, sizeof(double2) * hp.size()));
-    TCK(cudaMemcpyAsync(P.p, hp.data(), sizeof(double2) * hp.size(), cudaMemcpyHostToDevice, st));
+    if (fp64) {
+      TCKS(P.alloc(h, sizeof(double2) * hp.size()));
+      TCK(cudaMemcpyAsync(P.p, hp.data(), sizeof(double2) * hp.size(), cudaMemcpyHostToDevice, st));
+    } else {
+      DBuf P64;
+      TCKS(P64.alloc(h, sizeof(double2) * hp.size()));
+      TCK(cudaMemcpyAsync(P64.p, hp.data(), sizeof(double2) * hp.size(), cudaMemcpyHostToDevice, st));
+      TCKS(P.alloc(h, sizeof(PT) * hp.size()));
+      if (bf::launch_convert(P64.p, true, P.p, false, hp.size(), st)) return bf_fail(h, BF_ERR_CUDA, "convert");
+    }
   } else {
     TfCache* c = nullptr;
     TCKS(tf_setup(h, s, md, fp64, &c));
     const int j0 = only_matrices ? 0 : 1;
-    if (fp64) TCKS(tf_propagation_matrices<double2>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
-    else TCKS(tf_propagation_matrices<float2>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
+    TCKS(tf_propagation_matrices<PT>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
   }
   if (only_matrices) {
     // out_pm: [nf][nd] Julia (nm, nm) column-major matrices
     std::vector<double2> hp((size_t)nf * nd * nm * nm);
-    TCK(cudaMemcpyAsync(hp.data(), P.p, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, st));
+    DBuf P64;
+    const void* src = P.p;
+    if (!fp64) {
+      TCKS(P64.alloc(h, sizeof(double2) * hp.size()));
+      if (bf::launch_convert(P.p, false, P64.p, true, hp.size(), st)) return bf_fail(h, BF_ERR_CUDA, "convert");
+      src = P64.p;
+    }
+    TCK(cudaMemcpyAsync(hp.data(), src, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
     cd* o = reinterpret_cast<cd*>(out_pm);
     for (int f = 0; f < nf; ++f)
@@ -915,10 +1125,10 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
     return BF_OK;
   }
   tf_mark(h, 1);
-  // The inverses, the chain and the boundary solve run in FP64 for either
-  // precision: near a resonance T22 is ill-conditioned and FP32 chains lose
-  // the 1e-4 bar on beta^2 (the propagation matrices themselves may be FP32).
-  using D2 = double2;
+  // P and its inverses in PT (complex64 on the mixed path: their rounding
+  // moves beta^2 by ~1e-6); the chain's T in FP64 or double-float, and the
+  // boundary solve, near resonance, in FP64.
+  using D2 = PT;
   const D2* Pd = P.as<D2>();
   TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
   {
@@ -953,15 +1163,27 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
   TCK(cudaMemcpyAsync(d_cr.p, cr.data(), sizeof(ChainRegion) * nd, cudaMemcpyHostToDevice, st));
   TCKS(d_em.alloc(h, sizeof(cd) * nm));
   TCK(cudaMemcpyAsync(d_em.p, em.data(), sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
-  TCKS(T21.alloc(h, sizeof(D2) * (size_t)nf * nm * nm));
-  TCKS(T22.alloc(h, sizeof(D2) * (size_t)nf * nm * nm));
+  // T21 / T22 for the boundary solve, FP64
+  TCKS(T21.alloc(h, sizeof(double2) * (size_t)nf * nm * nm));
+  TCKS(T22.alloc(h, sizeof(double2) * (size_t)nf * nm * nm));
   TCKS(ax.alloc(h, sizeof(double2) * (size_t)nf * nm));
-  {
+  if constexpr (fp64) {
     const size_t smem = sizeof(D2) * 2 * nm * nm + sizeof(double2) * 2 * nm;
     TCK(cudaFuncSetAttribute(k_chain<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bf::note_launch();
     k_chain<D2><<<nf, 256, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                        T21.as<D2>(), T22.as<D2>(), ax.as<double2>());
+    TCK(cudaGetLastError());
+  } else {
+    DBuf T21df, T22df;
+    TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
+    TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
+    const size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
+    TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    bf::note_launch();
+    k_chain_df<<<nf, 256, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
+                                      T21df.as<DFc>(), T22df.as<DFc>(), ax.as<double2>(), T21.as<double2>(),
+                                      T22.as<double2>());
     TCK(cudaGetLastError());
   }
   if (reflect) {
@@ -973,9 +1195,9 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
   TCKS(b2.alloc(h, sizeof(double) * nf));
   {
     const size_t smem = sizeof(double2) * nm * (nm + 2) + 256 * (sizeof(double) + sizeof(int));
-    TCK(cudaFuncSetAttribute(k_final_solve<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TCK(cudaFuncSetAttribute(k_final_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bf::note_launch();
-    k_final_solve<D2><<<nf, 256, smem, st>>>(T21.as<D2>(), T22.as<D2>(), ax.as<double2>(),
+    k_final_solve<double2><<<nf, 256, smem, st>>>(T21.as<double2>(), T22.as<double2>(), ax.as<double2>(),
                                              reflect ? d_refl.as<double2>() : nullptr, nm, boost.as<double2>(),
                                              reflect ? refl.as<double2>() : nullptr, b2.as<double>());
     TCK(cudaGetLastError());
@@ -1002,6 +1224,16 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
   if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
   return BF_OK;
+}
+
+static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
+                  const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
+                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm) {
+  if (fp64)
+    return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
+                             out_beta2, mirror_1e30, only_matrices, out_pm);
+  return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
+                          out_beta2, mirror_1e30, only_matrices, out_pm);
 }
 
 static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
