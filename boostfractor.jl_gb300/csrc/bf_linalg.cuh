@@ -78,14 +78,19 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   hi = t;
 }
 
+// blockIdx.z selects the K slice [z kchunk, (z+1) kchunk) and the output
+// plane Cout + z R Ncol (split-K for grids that would not fill the SMs).
 __global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__ A, const float2* __restrict__ B,
-                                                       double2* __restrict__ Cout, int R, int K, int Ncol) {
+                                                       double2* __restrict__ Cout, int R, int K, int Ncol,
+                                                       int kchunk) {
   constexpr int TM = 64, TN = 64, TK = 16;
   __shared__ float2 As[TK][TM + 1];
   __shared__ float2 Bs[TK][TN];
   const int tid = threadIdx.x;
   const int tr = tid / 16, tc = tid % 16;
   const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TN;
+  const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
+  Cout += (size_t)blockIdx.z * R * Ncol;
   float hr[4][4], lr[4][4], hi[4][4], li[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -99,14 +104,14 @@ __global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__
       const int e = tid + 256 * q;
       const int rr = e / TK, kk = e % TK;
       const int gr = r0 + rr, gk = k0 + kk;
-      pa[q] = (gr < R && gk < K) ? A[(size_t)gr * K + gk] : make_float2(0.f, 0.f);
+      pa[q] = (gr < R && gk < kend) ? A[(size_t)gr * K + gk] : make_float2(0.f, 0.f);
       const int kb = e / TN, cc = e % TN;
       const int gkb = k0 + kb, gc = c0 + cc;
-      pb[q] = (gkb < K && gc < Ncol) ? B[(size_t)gkb * Ncol + gc] : make_float2(0.f, 0.f);
+      pb[q] = (gkb < kend && gc < Ncol) ? B[(size_t)gkb * Ncol + gc] : make_float2(0.f, 0.f);
     }
   };
-  fetch(0);
-  for (int k0 = 0; k0 < K; k0 += TK) {
+  fetch(kbeg);
+  for (int k0 = kbeg; k0 < kend; k0 += TK) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int e = tid + 256 * q;
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__
       Bs[e / TN][e % TN] = pb[q];
     }
     __syncthreads();
-    if (k0 + TK < K) fetch(k0 + TK);
+    if (k0 + TK < kend) fetch(k0 + TK);
     float ar[4][4], ai[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -155,6 +160,19 @@ __global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__
         Cout[(size_t)gr * Ncol + gc] =
             make_double2((double)hr[i][j] + (double)lr[i][j], (double)hi[i][j] + (double)li[i][j]);
     }
+}
+
+// out[i] = sum over the split-K planes of part[z][i], in plane order
+__global__ void k_sum_planes(double2* __restrict__ out, const double2* __restrict__ part, size_t n, int planes) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double2 acc = part[i];
+    for (int z = 1; z < planes; ++z) {
+      const double2 v = part[(size_t)z * n + i];
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    out[i] = acc;
+  }
 }
 
 template <typename C>

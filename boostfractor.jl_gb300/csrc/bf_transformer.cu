@@ -147,96 +147,130 @@ __global__ void k_build_v(C* V, const double2* pat, const int* supp, int Kd, int
   V[(size_t)mm * Kd + s] = dto<C>(make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x));
 }
 
-// D[o][f*npar + p] = exp(-i sqrt(k0^2 - kx^2 - ky^2) dz) at the orbit representative
-template <typename C>
-__global__ void k_build_d(C* D, const int2* rep, int K, const double* freqs, int nf, const RegionT* regs,
-                          const int* par_regions, int npar, const double* kX, const double* kY) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;   // f * npar + p
-  if (o >= K) return;
-  const int f = c / npar, p = c % npar;
-  const RegionT g = regs[par_regions[p]];
-  const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
-  const int2 sr = rep[o];
-  const double kx = kX[sr.x], ky = kY[sr.y];
-  const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
-  const double re = (k0sq.x - kx * kx) - ky * ky;
-  const double2 kz = dsqrt_c(re, k0sq.y);
-  D[(size_t)o * (nf * npar) + c] = cexp_as<C>(kz.y * g.dz, -kz.x * g.dz);
+// kz[e][o][f] = sqrt(k0^2 - kx^2 - ky^2) at the orbit representative o, for the
+// distinct permittivities e of the k-space regions (FP64, once per solve)
+__global__ void k_build_kz(double2* KZ, const int2* rep, int K, const double* freqs, int nf, const double2* eps,
+                           const double* kX, const double* kY) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  const int e = blockIdx.z;
+  for (int o = blockIdx.y; o < K; o += gridDim.y) {
+    const double2 k0 = k0_c(kC / freqs[f], eps[e].x, eps[e].y);
+    const int2 sr = rep[o];
+    const double kx = kX[sr.x], ky = kY[sr.y];
+    const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+    const double re = (k0sq.x - kx * kx) - ky * ky;
+    KZ[((size_t)e * K + o) * nf + f] = dsqrt_c(re, k0sq.y);
+  }
 }
 
-// E[s][f*npix_regions + q]: tilt/surface phase of pixel class regions
+// D[o][f*npar + p] = exp(-i kz dz_p) (the k-space class GEMM operand)
 template <typename C>
-__global__ void k_build_e(C* E, const int* supp, int Kd, const double* freqs, int nf, const RegionT* regs,
-                          const int* pix_regions, int npx, const double* X, const double* Y, int nx,
+__global__ void k_build_d(C* D, const double2* KZ, int K, int nf, const RegionT* regs, const int* par_regions,
+                          const int* par_eps, int npar) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;   // f * npar + p
+  const int ncol = nf * npar;
+  if (c >= ncol) return;
+  const int f = c / npar, p = c % npar;
+  const double dz = regs[par_regions[p]].dz;
+  const double2* kzp = KZ + (size_t)par_eps[p] * K * nf + f;
+  for (int o = blockIdx.y; o < K; o += gridDim.y) {
+    const double2 kz = kzp[(size_t)o * nf];
+    D[(size_t)o * ncol + c] = cexp_as<C>(kz.y * dz, -kz.x * dz);
+  }
+}
+
+// k0[f][q] of the pixel-class regions (FP64)
+__global__ void k_build_k0(double2* K0, const double* freqs, int nf, const RegionT* regs, const int* pix_regions,
+                           int npx) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nf * npx) return;
+  const RegionT g = regs[pix_regions[c % npx]];
+  K0[c] = k0_c(kC / freqs[c / npx], g.er, g.ei);
+}
+
+// E[s][f*npx + q]: tilt/surface phase of pixel class regions at support pixel s
+template <typename C>
+__global__ void k_build_e(C* E, const int* supp, int Kd, int nf, const RegionT* regs, const int* pix_regions,
+                          int npx, const double2* K0, const double* X, const double* Y, int nx,
                           const double2* surf, int npix) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
-  if (s >= Kd) return;
-  const int f = c / npx, q = c % npx;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ncol = nf * npx;
+  if (c >= ncol) return;
+  const int q = c % npx;
   const int reg = pix_regions[q];
   const RegionT g = regs[reg];
-  const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
-  if constexpr (std::is_same<C, float2>::value) {
-    double re, im;
-    if (g.klass == 2) {
-      re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
-      im = -k0.x * g.dz;
-    } else {
-      const int x = supp[s] % nx, y = supp[s] / nx;
-      const double t = g.tx * X[x] + g.ty * Y[y];
-      re = k0.y * t;
-      im = -k0.x * t;
-      if (surf) {
-        const double2 sv = surf[(size_t)reg * npix + supp[s]];
-        re += k0.x * sv.y + k0.y * sv.x;
-        im -= k0.x * sv.x - k0.y * sv.y;
-      }
-    }
-    E[(size_t)s * (nf * npx) + c] = cexp_as<C>(re, im);
-    return;
-  }
-  double2 v;
-  if (g.klass == 2) {
-    v = dexp_c(k0.y * g.dz, -k0.x * g.dz);   // propagator1D: exp(-i k0 dz)
-  } else {
+  const double2 k0 = K0[c];
+  for (int s = blockIdx.y; s < Kd; s += gridDim.y) {
     const int x = supp[s] % nx, y = supp[s] / nx;
-    const double2 a = dexp_c(k0.y * g.tx * X[x], -k0.x * g.tx * X[x]);
-    const double2 b = dexp_c(k0.y * g.ty * Y[y], -k0.x * g.ty * Y[y]);
-    v = bf::cmul(a, b);
-    if (surf) {
-      const double2 sv = surf[(size_t)reg * npix + supp[s]];
-      const double re = k0.x * sv.x - k0.y * sv.y, im = k0.x * sv.y + k0.y * sv.x;
-      v = bf::cmul(v, dexp_c(im, -re));
+    if constexpr (std::is_same<C, float2>::value) {
+      double re, im;
+      if (g.klass == 2) {
+        re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
+        im = -k0.x * g.dz;
+      } else {
+        const double t = g.tx * X[x] + g.ty * Y[y];
+        re = k0.y * t;
+        im = -k0.x * t;
+        if (surf) {
+          const double2 sv = surf[(size_t)reg * npix + supp[s]];
+          re += k0.x * sv.y + k0.y * sv.x;
+          im -= k0.x * sv.x - k0.y * sv.y;
+        }
+      }
+      E[(size_t)s * ncol + c] = cexp_as<C>(re, im);
+    } else {
+      double2 v;
+      if (g.klass == 2) {
+        v = dexp_c(k0.y * g.dz, -k0.x * g.dz);
+      } else {
+        const double2 a = dexp_c(k0.y * g.tx * X[x], -k0.x * g.tx * X[x]);
+        const double2 b = dexp_c(k0.y * g.ty * Y[y], -k0.x * g.ty * Y[y]);
+        v = bf::cmul(a, b);
+        if (surf) {
+          const double2 sv = surf[(size_t)reg * npix + supp[s]];
+          const double re = k0.x * sv.x - k0.y * sv.y, im = k0.x * sv.y + k0.y * sv.x;
+          v = bf::cmul(v, dexp_c(im, -re));
+        }
+      }
+      E[(size_t)s * ncol + c] = v;
     }
   }
-  E[(size_t)s * (nf * npx) + c] = dto<C>(v);
+}
+
+// diag[f][q][m] = exp(-i kz_m dz) with kz_m = sqrt(k0^2 - kT_m^2): the
+// propagation of a pixel-class disk region in the mode basis (FP64)
+__global__ void k_build_diag(double2* DG, const double2* K0, int nf, int npx, const RegionT* regs,
+                             const int* pix_regions, const double2* kt, int nm) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nf * npx * nm) return;
+  const int m = (int)(i % nm);
+  const int c = (int)(i / nm);   // f * npx + q
+  const RegionT g = regs[pix_regions[c % npx]];
+  const double2 k0 = K0[c];
+  const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+  const double2 t = kt[m];
+  const double2 ktsq = make_double2(t.x * t.x - t.y * t.y, t.x * t.y + t.y * t.x);
+  const double2 kz = dsqrt_c(k0sq.x - ktsq.x, k0sq.y - ktsq.y);
+  DG[i] = dexp_c(kz.y * g.dz, -kz.x * g.dz);
 }
 
 // P[f][j][m][m'] from a class GEMM output G[mm'][f*ncols + col]; pixel-class
 // disk regions get the propagation diag(exp(-i kz_m dz)) from the left.
 template <typename PT>
 __global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const RegionT* regs,
-                            const int* cls_regions, int nd, int nm, const double* freqs, const double2* kt,
-                            int left_diag) {
+                            const int* cls_regions, int nd, int nm, const double2* DG) {
   using C = double2;
   const int mm = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = blockIdx.y;
   if (mm >= nm * nm) return;
-  const int f = c / ncols, q = c % ncols;
-  const int j = cls_regions[q];
-  const RegionT g = regs[j];
-  C v = Gm[(size_t)mm * (nf * ncols) + c];
-  if (left_diag && g.klass == 1) {
-    const int m = mm / nm;
-    const double2 k0 = k0_c(kC / freqs[f], g.er, g.ei);
-    const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
-    const double2 t = kt[m];
-    const double2 ktsq = make_double2(t.x * t.x - t.y * t.y, t.x * t.y + t.y * t.x);
-    const double2 kz = dsqrt_c(k0sq.x - ktsq.x, k0sq.y - ktsq.y);
-    v = bf::cmul(dto<C>(dexp_c(kz.y * g.dz, -kz.x * g.dz)), v);
+  for (int c = blockIdx.y; c < nf * ncols; c += gridDim.y) {
+    const int f = c / ncols, q = c % ncols;
+    const int j = cls_regions[q];
+    const RegionT g = regs[j];
+    C v = Gm[(size_t)mm * (nf * ncols) + c];
+    if (DG && g.klass == 1) v = bf::cmul(DG[(size_t)c * nm + mm / nm], v);
+    P[(((size_t)f * nd + j) * nm) * nm + mm] = dto<PT>(v);
   }
-  P[(((size_t)f * nd + j) * nm) * nm + mm] = dto<PT>(v);
 }
 
 // field class: P[m][m'] = sum_x conj(Psi_m(x)) Q[m'][x]
@@ -269,6 +303,77 @@ __global__ void k_copy_modes(C* out, const double2* pat, int nm, int npix, int r
   const size_t total = (size_t)reps * nm * npix;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
     out[i] = dto<C>(pat[i % ((size_t)nm * npix)]);
+}
+
+// ---- batched inversion, one warp per matrix (nm <= NM <= 32) -------------------
+// Gauss-Jordan with partial pivoting: lane r keeps row r of [A | I] in
+// registers (the column loop is unrolled, so every index is static); the
+// pivot is a warp argmax (largest |a|^2, lowest row on ties), row swaps and
+// the pivot-row broadcast are shuffles.  Rows nm..NM-1 are identity padding.
+template <typename C, int NM>
+__global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd, int j0, int nm, int nmat) {
+  using R = decltype(C().x);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int idx = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (idx >= nmat) return;   // the whole warp leaves together
+  const int nj = nd - j0;
+  const int f = idx / nj, j = j0 + idx % nj;
+  const size_t off = (((size_t)f * nd + j) * nm) * nm;
+  C a[NM], b[NM];
+#pragma unroll
+  for (int c = 0; c < NM; ++c) {
+    if (lane < nm && c < nm) a[c] = P[off + (size_t)lane * nm + c];
+    else a[c] = bf::mk(R(lane == c ? 1 : 0), R(0));
+    b[c] = bf::mk(R(lane == c ? 1 : 0), R(0));
+  }
+#pragma unroll
+  for (int c = 0; c < NM; ++c) {
+    double v = (lane >= c && lane < NM) ? bf::cabs2(a[c]) : -1.0;
+    int p = lane;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double vo = __shfl_xor_sync(FULL, v, o);
+      const int po = __shfl_xor_sync(FULL, p, o);
+      if (vo > v || (vo == v && po < p)) {
+        v = vo;
+        p = po;
+      }
+    }
+    const int src = lane == c ? p : (lane == p ? c : lane);
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+      a[k].x = __shfl_sync(FULL, a[k].x, src);
+      a[k].y = __shfl_sync(FULL, a[k].y, src);
+      b[k].x = __shfl_sync(FULL, b[k].x, src);
+      b[k].y = __shfl_sync(FULL, b[k].y, src);
+    }
+    if (lane == c) {
+      const C inv = bf::crecip(a[c]);
+#pragma unroll
+      for (int k = 0; k < NM; ++k) {
+        a[k] = bf::cmul(a[k], inv);
+        b[k] = bf::cmul(b[k], inv);
+      }
+    }
+    const C fct = a[c];
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+      C pa, pb;
+      pa.x = __shfl_sync(FULL, a[k].x, c);
+      pa.y = __shfl_sync(FULL, a[k].y, c);
+      pb.x = __shfl_sync(FULL, b[k].x, c);
+      pb.y = __shfl_sync(FULL, b[k].y, c);
+      if (lane != c) {
+        a[k] = bf::csub(a[k], bf::cmul(fct, pa));
+        b[k] = bf::csub(b[k], bf::cmul(fct, pb));
+      }
+    }
+  }
+  if (lane < nm)
+#pragma unroll
+    for (int c = 0; c < NM; ++c)
+      if (c < nm) Pinv[off + (size_t)lane * nm + c] = b[c];
 }
 
 // ---- batched inversion: Pinv[f][j] = inv(P[f][j]), j in [j0, nd) -----------
@@ -788,10 +893,27 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
   g_tf_gemm_flops += 8.0 * (double)R * (double)K * (double)N;
   dim3 grid((N + 63) / 64, (R + 63) / 64);
   bf::note_launch();
-  if constexpr (std::is_same<S, double2>::value)
+  if constexpr (std::is_same<S, double2>::value) {
     bf::k_cgemm<double2><<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
-  else
-    bf::k_cgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
+  } else {
+    // split K when the output tiles alone would leave SMs idle (few modes)
+    const long tiles = (long)grid.x * grid.y;
+    int splits = 1;
+    while (splits < 16 && tiles * splits < 2 * 152 && K / (splits * 2) >= 256) splits *= 2;
+    if (splits == 1) {
+      bf::k_cgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N, K);
+    } else {
+      const int kchunk = ((K + splits - 1) / splits + 15) / 16 * 16;
+      DBuf part;
+      TCKS(part.alloc(h, sizeof(double2) * (size_t)splits * R * N));
+      grid.z = splits;
+      bf::k_cgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, part.as<double2>(), R, K, N, kchunk);
+      TCK(cudaGetLastError());
+      const size_t n = (size_t)R * N;
+      bf::note_launch();
+      bf::k_sum_planes<<<blocks_for(n), 256, 0, h->stream()>>>(Cm, part.as<double2>(), n, splits);
+    }
+  }
   TCK(cudaGetLastError());
   return BF_OK;
 }
@@ -829,20 +951,38 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(lst.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(lst.p, kreg.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npar;
+    // distinct permittivities of the k-space regions (normally one: air)
+    std::vector<double2> eps_list;
+    std::vector<int> par_eps(npar);
+    for (int p = 0; p < npar; ++p) {
+      const RegionT& g = regs[kreg[p]];
+      int e = 0;
+      while (e < (int)eps_list.size() && !(eps_list[e].x == g.er && eps_list[e].y == g.ei)) ++e;
+      if (e == (int)eps_list.size()) eps_list.push_back(make_double2(g.er, g.ei));
+      par_eps[p] = e;
+    }
+    const int neps = (int)eps_list.size();
+    DBuf d_eps, d_peps, KZ;
+    TCKS(d_eps.alloc(h, sizeof(double2) * neps));
+    TCK(cudaMemcpyAsync(d_eps.p, eps_list.data(), sizeof(double2) * neps, cudaMemcpyHostToDevice, st));
+    TCKS(d_peps.alloc(h, sizeof(int) * npar));
+    TCK(cudaMemcpyAsync(d_peps.p, par_eps.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
+    TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
     TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
-    dim3 gd(blocks_for(c.K), ncol);
     bf::note_launch();
-    k_build_d<S><<<gd, 256, 0, st>>>(D.as<S>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, dr, lst.as<int>(),
-                                     npar, s->dkX, s->dkY);
+    k_build_kz<<<dim3(blocks_for(nf), std::min(c.K, 65535), neps), 256, 0, st>>>(
+        KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
+    TCK(cudaGetLastError());
+    bf::note_launch();
+    k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
+        D.as<S>(), KZ.as<double2>(), c.K, nf, dr, lst.as<int>(), d_peps.as<int>(), npar);
     TCK(cudaGetLastError());
     TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
-    dim3 gs(blocks_for((size_t)nm * nm), ncol);
+    dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
-    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
-                                    d_kt.as<double2>(), 0);
+    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
     TCK(cudaGetLastError());
-    TCK(cudaStreamSynchronize(st));
   }
   // pixel class: one GEMM V * E
   if (!preg.empty()) {
@@ -853,18 +993,26 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     const int ncol = nf * npx;
     TCKS(E.alloc(h, sizeof(S) * (size_t)c.Kd * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
-    dim3 ge(blocks_for(c.Kd), ncol);
+    DBuf K0, DG;
+    TCKS(K0.alloc(h, sizeof(double2) * (size_t)ncol));
+    TCKS(DG.alloc(h, sizeof(double2) * (size_t)ncol * nm));
     bf::note_launch();
-    k_build_e<S><<<ge, 256, 0, st>>>(E.as<S>(), c.supp.as<int>(), c.Kd, d_freq.as<double>(), nf, dr, lst.as<int>(),
-                                     npx, s->dX, s->dY, nx, s->d_surf, (int)npix);
+    k_build_k0<<<blocks_for(ncol), 256, 0, st>>>(K0.as<double2>(), d_freq.as<double>(), nf, dr, lst.as<int>(), npx);
+    TCK(cudaGetLastError());
+    bf::note_launch();
+    k_build_diag<<<blocks_for((size_t)ncol * nm), 256, 0, st>>>(DG.as<double2>(), K0.as<double2>(), nf, npx, dr,
+                                                               lst.as<int>(), d_kt.as<double2>(), nm);
+    TCK(cudaGetLastError());
+    bf::note_launch();
+    k_build_e<S><<<dim3(blocks_for(ncol), std::min(c.Kd, 65535)), 256, 0, st>>>(
+        E.as<S>(), c.supp.as<int>(), c.Kd, nf, dr, lst.as<int>(), npx, K0.as<double2>(), s->dX, s->dY, nx,
+        s->d_surf, (int)npix);
     TCK(cudaGetLastError());
     TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
-    dim3 gs(blocks_for((size_t)nm * nm), ncol);
+    dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
-    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, d_freq.as<double>(),
-                                    d_kt.as<double2>(), 1);
+    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, DG.as<double2>());
     TCK(cudaGetLastError());
-    TCK(cudaStreamSynchronize(st));
   }
   // field class: propagate every mode (FP64), then overlap
   if (!freg.empty()) {
@@ -886,7 +1034,6 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
                                               (int)npix);
         TCK(cudaGetLastError());
       }
-      TCK(cudaStreamSynchronize(st));
     }
   }
   return BF_OK;
@@ -1131,7 +1278,13 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   using D2 = PT;
   const D2* Pd = P.as<D2>();
   TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
-  {
+  if (nm <= 16) {
+    const int nmat = (nd - 1) * nf;
+    bf::note_launch();
+    if (nm <= 8) k_invert_warp<D2, 8><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
+    else k_invert_warp<D2, 16><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
+    TCK(cudaGetLastError());
+  } else {
     const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
     TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(nd - 1, nf);
