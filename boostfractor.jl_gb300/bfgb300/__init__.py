@@ -29,7 +29,7 @@ __all__ = [
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
-    "calc_propagation_matrices", "transformer", "Server",
+    "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -556,6 +556,47 @@ def transformer(bdry, coords, modes, f=10.0e9, velocity_x=0.0, prop=propagator, 
     if reflect is None:
         return boost
     return boost, refl
+
+
+def transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes, inlcudes_axion=False, f=10.0e9,
+                           velocity_x=0, prop=propagator, propagation_matrices=None, diskR=0.15, emit=None,
+                           precision="fp64"):
+    """src/boost_fractor_transformer.jl:372-421 on the GPU: the (nd, 2, nm)
+    array of per-region mode amplitudes (a leading frequency axis when f is an
+    array).  vcat(input_beam, reflected_beam) must have 2 nm elements, as in
+    the reference; each region's vector fills its (2, nm) slice in
+    column-major order, as the reference's slice assignment does.  The
+    keyword `inlcudes_axion` keeps the reference's spelling."""
+    freqs = np.ascontiguousarray(np.atleast_1d(f), dtype=np.float64)
+    nf, nm = len(freqs), modes.nm
+    inp = np.atleast_1d(np.asarray(input_beam, dtype=np.complex128))
+    ref = np.atleast_1d(np.asarray(reflected_beam, dtype=np.complex128))
+    if inp.size + ref.size != 2 * nm or inp.size != nm:
+        raise ValueError(f"vcat(input_beam, reflected_beam) needs {nm} + {nm} elements")
+    inp = np.ascontiguousarray(inp.reshape(nm))
+    ref = np.ascontiguousarray(ref.reshape(nm))
+    st = Stack(bdry, coords, diskR, handle=modes.h)
+    try:
+        nd = st.nd
+        ebuf = pbuf = None
+        if emit is not None:
+            ebuf = np.ascontiguousarray(emit, dtype=np.complex128).reshape(nm).view(np.float64)
+        per_freq = 0
+        if propagation_matrices is not None and len(propagation_matrices):
+            pmat = np.asarray(propagation_matrices, dtype=np.complex128)
+            if pmat.ndim == 3:
+                pmat = pmat[None]
+            per_freq = int(pmat.shape[0] == nf and nf > 1)
+            pbuf = np.ascontiguousarray(pmat.transpose(0, 1, 3, 2)).view(np.float64)
+        out = np.empty((nf, nm, 2, nd), dtype=np.complex128)   # column-major (nd, 2, nm) per frequency
+        st.h.check(_lib.lib().bf_transformer_trace_back(
+            st.h.ptr, st._s, modes._m, nf, _lib.ptr(freqs), _prop_kind(prop), _prec(precision),
+            _lib.ptr(ref.view(np.float64)), _lib.ptr(inp.view(np.float64)), 0, int(bool(inlcudes_axion)),
+            _lib.ptr(ebuf), _lib.ptr(pbuf), per_freq, _lib.ptr(out.view(np.float64))))
+    finally:
+        st.close()
+    out = out.transpose(0, 3, 2, 1)
+    return out[0] if np.ndim(f) == 0 else out
 
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,

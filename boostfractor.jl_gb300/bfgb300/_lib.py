@@ -65,6 +65,8 @@ _SIGS = {
                               _p_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
     "bf_propagate_noalloc": (_c_int, [_vp, _c_int, _vp, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl,
                                       _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
+    "bf_transformer_trace_back": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _c_int,
+                                           _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl]),
     "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),
     "bf_server_destroy": (_c_int, [_vp]),
     "bf_submit": (_c_int, [_vp, ctypes.POINTER(BFRequest), ctypes.POINTER(_ull)]),

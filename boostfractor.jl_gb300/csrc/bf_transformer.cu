@@ -616,6 +616,65 @@ __global__ void __launch_bounds__(256) k_chain_df(const float2* P, const float2*
   }
 }
 
+// ---- transformer_trace_back: per-region amplitudes, one CTA per frequency ----
+// sol <- G_j blockdiag(P_j, inverse(P_j)) sol (+ S_j [emit; emit]), j = nd-1 .. 1,
+// starting from vcat(input, reflected) in the last region; every region's
+// vector is stored into its (2, nm) slice of the column-major (nd, 2, nm)
+// output in column-major order, as the reference's slice assignment does
+// (src/boost_fractor_transformer.jl:401, :419).  Vectors in FP64.
+template <typename PT>
+__global__ void __launch_bounds__(256) k_trace_back(const PT* P, const PT* Pinv, const ChainRegion* cr, int nd,
+                                                    int nm, const double2* refl, const double2* inp,
+                                                    int beam_stride, const double2* emit, int with_axion,
+                                                    double2* out) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  double2* Rv = reinterpret_cast<double2*>(sm);
+  double2* Lv = Rv + nm;
+  double2* R2 = Lv + nm;
+  double2* L2 = R2 + nm;
+  const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
+  double2* o = out + (size_t)f * nd * 2 * nm;
+  for (int m = tid; m < nm; m += nt) {
+    Rv[m] = inp[(size_t)f * beam_stride + m];
+    Lv[m] = refl[(size_t)f * beam_stride + m];
+  }
+  __syncthreads();
+  auto put = [&](int region) {
+    for (int k = tid; k < 2 * nm; k += nt)
+      o[region + (size_t)nd * ((k % 2) + 2 * (k / 2))] = k < nm ? Rv[k] : Lv[k - nm];
+  };
+  put(nd - 1);
+  for (int st = 1; st < nd; ++st) {
+    const int j = nd - st;
+    const ChainRegion g = cr[j];
+    const PT* Pj = P + (((size_t)f * nd + j) * nm) * nm;
+    const PT* Qj = Pinv + (((size_t)f * nd + j) * nm) * nm;
+    for (int r = tid; r < nm; r += nt) {
+      double2 pr = make_double2(0.0, 0.0), ql = pr;
+      for (int k = 0; k < nm; ++k) {
+        pr = bf::cadd(pr, bf::cmul(bf::to_d(Pj[r * nm + k]), Rv[k]));
+        ql = bf::cadd(ql, bf::cmul(bf::to_d(Qj[r * nm + k]), Lv[k]));
+      }
+      double2 nr = bf::cmul(g.inv2n, bf::cadd(bf::cmul(g.a, pr), bf::cmul(g.b, ql)));
+      double2 nl = bf::cmul(g.inv2n, bf::cadd(bf::cmul(g.b, pr), bf::cmul(g.a, ql)));
+      if (with_axion) {
+        const double2 se = bf::cmul(g.S, emit[r]);
+        nr = bf::cadd(nr, se);
+        nl = bf::cadd(nl, se);
+      }
+      R2[r] = nr;
+      L2[r] = nl;
+    }
+    __syncthreads();
+    for (int m = tid; m < nm; m += nt) {
+      Rv[m] = R2[m];
+      Lv[m] = L2[m];
+    }
+    __syncthreads();
+    put(j - 1);
+  }
+}
+
 // ---- FP64 boundary solve: boost = -T22 \ ax, refl = -T22 \ (T21 reflect) ----
 template <typename C>
 __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22g, const double2* axg,
@@ -1199,13 +1258,23 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
 // One transformer solve (or, with only_matrices, the propagation matrices).
 // fp64 selects FP64 class-GEMM operands; otherwise double-float operands on
 // the FP32 pipes.  Propagation matrices, inverses, chain and solve are FP64.
+// Inputs and output of transformer_trace_back (a solve that stops after the
+// inverses and walks the regions instead of running the chain).
+struct TraceArgs {
+  const double* refl;   // reflected beam, nm complex (per frequency when per_freq)
+  const double* inp;    // input beam, nm complex (per frequency when per_freq)
+  int per_freq;
+  int axion;
+  double* out;          // nf x (nd, 2, nm) complex, column-major per frequency
+};
+
 // PT: storage of the propagation matrices, their inverses and the chain:
 // double2 (FP64 path) or float2 (mixed path); the boundary solve is FP64.
 template <typename PT>
 static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                     const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                     double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
-                    double* out_pm) {
+                    double* out_pm, const TraceArgs* tb = nullptr) {
   constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
@@ -1316,6 +1385,24 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   TCK(cudaMemcpyAsync(d_cr.p, cr.data(), sizeof(ChainRegion) * nd, cudaMemcpyHostToDevice, st));
   TCKS(d_em.alloc(h, sizeof(cd) * nm));
   TCK(cudaMemcpyAsync(d_em.p, em.data(), sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
+  if (tb) {
+    const size_t nb = (size_t)(tb->per_freq ? nf : 1) * nm;
+    DBuf d_in, d_rf, d_out;
+    TCKS(d_in.alloc(h, sizeof(cd) * nb));
+    TCK(cudaMemcpyAsync(d_in.p, tb->inp, sizeof(cd) * nb, cudaMemcpyHostToDevice, st));
+    TCKS(d_rf.alloc(h, sizeof(cd) * nb));
+    TCK(cudaMemcpyAsync(d_rf.p, tb->refl, sizeof(cd) * nb, cudaMemcpyHostToDevice, st));
+    const size_t nout = (size_t)nf * nd * 2 * nm;
+    TCKS(d_out.alloc(h, sizeof(cd) * nout));
+    bf::note_launch();
+    k_trace_back<D2><<<nf, 256, sizeof(double2) * 4 * nm, st>>>(
+        Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_rf.as<double2>(), d_in.as<double2>(),
+        tb->per_freq ? nm : 0, d_em.as<double2>(), tb->axion, d_out.as<double2>());
+    TCK(cudaGetLastError());
+    TCK(cudaMemcpyAsync(tb->out, d_out.p, sizeof(cd) * nout, cudaMemcpyDeviceToHost, st));
+    TCK(cudaStreamSynchronize(st));
+    return BF_OK;
+  }
   // T21 / T22 for the boundary solve, FP64
   TCKS(T21.alloc(h, sizeof(double2) * (size_t)nf * nm * nm));
   TCKS(T22.alloc(h, sizeof(double2) * (size_t)nf * nm * nm));
@@ -1381,12 +1468,13 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
 
 static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
                   const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
-                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm) {
+                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm,
+                  const TraceArgs* tb = nullptr) {
   if (fp64)
     return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                             out_beta2, mirror_1e30, only_matrices, out_pm);
+                             out_beta2, mirror_1e30, only_matrices, out_pm, tb);
   return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                          out_beta2, mirror_1e30, only_matrices, out_pm);
+                          out_beta2, mirror_1e30, only_matrices, out_pm, tb);
 }
 
 static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
@@ -1410,6 +1498,20 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
   TCK(cudaSetDevice(h->device));
   return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, emit, reflect, propagation_matrices,
                 pm_per_freq, out_boost, out_refl, out_beta2, 1, 0, nullptr);
+}
+
+extern "C" int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,
+                                         int prop_kind, int precision, const double* reflected_beam,
+                                         const double* input_beam, int beams_per_freq, int includes_axion,
+                                         const double* emit, const double* propagation_matrices, int pm_per_freq,
+                                         double* out) {
+  TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
+  if (!reflected_beam || !input_beam || !out) return bf_fail(h, BF_ERR_INVALID, "null beam or output");
+  TCK(cudaSetDevice(h->device));
+  TraceArgs tb{reflected_beam, input_beam, beams_per_freq ? 1 : 0, includes_axion ? 1 : 0, out};
+  // the reference's trace-back does not replace a NaN mirror permittivity (no mutation here either)
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, emit, nullptr, propagation_matrices,
+                pm_per_freq, nullptr, nullptr, nullptr, 0, 0, nullptr, &tb);
 }
 
 extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,

@@ -173,4 +173,43 @@ function transformer(bdry::SetupBoundaries, coords::CoordinateSystem, modes::Mod
     return b, (f isa Number ? refl[:, 1] : refl)
 end
 
+"""
+    transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes; inlcudes_axion=false,
+                           f=10.0e9, prop=propagator, propagation_matrices=nothing, diskR=0.15,
+                           emit=nothing, precision=:fp64)
+
+src/boost_fractor_transformer.jl:372 on the GPU: the (Nregions, 2, nm) array
+of per-region mode amplitudes.
+"""
+function transformer_trace_back(reflected_beam, input_beam, bdry::SetupBoundaries, coords::CoordinateSystem,
+                                modes::Modes; inlcudes_axion=false, f=10.0e9, velocity_x=0, prop=propagator,
+                                propagation_matrices=nothing, diskR=0.15, emit=nothing, precision=:fp64,
+                                handle=default_handle())
+    nm = modes.M * (2modes.L + 1)
+    inp = ComplexF64.(collect(input_beam))
+    ref = ComplexF64.(collect(reflected_beam))
+    length(inp) + length(ref) == 2nm || throw(DimensionMismatch("vcat(input_beam, reflected_beam) needs 2nm elements"))
+    mref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(handle, ccall((:bf_modes_create, lib), Cint,
+        (Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Float64,
+         Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Ptr{Cvoid}}),
+        handle.ptr, length(coords.X), length(coords.Y), collect(Float64, coords.X),
+        collect(Float64, coords.Y), 1, modes.M, modes.L, diskR, modes.mode_patterns, modes.mode_kt, mref))
+    s = stack(handle, bdry, coords, diskR)
+    out = Array{ComplexF64}(undef, length(bdry.eps), 2, nm)
+    pm = (propagation_matrices === nothing || isempty(propagation_matrices)) ? C_NULL :
+         reduce(hcat, vec.(propagation_matrices))
+    try
+        check(handle, ccall((:bf_transformer_trace_back, lib), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint, Ptr{ComplexF64},
+             Ptr{ComplexF64}, Cint, Cint, Ptr{ComplexF64}, Ptr{ComplexF64}, Cint, Ptr{ComplexF64}),
+            handle.ptr, s, mref[], 1, [Float64(f)], BF_PROP[prop], BF_PREC[precision], ref, inp, 0,
+            inlcudes_axion, emit === nothing ? C_NULL : ComplexF64.(emit), pm, 0, out))
+    finally
+        stack_destroy(handle, s)
+        ccall((:bf_modes_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), handle.ptr, mref[])
+    end
+    return out
+end
+
 end # module

@@ -18,7 +18,7 @@
  *   - Caller-owned host buffers are read or written only during the call.
  *     Device objects (stacks, mode bases) are owned by the handle.
  *   - A handle is not thread-safe: use one handle per host thread.  It owns
- *     one CUDA stream, its device allocations and its CUDA graphs.
+ *     one CUDA stream and its device allocations.
  */
 #ifndef BOOSTFRACTOR_GB300_H
 #define BOOSTFRACTOR_GB300_H
@@ -228,6 +228,23 @@ int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double*
                    int prop_kind, int precision, const double* emit, const double* reflect,
                    const double* propagation_matrices, int pm_per_freq, double* out_boost,
                    double* out_refl, double* out_beta2);
+
+/* transformer_trace_back for nf frequencies: starting from vcat(input_beam,
+ * reflected_beam) in the last region, apply G_s blockdiag(P_s, inv(P_s))
+ * (+ axion_S_factor [emit; emit] when includes_axion) region by region.
+ * reflected_beam, input_beam: nm complex each (nf x nm when beams_per_freq);
+ * emit: nm complex or NULL (= the modes of a uniform field in the disk);
+ * propagation_matrices as in bf_transformer.  out: per frequency the
+ * reference's (nd, 2, nm) complex array, column-major, each region's
+ * 2nm-vector stored in that slice's column-major order as the reference's
+ * slice assignment does.  The stack's permittivities are used as they are
+ * (a NaN mirror gives NaN, as in the reference).
+ * Replaces src/boost_fractor_transformer.jl:372-421. */
+int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs,
+                              int prop_kind, int precision, const double* reflected_beam,
+                              const double* input_beam, int beams_per_freq, int includes_axion,
+                              const double* emit, const double* propagation_matrices, int pm_per_freq,
+                              double* out);
 
 /* ---- serving: a request loop over resident stacks ------------------------ */
 /* No counterpart in the reference, whose callers (the optimiser utilities,

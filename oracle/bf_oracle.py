@@ -612,7 +612,14 @@ def transformer(bdry, coords, modes, f=10.0e9, velocity_x=0.0, prop=propagator,
 def transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes, inlcudes_axion=False,
                            f=10.0e9, velocity_x=0.0, prop=propagator, propagation_matrices=None,
                            diskR=0.15, emit=None):
-    """Per-region (R, L) mode amplitudes (src/boost_fractor_transformer.jl:372-421)."""
+    """Per-region mode amplitudes (src/boost_fractor_transformer.jl:372-421).
+
+    The reference stores each region's solution vector vcat(R, L) (length
+    2 nm) into the (2, nm) slice fields_regions[i, :, :] (:401, :419), which
+    Julia fills in column-major order: element k lands at (k % 2, k // 2).
+    That fill is kept here (a Fortran-order reshape); for nm = 1 it is the
+    plain (R, L) pair.  vcat(input_beam, reflected_beam) must have 2 nm
+    elements, as in the reference (a DimensionMismatch there otherwise)."""
     if emit is None:
         nx, ny = len(coords.X), len(coords.Y)
         emit = axion_induced_modes(coords, modes, B=np.ones((nx, ny)), diskR=diskR)
@@ -622,13 +629,14 @@ def transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes, inlc
     out = np.zeros((nreg, 2, nm), dtype=np.complex128)
     emit = np.atleast_1d(np.asarray(emit, dtype=np.complex128))
     both = np.concatenate([emit, emit])
-    sol = np.concatenate([np.atleast_1d(input_beam) * np.ones(nm),
-                          np.atleast_1d(reflected_beam) * np.ones(nm)]).astype(np.complex128)
+    sol = np.concatenate([np.atleast_1d(input_beam), np.atleast_1d(reflected_beam)]).astype(np.complex128)
+    if len(sol) != 2 * nm:
+        raise ValueError("vcat(input_beam, reflected_beam) must have 2 nm elements")
 
     def idx(s):
         return nreg - s
 
-    out[idx(1)] = sol.reshape(2, nm)
+    out[idx(1)] = sol.reshape((2, nm), order="F")
     for s in range(1, nreg):
         j = idx(s)
         if propagation_matrices is None:
@@ -641,7 +649,7 @@ def transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes, inlc
         sol = Gb @ sol
         if inlcudes_axion:
             sol = sol + axion_S_factor(np.sqrt(bdry.eps[idx(s + 1)]), np.sqrt(bdry.eps[j])) * both
-        out[idx(s + 1)] = sol.reshape(2, nm)
+        out[idx(s + 1)] = sol.reshape((2, nm), order="F")
     return out
 
 

@@ -67,6 +67,47 @@ def test_transformer_goldens_on_gpu(B):
     assert abs(pm[0][3, 5] - G.PROPMAT_1_4_6) / abs(G.PROPMAT_1_4_6) < G.RTOL
 
 
+def test_trace_back_golden_on_gpu(B):
+    """test/runtests.jl:196-207,221: 1D transformer over the Deps scan, then
+    transformer_trace_back of the 5th solution, through the GPU."""
+    eps = np.array([np.nan, 1, 9, 1], dtype=complex)
+    c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
+    sb1 = B.SeedSetupBoundaries(c1, diskno=1, distance=_dist(0.0), epsilon=eps)
+    m1 = B.SeedModes(c1, ThreeDim=False, Mmax=1, Lmax=0, diskR=0.15)
+    res = []
+    for d in DEPS:
+        sb1.distance = _dist(d)
+        res.append(B.transformer(sb1, c1, m1, prop=B.propagator1D, f=10e9, diskR=0.15))
+    ff = B.transformer_trace_back(res[4], 0, sb1, c1, m1, prop=B.propagator1D, f=10e9)
+    assert rel(ff[:, :, 0], np.array(G.TRACE_BACK)) < G.RTOL
+
+
+@pytest.mark.parametrize("axion", [False, True])
+def test_trace_back_3d_vs_oracle(B, axion):
+    """transformer_trace_back (transformer.jl:372-421) with L = 1 modes, tilted
+    disks and surface maps: FP64 within 1e-10 of the oracle, mixed within 1e-4."""
+    distance, eps, tx, ty, X, s = _stack(2, 40, seed=13, surf=True)
+    kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=3, Lmax=1, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=3, Lmax=1, diskR=0.15)
+    nm = mo.nm
+    rng = np.random.default_rng(14)
+    refl = rng.standard_normal(nm) + 1j * rng.standard_normal(nm)
+    inp = rng.standard_normal(nm) + 1j * rng.standard_normal(nm)
+    sbo = O.seed_setup_boundaries(co, **kw)
+    sbo.eps[0] = 1e30          # a boundary set the transformer already mutated (transformer.jl:289)
+    ref = O.transformer_trace_back(refl, inp, sbo, co, mo, inlcudes_axion=axion, f=20.1e9)
+    sbb = B.SeedSetupBoundaries(cb, **kw)
+    sbb.eps[0] = 1e30
+    got = B.transformer_trace_back(refl, inp, sbb, cb, mb, inlcudes_axion=axion, f=20.1e9)
+    assert got.shape == ref.shape == (len(distance), 2, nm)
+    assert rel(got, ref) < FP64_TOL
+    got32 = B.transformer_trace_back(refl, inp, sbb, cb, mb, inlcudes_axion=axion, f=20.1e9, precision="mixed")
+    assert rel(got32, ref) < 1e-4
+
+
 def _stack(ndisk, n, seed, tilt_air=False, surf=False):
     from bfgb300 import workloads as W
     rng = np.random.default_rng(seed)
