@@ -189,7 +189,7 @@ def SeedSetupBoundaries(coords, diskno=3, distance=None, epsilon=None, relative_
 # --------------------------------------------------------------------------
 # propagators: the prop= plug-ins (src/boost_fractor.jl:137-227)
 # --------------------------------------------------------------------------
-_PREC = {"fp64": _lib.BF_PREC_FP64, "mixed": _lib.BF_PREC_MIXED}
+_PREC = {"fp64": _lib.BF_PREC_FP64, "mixed": _lib.BF_PREC_MIXED, "tf32": _lib.BF_PREC_TF32}
 
 
 def _prec(p):

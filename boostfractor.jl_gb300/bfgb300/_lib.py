@@ -25,6 +25,7 @@ BF_NOALLOC_MAX_N = 256
 
 BF_PREC_FP64 = 0
 BF_PREC_MIXED = 1
+BF_PREC_TF32 = 2
 
 BF_OUT_DEVICE = 1
 

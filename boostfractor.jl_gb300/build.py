@@ -19,7 +19,7 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libbfgb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["bf_device.cu", "bf_api.cu", "bf_transformer.cu", "bf_noalloc.cu", "bf_server.cpp", "bf_modes.cpp"]
+SOURCES = ["bf_device.cu", "bf_api.cu", "bf_transformer.cu", "bf_noalloc.cu", "bf_tcgemm.cu", "bf_server.cpp", "bf_modes.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -52,6 +52,15 @@ int launch_fused_stage_d(int N, const FusedArgs<double2>& a, int nsteps, cudaStr
 size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64);
 bool fused_supported(int N, int nbx, int nby, bool fp64);
 
+// ---- split-TF32 tensor-core GEMM (bf_tcgemm.cu) --------------------------
+// planes[z][m][n] (FP32) = sum over the z-th of `splits` K slices of
+// (Ahi Bhi + Ahi Blo + Alo Bhi)[m][n]; A [M][Kp], B [N][Kp] row-major FP32
+// holding TF32-rounded hi/lo parts, Kp a multiple of 32, bases 16-byte
+// aligned.  *d_err becomes non-zero if a bounded wait in the kernel expired.
+int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
+                   int splits, float* planes, int* d_err, cudaStream_t st);
+bool tc_gemm_available();
+
 // ---- phasor / tilt tables (FP64 phase arguments) -----------------------
 struct RegionGeo {
   double dz;

@@ -1,0 +1,275 @@
+// Split-TF32 GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+//   planes[z][m][n] = sum_{k in slice z} (Ahi Bhi + Ahi Blo + Alo Bhi)[m][n]
+//
+// A is [M][Kp] and B is [N][Kp] (both K-major, FP32 containers holding values
+// already rounded to TF32: hi = tf32(x), lo = tf32(x - hi)), Kp a multiple of 32.
+// The three products recover ~21 bits of each operand.  The FP32 accumulation
+// of one K slice lives in tensor memory; the slices (planes) are summed in
+// FP64 afterwards.  The tensor cores' accumulation truncates (about half an
+// FP32 ulp of the running sum is lost per accumulation), so the error of a
+// slice grows with its depth.
+//
+// One CTA computes one 128 x 128 tile of one plane with 6 warps:
+//   warp 0     one thread issues the TMA loads (128B-swizzled tiles of A_hi,
+//              A_lo, B_hi, B_lo, 32 K-elements each) into a 3-stage ring;
+//   warp 1     allocates 128 TMEM columns; one thread issues the MMAs
+//              (kind::tf32, M = 128, N = 128, K = 8; 3 per K-step) and
+//              commits each stage back to the producer and the last one to
+//              the epilogue;
+//   warps 2-5  read the accumulator (tcgen05.ld 32x32b, each warp its 32 TMEM
+//              lanes) and store the FP32 tile.
+// Every mbarrier wait is bounded: after ~2 s of clock it records an error in
+// *err and gives up, and the CTA still frees its tensor memory.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "bf_device.cuh"
+
+namespace bf {
+
+namespace {
+
+constexpr int kTM = 128, kTN = 128, kTK = 32, kStages = 3;
+constexpr int kTileBytes = kTM * kTK * 4;              // 16 KB: one operand tile (also B, kTN = kTM)
+constexpr int kStageBytes = 4 * kTileBytes;            // A_hi, A_lo, B_hi, B_lo
+constexpr int kThreads = 192;
+constexpr uint32_t kTmemCols = 128;
+constexpr long long kWaitCycles = 4000000000LL;        // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// Bounded wait for the phase with the given parity; false (and *err set) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > kWaitCycles) {
+      atomicExch(err, code);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// groups 1024 B apart (SBO), start address in 16-byte units.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;              // leading-dimension offset (unused with a 128B K extent)
+  d |= (uint64_t)(1024 >> 4) << 32;    // stride-dimension offset
+  d |= (uint64_t)1 << 46;              // descriptor version
+  d |= (uint64_t)2 << 61;              // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor, kind::tf32: FP32 accumulator, TF32 A and B, both
+// K-major, N = 128, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTN >> 3) << 17) |
+                            ((uint32_t)(kTM >> 4) << 24);
+
+__device__ __forceinline__ void umma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_tc_gemm_tf32x3(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+                     const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+                     float* __restrict__ planes, int M, int N, int ktiles, int kt_per_slice, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte alignment of the tile ring (128B swizzle atoms)
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + kStages * kStageBytes);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 1);
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + kStages), done = smem_u32(bars + 2 * kStages);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * kTM, n0 = blockIdx.x * kTN, z = blockIdx.z;
+  const int kt0 = z * kt_per_slice;
+  const int nkt = max(0, min(ktiles, kt0 + kt_per_slice) - kt0);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(full0 + 8 * s, 1);
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0 && nkt > 0) {
+    // producer: TMA loads into the stage ring
+    int issued = 0;
+    for (int kt = 0; kt < nkt; ++kt, ++issued) {
+      const int s = kt % kStages;
+      if (kt >= kStages && !mbar_wait(empty0 + 8 * s, ((kt / kStages) - 1) & 1, err, 1)) break;
+      const uint32_t st = smem_u32(smem + s * kStageBytes);
+      const uint32_t fb = full0 + 8 * s;
+      mbar_expect_tx(fb, kStageBytes);
+      const int k = (kt0 + kt) * kTK;
+      tma_load_2d(st, &mAhi, k, m0, fb);
+      tma_load_2d(st + kTileBytes, &mAlo, k, m0, fb);
+      tma_load_2d(st + 2 * kTileBytes, &mBhi, k, n0, fb);
+      tma_load_2d(st + 3 * kTileBytes, &mBlo, k, n0, fb);
+    }
+    // the last stages' copies must have landed before the CTA may exit
+    // (they have, unless a wait above timed out); bounded as well
+    for (int kt = max(0, issued - kStages); kt < issued; ++kt)
+      if (!mbar_wait(full0 + 8 * (kt % kStages), (kt / kStages) & 1, err, 4)) break;
+  } else if (warp == 1 && lane == 0 && nkt > 0) {
+    // MMA issuer
+    for (int kt = 0; kt < nkt; ++kt) {
+      const int s = kt % kStages;
+      if (!mbar_wait(full0 + 8 * s, (kt / kStages) & 1, err, 2)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t st = smem_u32(smem + s * kStageBytes);
+      const uint64_t ahi = umma_desc(st), alo = umma_desc(st + kTileBytes);
+      const uint64_t bhi = umma_desc(st + 2 * kTileBytes), blo = umma_desc(st + 3 * kTileBytes);
+#pragma unroll
+      for (int kk = 0; kk < kTK / 8; ++kk) {
+        const uint64_t adv = (uint64_t)(kk * 32 >> 4);   // 8 TF32 = 32 bytes along K
+        umma_tf32(tmem, ahi + adv, bhi + adv, (kt > 0 || kk > 0) ? 1u : 0u);
+        umma_tf32(tmem, ahi + adv, blo + adv, 1u);
+        umma_tf32(tmem, alo + adv, bhi + adv, 1u);
+      }
+      umma_commit(empty0 + 8 * s);
+    }
+    umma_commit(done);
+  } else if (warp >= 2) {
+    // epilogue: TMEM -> registers -> FP32 plane
+    const int q = warp & 3;   // this warp's TMEM lane quarter
+    const int row = m0 + q * 32 + lane;
+    float* dst = planes + ((size_t)z * M + row) * N;
+    const bool ok = nkt > 0 && mbar_wait(done, 0, err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTN; c0 += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+          "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c0 + j;
+          if (n < N) dst[n] = ok ? __uint_as_float(v[j]) : 0.0f;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encoder() {
+  static std::once_flag once;
+  static EncodeTiled fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// 2D map of a row-major [rows][kp] FP32 array, boxes of 32 x 128, 128B swizzle.
+bool make_map(CUtensorMap* m, const float* base, int rows, int kp) {
+  EncodeTiled enc = encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)kp * sizeof(float)};
+  const cuuint32_t box[2] = {(cuuint32_t)kTK, (cuuint32_t)kTM};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+size_t tc_gemm_smem_bytes() { return (size_t)kStages * kStageBytes + 1024 + 256; }
+
+bool tc_gemm_available() { return encoder() != nullptr; }
+
+int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
+                   int splits, float* planes, int* d_err, cudaStream_t st) {
+  if (Kp % kTK || M < 1 || N < 1 || splits < 1) return (int)cudaErrorInvalidValue;
+  // TMA: 16-byte aligned bases (pool allocations) and row strides
+  for (const float* p : {Ahi, Alo, Bhi, Blo})
+    if (reinterpret_cast<uintptr_t>(p) & 15) return (int)cudaErrorInvalidValue;
+  CUtensorMap mAhi, mAlo, mBhi, mBlo;
+  if (!make_map(&mAhi, Ahi, M, Kp) || !make_map(&mAlo, Alo, M, Kp) || !make_map(&mBhi, Bhi, N, Kp) ||
+      !make_map(&mBlo, Blo, N, Kp))
+    return (int)cudaErrorInvalidValue;
+  const int ktiles = Kp / kTK;
+  const int per = (ktiles + splits - 1) / splits;
+  const size_t smem = tc_gemm_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  dim3 grid((N + kTN - 1) / kTN, (M + kTM - 1) / kTM, splits);
+  note_launch();
+  k_tc_gemm_tf32x3<<<grid, kThreads, smem, st>>>(mAhi, mAlo, mBhi, mBlo, planes, M, N, ktiles, per, d_err);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace bf

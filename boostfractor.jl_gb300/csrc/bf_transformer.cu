@@ -147,20 +147,110 @@ __global__ void k_build_v(C* V, const double2* pat, const int* supp, int Kd, int
   V[(size_t)mm * Kd + s] = dto<C>(make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x));
 }
 
-// kz[e][o][f] = sqrt(k0^2 - kx^2 - ky^2) at the orbit representative o, for the
+// kz[e][f][o] = sqrt(k0^2 - kx^2 - ky^2) at the orbit representative o, for the
 // distinct permittivities e of the k-space regions (FP64, once per solve)
 __global__ void k_build_kz(double2* KZ, const int2* rep, int K, const double* freqs, int nf, const double2* eps,
                            const double* kX, const double* kY) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= nf) return;
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K) return;
   const int e = blockIdx.z;
-  for (int o = blockIdx.y; o < K; o += gridDim.y) {
+  const int2 sr = rep[o];
+  const double kx = kX[sr.x], ky = kY[sr.y];
+  for (int f = blockIdx.y; f < nf; f += gridDim.y) {
     const double2 k0 = k0_c(kC / freqs[f], eps[e].x, eps[e].y);
-    const int2 sr = rep[o];
-    const double kx = kX[sr.x], ky = kY[sr.y];
     const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
     const double re = (k0sq.x - kx * kx) - ky * ky;
-    KZ[((size_t)e * K + o) * nf + f] = dsqrt_c(re, k0sq.y);
+    KZ[((size_t)e * nf + f) * K + o] = dsqrt_c(re, k0sq.y);
+  }
+}
+
+// TF32 hi/lo pair of x: hi = tf32(x), lo = tf32(x - hi) (round to nearest)
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  hi = __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - hi));
+  lo = __uint_as_float(l);
+}
+__device__ __forceinline__ void tf32_split_d(double x, float& hi, float& lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"((float)x));
+  hi = __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"((float)(x - (double)hi)));
+  lo = __uint_as_float(l);
+}
+
+// ---- operands of the tensor-core class GEMMs (BF_PREC_TF32) -------------------
+// The complex product G = A B becomes the real product [Gr; Gi] = A'' B'' with
+// A'' = [[Ar, -Ai], [Ai, Ar]] (2R x 2Kp) and B'' = [Br; Bi] (2Kp x N), both
+// stored K-major (B'' transposed, [N][2Kp]) as TF32 hi/lo pairs.  Columns
+// [0, K) hold real parts, [Kp, Kp + K) imaginary parts, the rest are zero.
+__device__ __forceinline__ void put_a2(float* Ahi, float* Alo, int R, int Kp, int row, int k, double re, double im) {
+  const size_t w = 2 * (size_t)Kp;
+  float h, l;
+  tf32_split_d(re, h, l);
+  Ahi[(size_t)row * w + k] = h;
+  Alo[(size_t)row * w + k] = l;
+  Ahi[(size_t)(R + row) * w + Kp + k] = h;
+  Alo[(size_t)(R + row) * w + Kp + k] = l;
+  tf32_split_d(im, h, l);
+  Ahi[(size_t)(R + row) * w + k] = h;
+  Alo[(size_t)(R + row) * w + k] = l;
+  Ahi[(size_t)row * w + Kp + k] = -h;
+  Alo[(size_t)row * w + Kp + k] = -l;
+}
+__device__ __forceinline__ void put_bt(float* Bhi, float* Blo, int Kp, int c, int k, float re, float im) {
+  const size_t w = 2 * (size_t)Kp;
+  float h, l;
+  tf32_split(re, h, l);
+  Bhi[(size_t)c * w + k] = h;
+  Blo[(size_t)c * w + k] = l;
+  tf32_split(im, h, l);
+  Bhi[(size_t)c * w + Kp + k] = h;
+  Blo[(size_t)c * w + Kp + k] = l;
+}
+
+// A'' of the k-space class from the FP64 orbit sums (rows mm = m nm + m')
+__global__ void k_build_w_t(float* Ahi, float* Alo, const double2* U, const double2* Phi, const int* members, int K,
+                            int Kp, int msz, int nm, int npix, double scale) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mm = blockIdx.y;
+  if (o >= K) return;
+  const int m = mm / nm, mp = mm % nm;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int q = 0; q < msz; ++q) {
+    const int k = members[(size_t)o * msz + q];
+    if (k < 0) break;
+    const double2 u = U[(size_t)m * npix + k], p = Phi[(size_t)mp * npix + k];
+    acc.x += u.x * p.x + u.y * p.y;
+    acc.y += u.x * p.y - u.y * p.x;
+  }
+  put_a2(Ahi, Alo, nm * nm, Kp, mm, o, acc.x * scale, acc.y * scale);
+}
+
+// A'' of the pixel class: conj(Psi_m(x_s)) Psi_m'(x_s)
+__global__ void k_build_v_t(float* Ahi, float* Alo, const double2* pat, const int* supp, int Kd, int Kdp, int nm,
+                            int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int mm = blockIdx.y;
+  if (s >= Kd) return;
+  const int m = mm / nm, mp = mm % nm;
+  const int x = supp[s];
+  const double2 a = pat[(size_t)m * npix + x], b = pat[(size_t)mp * npix + x];
+  put_a2(Ahi, Alo, nm * nm, Kdp, mm, s, a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+// G[r][n] = (sum_z planes[z][r][n], sum_z planes[z][R + r][n]), planes in order
+__global__ void k_planes_to_g(double2* G, const float* planes, int R, int N, int splits) {
+  const size_t n_out = (size_t)R * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n_out; i += (size_t)gridDim.x * blockDim.x) {
+    double re = 0.0, im = 0.0;
+    for (int z = 0; z < splits; ++z) {
+      const float* pz = planes + (size_t)z * 2 * n_out;
+      re += (double)pz[i];
+      im += (double)pz[n_out + i];
+    }
+    G[i] = make_double2(re, im);
   }
 }
 
@@ -173,10 +263,28 @@ __global__ void k_build_d(C* D, const double2* KZ, int K, int nf, const RegionT*
   if (c >= ncol) return;
   const int f = c / npar, p = c % npar;
   const double dz = regs[par_regions[p]].dz;
-  const double2* kzp = KZ + (size_t)par_eps[p] * K * nf + f;
+  const double2* kzp = KZ + ((size_t)par_eps[p] * nf + f) * K;
   for (int o = blockIdx.y; o < K; o += gridDim.y) {
-    const double2 kz = kzp[(size_t)o * nf];
+    const double2 kz = kzp[o];
     D[(size_t)o * ncol + c] = cexp_as<C>(kz.y * dz, -kz.x * dz);
+  }
+}
+
+// B''^T of the k-space class: row c = f * npar + p, column o (orbit)
+__global__ void k_build_d_t(float* Bhi, float* Blo, const double2* KZ, int K, int Kp, int nf, const RegionT* regs,
+                            const int* par_regions, const int* par_eps, int npar) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= Kp) return;
+  const int ncol = nf * npar;
+  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+    float2 v = make_float2(0.f, 0.f);
+    if (o < K) {
+      const int f = c / npar, p = c % npar;
+      const double dz = regs[par_regions[p]].dz;
+      const double2 kz = KZ[((size_t)par_eps[p] * nf + f) * K + o];
+      v = cexp_as<float2>(kz.y * dz, -kz.x * dz);
+    }
+    put_bt(Bhi, Blo, Kp, c, o, v.x, v.y);
   }
 }
 
@@ -235,6 +343,40 @@ __global__ void k_build_e(C* E, const int* supp, int Kd, int nf, const RegionT* 
       }
       E[(size_t)s * ncol + c] = v;
     }
+  }
+}
+
+// B''^T of the pixel class: row c = f * npx + q, column s (support pixel)
+__global__ void k_build_e_t(float* Bhi, float* Blo, const int* supp, int Kd, int Kdp, int nf, const RegionT* regs,
+                            const int* pix_regions, int npx, const double2* K0, const double* X, const double* Y,
+                            int nx, const double2* surf, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= Kdp) return;
+  const int ncol = nf * npx;
+  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+    float2 v = make_float2(0.f, 0.f);
+    if (s < Kd) {
+      const int reg = pix_regions[c % npx];
+      const RegionT g = regs[reg];
+      const double2 k0 = K0[c];
+      double re, im;
+      if (g.klass == 2) {
+        re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
+        im = -k0.x * g.dz;
+      } else {
+        const int x = supp[s] % nx, y = supp[s] / nx;
+        const double t = g.tx * X[x] + g.ty * Y[y];
+        re = k0.y * t;
+        im = -k0.x * t;
+        if (surf) {
+          const double2 sv = surf[(size_t)reg * npix + supp[s]];
+          re += k0.x * sv.y + k0.y * sv.x;
+          im -= k0.x * sv.x - k0.y * sv.y;
+        }
+      }
+      v = cexp_as<float2>(re, im);
+    }
+    put_bt(Bhi, Blo, Kdp, c, s, v.x, v.y);
   }
 }
 
@@ -814,9 +956,12 @@ unsigned blocks_for(size_t n) { return (unsigned)std::max<size_t>(1, (n + 255) /
 // and support tables.
 struct TfCache {
   unsigned long long modes_id = 0, geo_version = ~0ull;
-  int fp64 = -1;
+  int mode = -1;   // operands built for: 0 FP64, 1 complex64 (SIMT GEMM), 2 TF32 pairs (tensor cores)
   int K = 0, msz = 0, Kd = 0, nm = 0;
   DBuf W, V, rep, supp, U, Phi, members;
+  // BF_PREC_TF32: A'' of both classes as TF32 hi/lo pairs (K padded to Kp, Kdp)
+  DBuf Wt_hi, Wt_lo, Vt_hi, Vt_lo;
+  int Kp = 0, Kdp = 0;
   std::vector<int2> rep_h;
 };
 
@@ -824,11 +969,14 @@ static void tf_cache_delete(void* p) { delete static_cast<TfCache*>(p); }
 static size_t tf_cache_bytes(const void* p) {
   const TfCache* c = static_cast<const TfCache*>(p);
   size_t b = 0;
-  for (const DBuf* d : {&c->W, &c->V, &c->rep, &c->supp, &c->U, &c->Phi, &c->members}) b += d->p ? d->n : 0;
+  for (const DBuf* d : {&c->W, &c->V, &c->rep, &c->supp, &c->U, &c->Phi, &c->members, &c->Wt_hi, &c->Wt_lo,
+                        &c->Vt_hi, &c->Vt_lo})
+    b += d->p ? d->n : 0;
   return b;
 }
 
-static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache** out) {
+static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache** out) {
+  const bool fp64 = mode == 0;
   if (!s->tf_cache) {
     s->tf_cache = new TfCache();
     s->tf_cache_delete = tf_cache_delete;
@@ -839,7 +987,8 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   // W and V depend on the modes, the grid and the disk mask only, none of
   // which a stack changes after creation (bf_stack_set_distance moves the
   // disks), so gap updates of an optimiser reuse them.
-  if (c.modes_id == md->id && c.fp64 == (int)fp64) return BF_OK;
+  if (c.modes_id == md->id && c.mode == mode) return BF_OK;
+  for (DBuf* d : {&c.W, &c.V, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -902,12 +1051,29 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 0, 0, st);
   if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 1, 0, st);
   if (e) return bf_fail(h, BF_ERR_CUDA, "mode FFTs failed");
-  TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+  c.Kp = (c.K + 15) / 16 * 16;
   {
     dim3 grid(blocks_for(c.K), nm * nm);
     const double scale = 1.0 / ((double)nx * (double)ny);
-    if (fp64) { bf::note_launch(); k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
-    else { bf::note_launch(); k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(), c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale); }
+    bf::note_launch();
+    if (fp64) {
+      TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+      k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(),
+                                               c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
+    } else if (mode == 1) {
+      TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+      k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(),
+                                              c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
+    } else {
+      const size_t n = (size_t)2 * nm * nm * 2 * c.Kp;
+      TCKS(c.Wt_hi.alloc(h, sizeof(float) * n));
+      TCKS(c.Wt_lo.alloc(h, sizeof(float) * n));
+      TCK(cudaMemsetAsync(c.Wt_hi.p, 0, sizeof(float) * n, st));
+      TCK(cudaMemsetAsync(c.Wt_lo.p, 0, sizeof(float) * n, st));
+      k_build_w_t<<<grid, 256, 0, st>>>(c.Wt_hi.as<float>(), c.Wt_lo.as<float>(), c.U.as<double2>(),
+                                        c.Phi.as<double2>(), c.members.as<int>(), c.K, c.Kp, c.msz, nm, (int)npix,
+                                        scale);
+    }
     TCK(cudaGetLastError());
   }
   // support pixels (any mode non-zero) and V
@@ -921,11 +1087,26 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   c.Kd = (int)supp.size();
   TCKS(c.supp.alloc(h, sizeof(int) * supp.size()));
   TCK(cudaMemcpyAsync(c.supp.p, supp.data(), sizeof(int) * supp.size(), cudaMemcpyHostToDevice, st));
-  TCKS(c.V.alloc(h, csz * (size_t)nm * nm * c.Kd));
+  c.Kdp = (c.Kd + 15) / 16 * 16;
   {
     dim3 grid(blocks_for(c.Kd), nm * nm);
-    if (fp64) { bf::note_launch(); k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
-    else { bf::note_launch(); k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix); }
+    bf::note_launch();
+    if (fp64) {
+      TCKS(c.V.alloc(h, csz * (size_t)nm * nm * c.Kd));
+      k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm,
+                                               (int)npix);
+    } else if (mode == 1) {
+      TCKS(c.V.alloc(h, csz * (size_t)nm * nm * c.Kd));
+      k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix);
+    } else {
+      const size_t n = (size_t)2 * nm * nm * 2 * c.Kdp;
+      TCKS(c.Vt_hi.alloc(h, sizeof(float) * n));
+      TCKS(c.Vt_lo.alloc(h, sizeof(float) * n));
+      TCK(cudaMemsetAsync(c.Vt_hi.p, 0, sizeof(float) * n, st));
+      TCK(cudaMemsetAsync(c.Vt_lo.p, 0, sizeof(float) * n, st));
+      k_build_v_t<<<grid, 256, 0, st>>>(c.Vt_hi.as<float>(), c.Vt_lo.as<float>(), md->d_pat, c.supp.as<int>(), c.Kd,
+                                        c.Kdp, nm, (int)npix);
+    }
     TCK(cudaGetLastError());
   }
   TCK(cudaStreamSynchronize(st));
@@ -933,7 +1114,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, bool fp64, TfCache*
   c.Phi.release();
   c.modes_id = md->id;
   c.geo_version = s->geo_version;
-  c.fp64 = fp64;
+  c.mode = mode;
   return BF_OK;
 }
 
@@ -977,13 +1158,36 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
   return BF_OK;
 }
 
+// Class GEMM of the TF32 path on the tensor cores: G[R][N] (complex128) from
+// A'' [2R][2Kp] and B''^T [N][2Kp] (TF32 hi/lo).  K is cut into slices of at
+// most 2048 real terms (FP32 accumulation in tensor memory per slice) and into
+// enough slices to fill the SMs; the slices are summed in FP64.
+static int tc_class_gemm(bf_handle* h, const float* Ahi, const float* Alo, int R, int Kp, const float* Bhi,
+                         const float* Blo, int N, double2* G, int* d_err) {
+  cudaStream_t st = h->stream();
+  const int M2 = 2 * R, K2 = 2 * Kp;
+  g_tf_gemm_flops += 8.0 * (double)R * (double)Kp * (double)N;
+  const long tiles = (long)((N + 127) / 128) * ((M2 + 127) / 128);
+  const int ktiles = K2 / 32;
+  int splits = std::max((K2 + 2047) / 2048, (int)((2 * 152 + tiles - 1) / tiles));
+  splits = std::max(1, std::min({splits, ktiles, 64}));
+  DBuf planes;
+  TCKS(planes.alloc(h, sizeof(float) * (size_t)splits * M2 * N));
+  const int e = bf::tc_gemm_tf32x3(Ahi, Alo, Bhi, Blo, M2, N, K2, splits, planes.as<float>(), d_err, st);
+  if (e) return bf_fail(h, BF_ERR_CUDA, std::string("tensor-core GEMM: ") + cudaGetErrorString((cudaError_t)e));
+  bf::note_launch();
+  k_planes_to_g<<<blocks_for((size_t)R * N), 256, 0, st>>>(G, planes.as<float>(), R, N, splits);
+  TCK(cudaGetLastError());
+  return BF_OK;
+}
+
 // Propagation matrices of regions [j0, nd) for all frequencies into
 // P[f][j][m][m'] stored as S, which is also the operand storage of the class
 // GEMMs: double2 (FP64 path) or float2 (mixed path).
 template <typename S>
 static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
                                    const std::vector<RegionT>& regs, int j0, int nf,
-                                   const std::vector<double>& freqs, int prop_kind, DBuf& P) {
+                                   const std::vector<double>& freqs, int prop_kind, DBuf& P, int mode) {
   using C = double2;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm, nx = s->nx, ny = s->ny;
@@ -994,6 +1198,8 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     else if (regs[j].klass == 3) freg.push_back(j);
     else preg.push_back(j);
   }
+  int* tc_err = reinterpret_cast<int*>(h->d_scalar + 2);   // set by the tensor-core GEMM on a wait timeout
+  if (mode == 2) TCK(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
   TCKS(P.ensure(h, sizeof(S) * (size_t)nf * nd * nm * nm));
   DBuf d_regs, d_freq, d_kt, d_list;
   TCKS(d_regs.alloc(h, sizeof(RegionT) * regs.size()));
@@ -1027,17 +1233,31 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(d_peps.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(d_peps.p, par_eps.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
     TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
-    TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
     bf::note_launch();
-    k_build_kz<<<dim3(blocks_for(nf), std::min(c.K, 65535), neps), 256, 0, st>>>(
+    k_build_kz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
         KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
     TCK(cudaGetLastError());
-    bf::note_launch();
-    k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
-        D.as<S>(), KZ.as<double2>(), c.K, nf, dr, lst.as<int>(), d_peps.as<int>(), npar);
-    TCK(cudaGetLastError());
-    TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
+    if (mode != 2) {
+      TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
+      bf::note_launch();
+      k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
+          D.as<S>(), KZ.as<double2>(), c.K, nf, dr, lst.as<int>(), d_peps.as<int>(), npar);
+      TCK(cudaGetLastError());
+      TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
+    } else {
+      DBuf Bh, Bl;
+      const size_t nb = (size_t)ncol * 2 * c.Kp;
+      TCKS(Bh.alloc(h, sizeof(float) * nb));
+      TCKS(Bl.alloc(h, sizeof(float) * nb));
+      bf::note_launch();
+      k_build_d_t<<<dim3(blocks_for(c.Kp), std::min(ncol, 65535)), 256, 0, st>>>(
+          Bh.as<float>(), Bl.as<float>(), KZ.as<double2>(), c.K, c.Kp, nf, dr, lst.as<int>(), d_peps.as<int>(),
+          npar);
+      TCK(cudaGetLastError());
+      TCKS(tc_class_gemm(h, c.Wt_hi.as<float>(), c.Wt_lo.as<float>(), nm * nm, c.Kp, Bh.as<float>(),
+                         Bl.as<float>(), ncol, G.as<C>(), tc_err));
+    }
     dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
     k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
@@ -1050,7 +1270,6 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(lst.alloc(h, sizeof(int) * npx));
     TCK(cudaMemcpyAsync(lst.p, preg.data(), sizeof(int) * npx, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npx;
-    TCKS(E.alloc(h, sizeof(S) * (size_t)c.Kd * ncol));
     TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
     DBuf K0, DG;
     TCKS(K0.alloc(h, sizeof(double2) * (size_t)ncol));
@@ -1062,12 +1281,27 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     k_build_diag<<<blocks_for((size_t)ncol * nm), 256, 0, st>>>(DG.as<double2>(), K0.as<double2>(), nf, npx, dr,
                                                                lst.as<int>(), d_kt.as<double2>(), nm);
     TCK(cudaGetLastError());
-    bf::note_launch();
-    k_build_e<S><<<dim3(blocks_for(ncol), std::min(c.Kd, 65535)), 256, 0, st>>>(
-        E.as<S>(), c.supp.as<int>(), c.Kd, nf, dr, lst.as<int>(), npx, K0.as<double2>(), s->dX, s->dY, nx,
-        s->d_surf, (int)npix);
-    TCK(cudaGetLastError());
-    TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
+    if (mode != 2) {
+      TCKS(E.alloc(h, sizeof(S) * (size_t)c.Kd * ncol));
+      bf::note_launch();
+      k_build_e<S><<<dim3(blocks_for(ncol), std::min(c.Kd, 65535)), 256, 0, st>>>(
+          E.as<S>(), c.supp.as<int>(), c.Kd, nf, dr, lst.as<int>(), npx, K0.as<double2>(), s->dX, s->dY, nx,
+          s->d_surf, (int)npix);
+      TCK(cudaGetLastError());
+      TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
+    } else {
+      DBuf Bh, Bl;
+      const size_t nb = (size_t)ncol * 2 * c.Kdp;
+      TCKS(Bh.alloc(h, sizeof(float) * nb));
+      TCKS(Bl.alloc(h, sizeof(float) * nb));
+      bf::note_launch();
+      k_build_e_t<<<dim3(blocks_for(c.Kdp), std::min(ncol, 65535)), 256, 0, st>>>(
+          Bh.as<float>(), Bl.as<float>(), c.supp.as<int>(), c.Kd, c.Kdp, nf, dr, lst.as<int>(), npx,
+          K0.as<double2>(), s->dX, s->dY, nx, s->d_surf, (int)npix);
+      TCK(cudaGetLastError());
+      TCKS(tc_class_gemm(h, c.Vt_hi.as<float>(), c.Vt_lo.as<float>(), nm * nm, c.Kdp, Bh.as<float>(),
+                         Bl.as<float>(), ncol, G.as<C>(), tc_err));
+    }
     dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
     k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, DG.as<double2>());
@@ -1258,6 +1492,14 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
 // One transformer solve (or, with only_matrices, the propagation matrices).
 // fp64 selects FP64 class-GEMM operands; otherwise double-float operands on
 // the FP32 pipes.  Propagation matrices, inverses, chain and solve are FP64.
+// After a BF_PREC_TF32 solve has synchronised: the tensor-core GEMM's error flag.
+static int tc_status(bf_handle* h) {
+  int e = 0;
+  TCK(cudaMemcpy(&e, reinterpret_cast<int*>(h->d_scalar + 2), sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) return bf_fail(h, BF_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait expired (stage " + std::to_string(e) + ")");
+  return BF_OK;
+}
+
 // Inputs and output of transformer_trace_back (a solve that stops after the
 // inverses and walks the regions instead of running the chain).
 struct TraceArgs {
@@ -1274,7 +1516,7 @@ template <typename PT>
 static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                     const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                     double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
-                    double* out_pm, const TraceArgs* tb = nullptr) {
+                    double* out_pm, int mode, const TraceArgs* tb = nullptr) {
   constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
@@ -1314,9 +1556,9 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     }
   } else {
     TfCache* c = nullptr;
-    TCKS(tf_setup(h, s, md, fp64, &c));
+    TCKS(tf_setup(h, s, md, mode, &c));
     const int j0 = only_matrices ? 0 : 1;
-    TCKS(tf_propagation_matrices<PT>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P));
+    TCKS(tf_propagation_matrices<PT>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P, mode));
   }
   if (only_matrices) {
     // out_pm: [nf][nd] Julia (nm, nm) column-major matrices
@@ -1330,6 +1572,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     }
     TCK(cudaMemcpyAsync(hp.data(), src, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
+    if (mode == 2) TCKS(tc_status(h));
     cd* o = reinterpret_cast<cd*>(out_pm);
     for (int f = 0; f < nf; ++f)
       for (int j = 0; j < nd; ++j)
@@ -1401,6 +1644,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaGetLastError());
     TCK(cudaMemcpyAsync(tb->out, d_out.p, sizeof(cd) * nout, cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
+    if (mode == 2 && !pm) TCKS(tc_status(h));
     return BF_OK;
   }
   // T21 / T22 for the boundary solve, FP64
@@ -1463,18 +1707,20 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   if (out_refl && reflect) TCK(cudaMemcpyAsync(out_refl, refl.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
   if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
+  if (mode == 2 && !pm) TCKS(tc_status(h));
   return BF_OK;
 }
 
-static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind, bool fp64,
-                  const double* emit, const double* reflect, const double* pm, int pm_per_freq, double* out_boost,
-                  double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices, double* out_pm,
-                  const TraceArgs* tb = nullptr) {
-  if (fp64)
+// precision: BF_PREC_FP64 (mode 0), BF_PREC_MIXED (mode 1) or BF_PREC_TF32 (mode 2)
+static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
+                  int precision, const double* emit, const double* reflect, const double* pm, int pm_per_freq,
+                  double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
+                  double* out_pm, const TraceArgs* tb = nullptr) {
+  if (precision == BF_PREC_FP64)
     return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                             out_beta2, mirror_1e30, only_matrices, out_pm, tb);
+                             out_beta2, mirror_1e30, only_matrices, out_pm, 0, tb);
   return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                          out_beta2, mirror_1e30, only_matrices, out_pm, tb);
+                          out_beta2, mirror_1e30, only_matrices, out_pm, precision == BF_PREC_TF32 ? 2 : 1, tb);
 }
 
 static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
@@ -1486,7 +1732,10 @@ static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   for (int i = 0; i < nf; ++i)
     if (!(freqs[i] > 0) || !std::isfinite(freqs[i])) return bf_fail(h, BF_ERR_INVALID, "bad frequency");
   if (prop_kind < 0 || prop_kind > 3) return bf_fail(h, BF_ERR_INVALID, "unknown propagator kind");
-  if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED) return bf_fail(h, BF_ERR_INVALID, "unknown precision");
+  if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED && precision != BF_PREC_TF32)
+    return bf_fail(h, BF_ERR_INVALID, "unknown precision");
+  if (precision == BF_PREC_TF32 && !bf::tc_gemm_available())
+    return bf_fail(h, BF_ERR_UNSUPPORTED, "BF_PREC_TF32: the tensor-map encoder of the driver is unavailable");
   return BF_OK;
 }
 
@@ -1496,7 +1745,7 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
                               double* out_refl, double* out_beta2) {
   TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
   TCK(cudaSetDevice(h->device));
-  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, emit, reflect, propagation_matrices,
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision, emit, reflect, propagation_matrices,
                 pm_per_freq, out_boost, out_refl, out_beta2, 1, 0, nullptr);
 }
 
@@ -1510,7 +1759,7 @@ extern "C" int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* md
   TCK(cudaSetDevice(h->device));
   TraceArgs tb{reflected_beam, input_beam, beams_per_freq ? 1 : 0, includes_axion ? 1 : 0, out};
   // the reference's trace-back does not replace a NaN mirror permittivity (no mutation here either)
-  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, emit, nullptr, propagation_matrices,
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision, emit, nullptr, propagation_matrices,
                 pm_per_freq, nullptr, nullptr, nullptr, 0, 0, nullptr, &tb);
 }
 
@@ -1519,6 +1768,6 @@ extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes*
   TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
   if (!out) return bf_fail(h, BF_ERR_INVALID, "null output");
   TCK(cudaSetDevice(h->device));
-  return tf_run(h, s, md, nf, freqs, prop_kind, precision == BF_PREC_FP64, nullptr, nullptr, nullptr, 0, nullptr,
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision, nullptr, nullptr, nullptr, 0, nullptr,
                 nullptr, nullptr, 0, 1, out);
 }

@@ -49,6 +49,12 @@ extern "C" {
 #define BF_PREC_FP64  0  /* complex128 fields, FP64 transforms (the plain FP64 path) */
 #define BF_PREC_MIXED 1  /* complex64 fields and transforms; FP64 phase argument kz*dz,
                             FP64 exit (bounce-sum) accumulation, FP64 final solve */
+#define BF_PREC_TF32  2  /* transformer only, no reference counterpart: the mixed path
+                            with the overlap GEMMs on the tensor cores (split TF32,
+                            FP32 accumulation per K slice).  The tensor cores' FP32
+                            accumulation truncates, so beta^2 is only within ~1e-2 of
+                            FP64 (outside the 1e-4 bar of BF_PREC_MIXED); for coarse
+                            scans */
 
 /* ---- flags -------------------------------------------------------------- */
 #define BF_OUT_DEVICE 1  /* output pointers are device pointers (results stay in HBM) */

@@ -224,6 +224,64 @@ def test_transformer_full_size_lg_vs_oracle_fixture(B):
         assert abs(np.sum(np.abs(b32[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
 
 
+def _lg_reduced(B):
+    from bfgb300 import workloads as W
+    distance, eps, tx, ty, _, _ = _stack(4, 64, seed=41)
+    X = W.symmetric_grid(64, width=0.4)
+    rng = np.random.default_rng(42)
+    nd = len(distance)
+    s = np.zeros((nd, 64, 64))
+    s[2:nd - 1:2] = W.surface_roughness(X, X, 4, rng)
+    pats, kt = W.lg_modes(X, X, 16, 0.03, 0.15)
+    kw = dict(diskno=4, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb = B.SeedCoordinateSystem(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=16, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    return cb, mb, kw
+
+
+def test_tf32_propagation_matrices_vs_fp64(B):
+    """BF_PREC_TF32: the overlap GEMMs on the tensor cores (split TF32).  Every
+    propagation matrix within 1e-4 (relative, Frobenius) of the FP64 path; a
+    layout or descriptor error would show as O(1)."""
+    cb, mb, kw = _lg_reduced(B)
+    freqs = np.array([19.3e9, 20.6e9])
+    p64 = B.calc_propagation_matrices(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs)
+    p32 = B.calc_propagation_matrices(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="tf32")
+    for f in range(len(freqs)):
+        for j in range(1, len(kw["distance"])):
+            assert rel(p32[f][j], p64[f][j]) < 1e-4, (f, j)
+
+
+def test_tf32_transformer_full_size_vs_oracle_fixture(B):
+    """BF_PREC_TF32 on the full transformer workload: beta^2 within the stated
+    2e-2 of the oracle (the tensor cores' truncating FP32 accumulation keeps it
+    outside the 1e-4 bar of the mixed path)."""
+    import os
+    from bfgb300 import workloads as W
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "c3_lg_oracle.npz"))
+    w = W.config3_transformer()
+    c = B.SeedCoordinateSystem(X=w["X"], Y=w["Y"])
+    kw = dict(diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"], epsilon=w["eps"],
+              relative_tilt_x=w["relative_tilt_x"], relative_tilt_y=w["relative_tilt_y"],
+              relative_surfaces=w["relative_surfaces"])
+    m = B.SeedModes(c, ThreeDim=True, Mmax=w["M"], Lmax=w["L"], diskR=w["diskR"],
+                    pattern_input=w["pattern_input"], kT_arr=w["kT_arr"])
+    b = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"], precision="tf32")
+    for k in range(len(fx["freqs"])):
+        assert abs(np.sum(np.abs(b[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < 2e-2
+
+
+def test_tf32_rejected_by_bounce_solvers(B):
+    from bfgb300 import _lib
+    cb, _, kw = _lg_reduced(B)
+    st = B.Stack(B.SeedSetupBoundaries(cb, **kw), cb, 0.15)
+    with pytest.raises(B.BFError) as e:
+        st.cheerleader(np.array([20e9]), nmax=5, precision="tf32")
+    assert e.value.code == _lib.BF_ERR_INVALID
+    st.close()
+
+
 def test_transformer_1d_vs_analytical1d(B):
     d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
     c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
