@@ -30,6 +30,7 @@ __all__ = [
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
+    "gauss_profile", "unnormalized_match", "transformer_coupled",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -597,6 +598,70 @@ def transformer_trace_back(reflected_beam, input_beam, bdry, coords, modes, inlc
         st.close()
     out = out.transpose(0, 3, 2, 1)
     return out[0] if np.ndim(f) == 0 else out
+
+
+def gauss_profile(coords, z=0.000000001, omega0=0.1, f=10e9):
+    """src/beam_gaussian.jl:24-37: normalised 2D Gaussian beam (nx, ny) at distance
+    z from its waist (FP64, host)."""
+    X = np.ascontiguousarray(coords.X, dtype=np.float64)
+    Y = np.ascontiguousarray(coords.Y, dtype=np.float64)
+    out = np.empty((len(Y), len(X)), dtype=np.complex128)
+    rc = _lib.lib().bf_gauss_profile(len(X), len(Y), _lib.ptr(X), _lib.ptr(Y), float(z), float(omega0), float(f),
+                                     _lib.ptr(out.view(np.float64)))
+    if rc != _lib.BF_OK:
+        raise BFError(rc, "gauss_profile: bad arguments")
+    return out.T.copy()
+
+
+def unnormalized_match(Eout, Eantenna, dx=0.01, dy=0.01, handle=None):
+    """src/beam_coupling.jl:13-15 on the GPU: sum(Eout .* conj(Eantenna)) dx dy.
+    Eout may carry a leading batch axis (nb, nx, ny); one value per field."""
+    h = handle or default_handle()
+    A = np.asfortranarray(np.asarray(Eantenna, dtype=np.complex128))
+    E = np.asarray(Eout, dtype=np.complex128)
+    batched = E.ndim == A.ndim + 1
+    Eb = E if batched else E[None]
+    nb, npix = Eb.shape[0], A.size
+    ebuf = np.ascontiguousarray(np.stack([np.asfortranarray(e).T for e in Eb])).view(np.float64).reshape(-1)
+    abuf = np.ascontiguousarray(A.T).view(np.float64).reshape(-1)
+    out = np.empty(nb, dtype=np.complex128)
+    h.check(_lib.lib().bf_unnormalized_match(h.ptr, nb, npix, _lib.ptr(ebuf), _lib.ptr(abuf), float(dx), float(dy),
+                                             0, _lib.ptr(out.view(np.float64))))
+    return out if batched else out[0]
+
+
+def transformer_coupled(bdry, coords, modes, antenna, f=10.0e9, prop=propagator, propagation_matrices=None,
+                        diskR=0.15, emit=None, precision="fp64"):
+    """The transformer with the antenna coupling fused into its output: per
+    frequency |sum_m conj(boost_m) antenna_m|^2, antenna = the antenna's mode
+    coefficients (the coupled power of examples/transformer_optim_utilities.jl:137).
+    Returns (coupled, beta2), arrays over f (scalars for a scalar f)."""
+    freqs = np.ascontiguousarray(np.atleast_1d(f), dtype=np.float64)
+    nf, nm = len(freqs), modes.nm
+    bdry.eps[np.isnan(bdry.eps)] = 1e30
+    ant = np.ascontiguousarray(antenna, dtype=np.complex128).reshape(nm)
+    st = Stack(bdry, coords, diskR, handle=modes.h)
+    try:
+        ebuf = pbuf = None
+        if emit is not None:
+            ebuf = np.ascontiguousarray(emit, dtype=np.complex128).reshape(nm).view(np.float64)
+        per_freq = 0
+        if propagation_matrices is not None and len(propagation_matrices):
+            pmat = np.asarray(propagation_matrices, dtype=np.complex128)
+            if pmat.ndim == 3:
+                pmat = pmat[None]
+            per_freq = int(pmat.shape[0] == nf and nf > 1)
+            pbuf = np.ascontiguousarray(pmat.transpose(0, 1, 3, 2)).view(np.float64)
+        cpl = np.empty(nf)
+        b2 = np.empty(nf)
+        st.h.check(_lib.lib().bf_transformer_coupled(
+            st.h.ptr, st._s, modes._m, nf, _lib.ptr(freqs), _prop_kind(prop), _prec(precision), _lib.ptr(ebuf),
+            _lib.ptr(ant.view(np.float64)), _lib.ptr(pbuf), per_freq, _lib.ptr(cpl), _lib.ptr(b2)))
+    finally:
+        st.close()
+    if np.ndim(f) == 0:
+        return float(cpl[0]), float(b2[0])
+    return cpl, b2
 
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,

@@ -28,6 +28,7 @@ BF_PREC_MIXED = 1
 BF_PREC_TF32 = 2
 
 BF_OUT_DEVICE = 1
+BF_IN_DEVICE = 2
 
 _c_int = ctypes.c_int
 _c_dbl = ctypes.c_double
@@ -66,6 +67,10 @@ _SIGS = {
                               _p_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
     "bf_propagate_noalloc": (_c_int, [_vp, _c_int, _vp, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl,
                                       _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl, _c_dbl]),
+    "bf_gauss_profile": (_c_int, [_c_int, _c_int, _p_dbl, _p_dbl, _c_dbl, _c_dbl, _c_dbl, _p_dbl]),
+    "bf_unnormalized_match": (_c_int, [_vp, _c_int, _c_int, _vp, _p_dbl, _c_dbl, _c_dbl, _c_int, _p_dbl]),
+    "bf_transformer_coupled": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl,
+                                        _c_int, _p_dbl, _p_dbl]),
     "bf_transformer_trace_back": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _c_int,
                                            _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl]),
     "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),

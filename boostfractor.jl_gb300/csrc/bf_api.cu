@@ -280,6 +280,30 @@ extern "C" int bf_get_kspace_coords(int n, const double* real_coords, double* ou
   return BF_OK;
 }
 
+// gauss_profile (src/beam_gaussian.jl:24-37), FP64 in the reference's order:
+// r = sqrt(x^2 + y^2); amplitude omega0/omega(z) exp(-r^2/omega(z)^2);
+// phase exp(-i (k z + k r^2 / (2 R(z)) - Psi(z))).
+extern "C" int bf_gauss_profile(int nx, int ny, const double* X, const double* Y, double z, double omega0,
+                                double f, double* out) {
+  if (nx < 1 || ny < 1 || !X || !Y || !out || !(omega0 > 0.0) || !(f > 0.0)) return BF_ERR_INVALID;
+  const double lambda = 299792458.0 / f;
+  const double k = 2.0 * M_PI / lambda;
+  const double zR = M_PI * omega0 * omega0 / lambda;
+  const double omega = omega0 * std::sqrt(1.0 + (z / zR) * (z / zR));
+  const double Rz = z * (1.0 + (zR / z) * (zR / z));
+  const double psi = std::atan(z / zR);
+  cd* o = reinterpret_cast<cd*>(out);
+  for (int y = 0; y < ny; ++y)
+    for (int x = 0; x < nx; ++x) {
+      const double r = std::sqrt(X[x] * X[x] + Y[y] * Y[y]);
+      const double r2 = r * r;
+      const double amp = omega0 / omega * std::exp(-r2 / (omega * omega));
+      const double ph = (k * z + k * r2 / (2.0 * Rz)) - psi;
+      o[(size_t)y * nx + x] = amp * std::exp(cd(0.0, -ph));
+    }
+  return BF_OK;
+}
+
 extern "C" int bf_fresnel_reflectivities(int nd, const double* eps, double* r_out) {
   if (nd < 2 || !eps || !r_out) return BF_ERR_INVALID;
   cd* r = reinterpret_cast<cd*>(r_out);
@@ -585,6 +609,54 @@ extern "C" int bf_propagate(bf_handle* h, int prop_kind, int precision, double* 
   CK(cudaMemcpyAsync(E, bE64.p, 16 * npix, cudaMemcpyDeviceToHost, h->stream()));
   CK(cudaStreamSynchronize(h->stream()));
   s.dX = s.dY = s.dkX = s.dkY = nullptr; s.d_mask_full = nullptr; s.d_surf = nullptr;
+  return BF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// unnormalized_match (src/beam_coupling.jl:13-15), batched over fields
+// ---------------------------------------------------------------------------
+// out[b] = dx dy sum_p E[b][p] conj(A[p]); one CTA per field, FP64, fixed
+// reduction order (a per-thread stride sum, then a tree).
+__global__ void k_match(double2* out, const double2* E, const double2* A, size_t npix, double dxdy) {
+  __shared__ double2 red[256];
+  const double2* e = E + (size_t)blockIdx.x * npix;
+  double2 acc = make_double2(0.0, 0.0);
+  for (size_t p = threadIdx.x; p < npix; p += blockDim.x) {
+    const double2 u = e[p], v = A[p];
+    acc.x += u.x * v.x + u.y * v.y;
+    acc.y += u.y * v.x - u.x * v.y;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x].x += red[threadIdx.x + s].x;
+      red[threadIdx.x].y += red[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = make_double2(red[0].x * dxdy, red[0].y * dxdy);
+}
+
+extern "C" int bf_unnormalized_match(bf_handle* h, int nb, int npix, const double* E, const double* Eantenna,
+                                     double dx, double dy, int flags, double* out) {
+  if (!h) return BF_ERR_INVALID;
+  if (nb < 1 || npix < 1 || !E || !Eantenna || !out) return fail(h, BF_ERR_INVALID, "empty or null match input");
+  CK(cudaSetDevice(h->device));
+  cudaStream_t st = h->stream();
+  DBuf dE, dA, dO;
+  const double2* pe = reinterpret_cast<const double2*>(E);
+  if (!(flags & BF_IN_DEVICE)) {
+    CKS(upload(h, dE, E, sizeof(double2) * (size_t)nb * npix));
+    pe = dE.as<double2>();
+  }
+  CKS(upload(h, dA, Eantenna, sizeof(double2) * (size_t)npix));
+  CKS(dO.alloc(h, sizeof(double2) * nb));
+  bf::note_launch();
+  k_match<<<nb, 256, 0, st>>>(dO.as<double2>(), pe, dA.as<double2>(), (size_t)npix, dx * dy);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, dO.p, sizeof(double2) * nb, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
   return BF_OK;
 }
 

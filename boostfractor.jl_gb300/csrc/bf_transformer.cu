@@ -1500,6 +1500,26 @@ static int tc_status(bf_handle* h) {
   return BF_OK;
 }
 
+// Antenna coupling fused after the boundary solve: out[f] = |sum_m
+// conj(boost[f][m]) antenna[m]|^2, the coupled power of the optimiser cost
+// (examples/transformer_optim_utilities.jl:137).
+__global__ void k_coupled(double* out, const double2* boost, const double2* ant, int nm, int nf) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= nf) return;
+  double re = 0.0, im = 0.0;
+  for (int m = 0; m < nm; ++m) {
+    const double2 b = boost[(size_t)f * nm + m], a = ant[m];
+    re += b.x * a.x + b.y * a.y;
+    im += b.x * a.y - b.y * a.x;
+  }
+  out[f] = re * re + im * im;
+}
+
+struct CoupleArgs {
+  const double* antenna;   // nm complex (the antenna's mode coefficients)
+  double* out;             // nf coupled powers
+};
+
 // Inputs and output of transformer_trace_back (a solve that stops after the
 // inverses and walks the regions instead of running the chain).
 struct TraceArgs {
@@ -1516,7 +1536,7 @@ template <typename PT>
 static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                     const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                     double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
-                    double* out_pm, int mode, const TraceArgs* tb = nullptr) {
+                    double* out_pm, int mode, const TraceArgs* tb = nullptr, const CoupleArgs* cp = nullptr) {
   constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
@@ -1686,6 +1706,15 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
                                              reflect ? refl.as<double2>() : nullptr, b2.as<double>());
     TCK(cudaGetLastError());
   }
+  DBuf d_ant, d_cpl;
+  if (cp) {
+    TCKS(d_ant.alloc(h, sizeof(cd) * nm));
+    TCK(cudaMemcpyAsync(d_ant.p, cp->antenna, sizeof(cd) * nm, cudaMemcpyHostToDevice, st));
+    TCKS(d_cpl.alloc(h, sizeof(double) * nf));
+    bf::note_launch();
+    k_coupled<<<blocks_for(nf), 256, 0, st>>>(d_cpl.as<double>(), boost.as<double2>(), d_ant.as<double2>(), nm, nf);
+    TCK(cudaGetLastError());
+  }
   tf_mark(h, 2);
   if (h->profiling) {
     TCK(cudaEventSynchronize(h->ev[2]));
@@ -1706,6 +1735,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   if (out_boost) TCK(cudaMemcpyAsync(out_boost, boost.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
   if (out_refl && reflect) TCK(cudaMemcpyAsync(out_refl, refl.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
   if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+  if (cp) TCK(cudaMemcpyAsync(cp->out, d_cpl.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
   if (mode == 2 && !pm) TCKS(tc_status(h));
   return BF_OK;
@@ -1715,12 +1745,12 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
 static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                   int precision, const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                   double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
-                  double* out_pm, const TraceArgs* tb = nullptr) {
+                  double* out_pm, const TraceArgs* tb = nullptr, const CoupleArgs* cp = nullptr) {
   if (precision == BF_PREC_FP64)
     return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                             out_beta2, mirror_1e30, only_matrices, out_pm, 0, tb);
+                             out_beta2, mirror_1e30, only_matrices, out_pm, 0, tb, cp);
   return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                          out_beta2, mirror_1e30, only_matrices, out_pm, precision == BF_PREC_TF32 ? 2 : 1, tb);
+                          out_beta2, mirror_1e30, only_matrices, out_pm, precision == BF_PREC_TF32 ? 2 : 1, tb, cp);
 }
 
 static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
@@ -1747,6 +1777,18 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
   TCK(cudaSetDevice(h->device));
   return tf_run(h, s, md, nf, freqs, prop_kind, precision, emit, reflect, propagation_matrices,
                 pm_per_freq, out_boost, out_refl, out_beta2, 1, 0, nullptr);
+}
+
+extern "C" int bf_transformer_coupled(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,
+                                      int prop_kind, int precision, const double* emit, const double* antenna,
+                                      const double* propagation_matrices, int pm_per_freq, double* out_coupled,
+                                      double* out_beta2) {
+  TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
+  if (!antenna || !out_coupled) return bf_fail(h, BF_ERR_INVALID, "null antenna or output");
+  TCK(cudaSetDevice(h->device));
+  CoupleArgs cp{antenna, out_coupled};
+  return tf_run(h, s, md, nf, freqs, prop_kind, precision, emit, nullptr, propagation_matrices, pm_per_freq,
+                nullptr, nullptr, out_beta2, 1, 0, nullptr, nullptr, &cp);
 }
 
 extern "C" int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,

@@ -58,6 +58,7 @@ extern "C" {
 
 /* ---- flags -------------------------------------------------------------- */
 #define BF_OUT_DEVICE 1  /* output pointers are device pointers (results stay in HBM) */
+#define BF_IN_DEVICE  2  /* field inputs are device pointers (e.g. BF_OUT_DEVICE results) */
 
 typedef struct bf_handle bf_handle;
 typedef struct bf_stack bf_stack;
@@ -100,6 +101,20 @@ int bf_get_kspace_coords(int n, const double* real_coords, double* kspace_out);
  * (0-based), real eps taken as re - 0.0im.  eps: nd complex, r_out: nd-1 complex.
  * Replaces src/boost_fractor.jl:98-103. */
 int bf_fresnel_reflectivities(int nd, const double* eps, double* r_out);
+
+/* gauss_profile(coords; z, omega0, f): the normalised 2D Gaussian beam at
+ * distance z from its waist, out (nx, ny) complex.  FP64 on the host.
+ * Replaces src/beam_gaussian.jl:24-37. */
+int bf_gauss_profile(int nx, int ny, const double* X, const double* Y, double z, double omega0, double f,
+                     double* out);
+
+/* ---- antenna coupling ----------------------------------------------------- */
+/* unnormalized_match(Eout, Eantenna; dx, dy) for nb fields at once:
+ * out[b] = dx dy sum_p E[b][p] conj(Eantenna[p]), E nb x npix complex (device
+ * memory with BF_IN_DEVICE), Eantenna npix complex, out nb complex (host).
+ * Replaces src/beam_coupling.jl:13-15. */
+int bf_unnormalized_match(bf_handle* h, int nb, int npix, const double* E, const double* Eantenna, double dx,
+                          double dy, int flags, double* out);
 
 /* ---- per-op propagator: the `prop=` drop-in ------------------------------ */
 /* E (nx, ny) complex, propagated in place by distance dz through a medium of
@@ -234,6 +249,17 @@ int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double*
                    int prop_kind, int precision, const double* emit, const double* reflect,
                    const double* propagation_matrices, int pm_per_freq, double* out_boost,
                    double* out_refl, double* out_beta2);
+
+/* The transformer with the antenna coupling fused after the boundary solve:
+ * out_coupled[f] = |sum_m conj(boost_m) antenna_m|^2, antenna = the antenna's
+ * mode coefficients (field2modes of e.g. gauss_profile), nm complex; the
+ * coupled power of the reference's optimiser cost
+ * (examples/transformer_optim_utilities.jl:137).  Other arguments as in
+ * bf_transformer (mirror eps NaN taken as 1e30); out_beta2 may be NULL. */
+int bf_transformer_coupled(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs, int prop_kind,
+                           int precision, const double* emit, const double* antenna,
+                           const double* propagation_matrices, int pm_per_freq, double* out_coupled,
+                           double* out_beta2);
 
 /* transformer_trace_back for nf frequencies: starting from vcat(input_beam,
  * reflected_beam) in the last region, apply G_s blockdiag(P_s, inv(P_s))

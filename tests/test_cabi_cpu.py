@@ -61,6 +61,20 @@ def test_kspace_helper_matches_oracle(L):
         assert np.max(np.abs(got - ref) / np.maximum(1e-300, np.abs(ref).max())) < 1e-15
 
 
+def test_gauss_profile_matches_golden_and_oracle(L):
+    """bf_gauss_profile (host FP64) against test/runtests.jl:47 and the oracle."""
+    import bfgb300 as B
+    from tests.golden import reference_goldens as G
+    c, co = B.SeedCoordinateSystem(), O.seed_coordinate_system()
+    g = B.gauss_profile(c, z=1e-9, omega0=0.097, f=22e9)
+    got = g.flatten(order="F")[3999]
+    assert abs(got - G.GAUSS_4000) / abs(G.GAUSS_4000) < G.RTOL
+    for z, w0, f in ((1e-9, 0.097, 22e9), (0.3, 0.05, 19e9)):
+        ref = O.gauss_profile(co, z=z, omega0=w0, f=f)
+        got = B.gauss_profile(c, z=z, omega0=w0, f=f)
+        assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-13
+
+
 def test_seed_setup_boundaries_matches_oracle(L):
     import bfgb300 as B
     c = B.SeedCoordinateSystem()

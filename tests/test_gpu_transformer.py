@@ -282,6 +282,43 @@ def test_tf32_rejected_by_bounce_solvers(B):
     st.close()
 
 
+def test_unnormalized_match_golden_and_batch(B):
+    """unnormalized_match (beam_coupling.jl:13-15) on the GPU: the golden of
+    test/runtests.jl:52, and a batch of fields against the oracle."""
+    c, co = B.SeedCoordinateSystem(), O.seed_coordinate_system()
+    g = B.gauss_profile(c, z=1e-9, omega0=0.097, f=22e9)
+    dx = 0.0001 * math.floor(10000.0 * (c.X[1] - c.X[0]))
+    m = B.unnormalized_match(g, 3 * g, dx=dx, dy=dx)
+    assert abs(m - G.MATCH) / abs(G.MATCH) < G.RTOL
+    rng = np.random.default_rng(3)
+    E = rng.standard_normal((5,) + g.shape) + 1j * rng.standard_normal((5,) + g.shape)
+    got = B.unnormalized_match(E, g, dx=0.01, dy=0.02)
+    ref = np.array([O.unnormalized_match(e, g, dx=0.01, dy=0.02) for e in E])
+    assert rel(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", FP64_TOL), ("mixed", MIXED_BETA2_TOL)])
+def test_transformer_coupled_vs_oracle(B, precision, tol):
+    """The antenna coupling fused into the transformer output: |sum conj(boost)
+    * antenna|^2 per frequency (transformer_optim_utilities.jl:137), with the
+    antenna's mode coefficients from field2modes(gauss_profile)."""
+    distance, eps, tx, ty, X, s = _stack(2, 48, seed=23, surf=True)
+    kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=4, Lmax=1, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=4, Lmax=1, diskR=0.15)
+    ant = O.field2modes(O.gauss_profile(co, z=0.2, omega0=0.05, f=20e9), co, mo, diskR=0.15)
+    freqs = np.array([19.4e9, 20.0e9, 20.7e9])
+    cpl, b2 = B.transformer_coupled(B.SeedSetupBoundaries(cb, **kw), cb, mb, ant, f=freqs, precision=precision)
+    for k, f in enumerate(freqs):
+        boost = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
+        ref = abs(np.sum(np.conj(boost) * ant)) ** 2
+        assert abs(cpl[k] - ref) / ref < tol
+        r2 = np.sum(np.abs(boost) ** 2)
+        assert abs(b2[k] - r2) / r2 < tol
+
+
 def test_transformer_1d_vs_analytical1d(B):
     d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
     c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
