@@ -30,7 +30,7 @@ __all__ = [
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
-    "gauss_profile", "unnormalized_match", "transformer_coupled",
+    "gauss_profile", "unnormalized_match", "transformer_coupled", "transformer_1d_batch",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -662,6 +662,24 @@ def transformer_coupled(bdry, coords, modes, antenna, f=10.0e9, prop=propagator,
     if np.ndim(f) == 0:
         return float(cpl[0]), float(b2[0])
     return cpl, b2
+
+
+def transformer_1d_batch(distances, eps, freqs, emit=None, handle=None):
+    """The 1D transformer (propagator1D, one 1D mode) for many spacing
+    configurations at once: distances (nconf, nd), eps (nd,) shared, freqs (nf,).
+    Returns (boost, beta2), both (nconf, nf)."""
+    h = handle or default_handle()
+    d = np.ascontiguousarray(np.atleast_2d(distances), dtype=np.float64)
+    nconf, nd = d.shape
+    e = np.ascontiguousarray(eps, dtype=np.complex128).reshape(nd)
+    fr = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+    em = None if emit is None else np.array([complex(emit)], dtype=np.complex128)
+    boost = np.empty((nconf, len(fr)), dtype=np.complex128)
+    beta2 = np.empty((nconf, len(fr)))
+    h.check(_lib.lib().bf_transformer_1d_batch(
+        h.ptr, nconf, nd, _lib.ptr(d), _lib.ptr(e.view(np.float64)), len(fr), _lib.ptr(fr),
+        _lib.ptr(None if em is None else em.view(np.float64)), _lib.ptr(boost.view(np.float64)), _lib.ptr(beta2)))
+    return boost, beta2
 
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,

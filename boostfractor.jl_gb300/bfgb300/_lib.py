@@ -71,6 +71,8 @@ _SIGS = {
     "bf_unnormalized_match": (_c_int, [_vp, _c_int, _c_int, _vp, _p_dbl, _c_dbl, _c_dbl, _c_int, _p_dbl]),
     "bf_transformer_coupled": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl,
                                         _c_int, _p_dbl, _p_dbl]),
+    "bf_transformer_1d_batch": (_c_int, [_vp, _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl, _p_dbl, _p_dbl,
+                                         _p_dbl]),
     "bf_transformer_trace_back": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _c_int,
                                            _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl]),
     "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),

@@ -1779,6 +1779,94 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
                 pm_per_freq, out_boost, out_refl, out_beta2, 1, 0, nullptr);
 }
 
+// ---- batched 1D model: one thread per (spacing configuration, frequency) ------
+// transformer(bdry, coords, SeedModes(coords; ThreeDim=false); prop=propagator1D)
+// with every matrix a scalar: P_j = exp(-i k0_j dz_j), T21' = s_j P_j (a_j T21 +
+// b_j T22), T22' = s_j / P_j (b_j T21 + a_j T22), axion_beam += S_j (T21 + T22)
+// emit, boost = -axion_beam / T22 (src/boost_fractor_transformer.jl:285-359).
+struct Region1D {
+  double2 a, b, inv2n, S;   // as ChainRegion
+  double2 n;                // sqrt(eps_j) of the propagated region
+};
+
+__global__ void k_tf1d(const double* dist, int nd, const Region1D* rg, const double* freqs, int nf, int nconf,
+                       double2 emit, double2* boost, double* beta2) {
+  const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= (long)nconf * nf) return;
+  const int c = (int)(i / nf), f = (int)(i % nf);
+  const double* dz = dist + (size_t)c * nd;
+  const double kc = 2.0 * M_PI / (kC / freqs[f]);
+  double2 t21 = make_double2(0.0, 0.0), t22 = make_double2(1.0, 0.0), ax = make_double2(0.0, 0.0);
+  for (int j = 1; j < nd; ++j) {
+    const Region1D g = rg[j];
+    ax = bf::cadd(ax, bf::cmul(g.S, bf::cmul(bf::cadd(t21, t22), emit)));
+    const double kr = kc * g.n.x, ki = kc * g.n.y;
+    const double2 P = dexp_c(ki * dz[j], -kr * dz[j]);
+    const double2 Pi = bf::crecip(P);
+    const double2 u = bf::cadd(bf::cmul(g.a, t21), bf::cmul(g.b, t22));
+    const double2 v = bf::cadd(bf::cmul(g.b, t21), bf::cmul(g.a, t22));
+    t21 = bf::cmul(g.inv2n, bf::cmul(u, P));
+    t22 = bf::cmul(g.inv2n, bf::cmul(v, Pi));
+  }
+  const double d = t22.x * t22.x + t22.y * t22.y;
+  const double2 q = make_double2(-(ax.x * t22.x + ax.y * t22.y) / d, -(ax.y * t22.x - ax.x * t22.y) / d);
+  if (boost) boost[i] = q;
+  beta2[i] = q.x * q.x + q.y * q.y;
+}
+
+extern "C" int bf_transformer_1d_batch(bf_handle* h, int nconf, int nd, const double* distances, const double* eps,
+                                       int nf, const double* freqs, const double* emit, double* out_boost,
+                                       double* out_beta2) {
+  if (!h) return BF_ERR_INVALID;
+  if (nconf < 1 || nd < 3 || nf < 1 || !distances || !eps || !freqs || !out_beta2)
+    return bf_fail(h, BF_ERR_INVALID, "transformer_1d_batch: empty or null input");
+  for (size_t i = 0; i < (size_t)nconf * nd; ++i)
+    if (!std::isfinite(distances[i])) return bf_fail(h, BF_ERR_INVALID, "non-finite distance");
+  for (int i = 0; i < nf; ++i)
+    if (!(freqs[i] > 0.0) || !std::isfinite(freqs[i]))
+      return bf_fail(h, BF_ERR_INVALID, "frequencies must be finite and positive");
+  TCK(cudaSetDevice(h->device));
+  cudaStream_t st = h->stream();
+  // permittivities as the stacks hold them (real eps as re - 0.0im), NaN mirror -> 1e30
+  std::vector<cd> e(nd);
+  for (int j = 0; j < nd; ++j) {
+    cd v = as_cdp(eps)[j];
+    if (std::isnan(v.real()) || std::isnan(v.imag())) v = cd(1e30, 0.0);
+    e[j] = bfhost::eps_cast(v);
+  }
+  std::vector<Region1D> rg(nd);
+  for (int j = 1; j < nd; ++j) {
+    const cd nl = std::sqrt(e[j]), nr = std::sqrt(e[j - 1]);
+    rg[j].a = make_double2((nr + nl).real(), (nr + nl).imag());
+    rg[j].b = make_double2((nr - nl).real(), (nr - nl).imag());
+    const cd inv = 1.0 / (2.0 * nr);
+    rg[j].inv2n = make_double2(inv.real(), inv.imag());
+    const cd S = (1.0 / (nr * nr) - 1.0 / (nl * nl)) / 2.0;
+    rg[j].S = make_double2(S.real(), S.imag());
+    rg[j].n = make_double2(nl.real(), nl.imag());
+  }
+  const double2 em = emit ? make_double2(emit[0], emit[1]) : make_double2(1.0, 0.0);
+  const size_t npts = (size_t)nconf * nf;
+  DBuf d_dist, d_rg, d_f, d_b, d_b2;
+  TCKS(d_dist.alloc(h, sizeof(double) * (size_t)nconf * nd));
+  TCK(cudaMemcpyAsync(d_dist.p, distances, sizeof(double) * (size_t)nconf * nd, cudaMemcpyHostToDevice, st));
+  TCKS(d_rg.alloc(h, sizeof(Region1D) * nd));
+  TCK(cudaMemcpyAsync(d_rg.p, rg.data(), sizeof(Region1D) * nd, cudaMemcpyHostToDevice, st));
+  TCKS(d_f.alloc(h, sizeof(double) * nf));
+  TCK(cudaMemcpyAsync(d_f.p, freqs, sizeof(double) * nf, cudaMemcpyHostToDevice, st));
+  if (out_boost) TCKS(d_b.alloc(h, sizeof(double2) * npts));
+  TCKS(d_b2.alloc(h, sizeof(double) * npts));
+  bf::note_launch();
+  k_tf1d<<<(unsigned)((npts + 255) / 256), 256, 0, st>>>(d_dist.as<double>(), nd, d_rg.as<Region1D>(),
+                                                          d_f.as<double>(), nf, nconf, em,
+                                                          out_boost ? d_b.as<double2>() : nullptr, d_b2.as<double>());
+  TCK(cudaGetLastError());
+  if (out_boost) TCK(cudaMemcpyAsync(out_boost, d_b.p, sizeof(double2) * npts, cudaMemcpyDeviceToHost, st));
+  TCK(cudaMemcpyAsync(out_beta2, d_b2.p, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
+  TCK(cudaStreamSynchronize(st));
+  return BF_OK;
+}
+
 extern "C" int bf_transformer_coupled(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs,
                                       int prop_kind, int precision, const double* emit, const double* antenna,
                                       const double* propagation_matrices, int pm_per_freq, double* out_coupled,

@@ -261,6 +261,16 @@ int bf_transformer_coupled(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const
                            const double* propagation_matrices, int pm_per_freq, double* out_coupled,
                            double* out_beta2);
 
+/* Batched 1D model: transformer(bdry, coords, SeedModes(coords; ThreeDim=false);
+ * prop=propagator1D) (src/boost_fractor_transformer.jl:285-359, the 1D model of
+ * src/Analytical1D.py) for nconf spacing configurations x nf frequencies in one
+ * launch, FP64.  distances: nconf x nd (configuration-major, each the nd region
+ * distances of one booster); eps: nd complex shared by all (NaN mirror taken
+ * as 1e30); emit: 1 complex or NULL (= 1, the axion-induced 1D mode).
+ * out_boost (nconf x nf complex, or NULL) and out_beta2 (nconf x nf) = |boost|^2. */
+int bf_transformer_1d_batch(bf_handle* h, int nconf, int nd, const double* distances, const double* eps, int nf,
+                            const double* freqs, const double* emit, double* out_boost, double* out_beta2);
+
 /* transformer_trace_back for nf frequencies: starting from vcat(input_beam,
  * reflected_beam) in the last region, apply G_s blockdiag(P_s, inv(P_s))
  * (+ axion_S_factor [emit; emit] when includes_axion) region by region.

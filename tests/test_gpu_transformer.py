@@ -319,6 +319,40 @@ def test_transformer_coupled_vs_oracle(B, precision, tol):
         assert abs(b2[k] - r2) / r2 < tol
 
 
+def test_1d_batch_vs_oracle(B):
+    """bf_transformer_1d_batch: 24 spacing configurations of a 5-disk booster x
+    9 frequencies in one launch against the oracle's 1D transformer
+    (propagator1D, ThreeDim=false) at the FP64 bar."""
+    from bfgb300 import workloads as W
+    rng = np.random.default_rng(31)
+    distance, eps, _, _ = W.booster(5, rng.uniform(7e-3, 9e-3, 5), eps_disk=9.4)
+    confs = np.array([W.optimiser_step(distance, rng, sigma=1e-4) for _ in range(24)])
+    freqs = np.linspace(18.5e9, 21.5e9, 9)
+    boost, beta2 = B.transformer_1d_batch(confs, eps, freqs)
+    c1 = O.seed_coordinate_system(X=np.array([1e-7]), Y=np.array([1e-7]))
+    m1 = O.seed_modes(c1, ThreeDim=False)
+    for c in range(0, 24, 5):
+        for k, f in enumerate(freqs):
+            sb = O.seed_setup_boundaries(c1, diskno=5, distance=confs[c], epsilon=eps.copy())
+            ref = O.transformer(sb, c1, m1, f=f, prop=O.propagator1d)[0]
+            assert abs(boost[c, k] - ref) / abs(ref) < FP64_TOL
+            assert abs(beta2[c, k] - abs(ref) ** 2) / abs(ref) ** 2 < FP64_TOL
+
+
+def test_1d_batch_vs_analytical1d(B):
+    """The reference's own 1D model (src/Analytical1D.py) through the batched entry point."""
+    d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
+    for k in range(int(d["ncases"])):
+        nd, eps_d, spac, freqs, gold = int(d[f"nd_{k}"]), float(d[f"eps_{k}"]), d[f"spacings_{k}"], d[f"freqs_{k}"], d[f"beta2_{k}"]
+        dist, eps = [0.0], [np.nan]
+        for i in range(nd):
+            dist += [spac[i], 1e-3]
+            eps += [1.0, eps_d]
+        dist += [0.0]; eps += [1.0]
+        _, b2 = B.transformer_1d_batch(np.array([dist]), np.array(eps, dtype=complex), freqs)
+        assert np.allclose(b2[0], gold, rtol=1e-6), k
+
+
 def test_transformer_1d_vs_analytical1d(B):
     d = np.load(os.path.join(HERE, "golden", "analytical1d.npz"))
     c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
