@@ -629,6 +629,74 @@ def run_serve(args, optimiser_class=False):
          "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
 
 
+def run_1d(args):
+    """Batched 1D model: 4096 spacing configurations of the 20-disk booster
+    (each gap moved by N(0, 10 um) from the seeded geometry) x 256 frequencies
+    19.5-20.5 GHz per step, one FP64 launch (bf_transformer_1d_batch).  The
+    plain path solves one configuration per 1D transformer call."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    from bfgb300 import _lib
+    w = W.config2_cheerleader()
+    rng = np.random.default_rng(77)
+    nconf, nf = 4096, 256
+    confs = np.ascontiguousarray([W.optimiser_step(w["distance"], rng) for _ in range(nconf)])
+    eps = np.ascontiguousarray(w["eps"], dtype=np.complex128)
+    freqs = np.ascontiguousarray(np.linspace(19.5e9, 20.5e9, nf))
+    h = B.Handle(0)
+    stream = torch.cuda.current_stream()
+    h.set_stream(stream.cuda_stream)
+    b2 = np.empty((nconf, nf))
+    L = _lib.lib()
+
+    def step():
+        h.check(L.bf_transformer_1d_batch(h.ptr, nconf, len(eps), _lib.ptr(confs), _lib.ptr(eps.view(np.float64)), nf,
+                                          _lib.ptr(freqs), None, None, _lib.ptr(b2)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    # plain: the 1D transformer per configuration (frequencies batched), 32 configurations
+    c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
+    m1 = B.SeedModes(c1, ThreeDim=False, handle=h)
+    t0 = time.perf_counter()
+    for c in range(32):
+        sb = B.SeedSetupBoundaries(c1, diskno=20, distance=confs[c], epsilon=w["eps"].copy())
+        B.transformer(sb, c1, m1, f=freqs, prop=B.propagator1D)
+    plain = 32 * nf / (time.perf_counter() - t0)
+    # accuracy: the oracle's 1D transformer on a sample of points
+    sys.path.insert(0, REPO)
+    from oracle import bf_oracle as O
+    co = O.seed_coordinate_system(X=np.array([1e-7]), Y=np.array([1e-7]))
+    mo = O.seed_modes(co, ThreeDim=False)
+    errs = []
+    for c, k in ((0, 0), (1000, 100), (4095, 255), (2048, 128)):
+        sb = O.seed_setup_boundaries(co, diskno=20, distance=confs[c], epsilon=w["eps"].copy())
+        ref = abs(O.transformer(sb, co, mo, f=freqs[k], prop=O.propagator1d)[0]) ** 2
+        errs.append(abs(b2[c, k] - ref) / ref)
+    m1.close()
+    h.close()
+    line = {"metric": "beta2 freq-points/s (batched 1D model, 20-disk booster, spacing configurations x frequencies)",
+            "value": nconf * nf / wall, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded geometry, gap steps N(0, 10 um))",
+            "config": {"workload": f"1d-20disk-{nconf}configs-{nf}f", "configs": nconf, "freqs": nf,
+                       "timing": "host wall clock around the C ABI call (host buffers in and out)"},
+            "plain_freqpts_per_s": plain, "beta2_rel_err_vs_oracle_max": float(max(errs)),
+            "e2e": {"value": nconf * nf / wall, "unit": UNIT, "h2d_bytes_per_step": int(confs.nbytes + freqs.nbytes),
+                    "d2h_bytes_per_step": int(b2.nbytes)}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     ws, rank, local = dist_env()
     if rank != 0:
@@ -673,7 +741,7 @@ def main():
     ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cheerleader",
-                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt"])
+                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "1d"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
@@ -682,6 +750,8 @@ def main():
         run_transformer(args)
     elif args.workload == "uneven" and args.impl == "ours":
         run_uneven(args)
+    elif args.workload == "1d" and args.impl == "ours":
+        run_1d(args)
     elif args.workload in ("serve", "serve-opt") and args.impl == "ours":
         run_serve(args, optimiser_class=args.workload == "serve-opt")
     elif args.impl == "reference":
