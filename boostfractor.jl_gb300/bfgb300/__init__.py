@@ -31,6 +31,7 @@ __all__ = [
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
     "gauss_profile", "unnormalized_match", "transformer_coupled", "transformer_1d_batch",
+    "PGrid",
 ]
 
 SPEED_OF_LIGHT = 299792458.0
@@ -680,6 +681,54 @@ def transformer_1d_batch(distances, eps, freqs, emit=None, handle=None):
         h.ptr, nconf, nd, _lib.ptr(d), _lib.ptr(e.view(np.float64)), len(fr), _lib.ptr(fr),
         _lib.ptr(None if em is None else em.view(np.float64)), _lib.ptr(boost.view(np.float64)), _lib.ptr(beta2)))
     return boost, beta2
+
+
+class PGrid:
+    """Propagation matrices on a grid of gap spacings, resident on the device,
+    with spline interpolation (examples/transformer_optim_utilities.jl:11-91).
+    spacing_grid is an evenly spaced sequence (the reference's range)."""
+
+    def __init__(self, bdry, coords, modes, frequencies, spacing_grid, prop=propagator, diskR=0.15,
+                 precision="fp64"):
+        sg = np.asarray(spacing_grid, dtype=np.float64)
+        if sg.ndim != 1 or len(sg) < 2 or not np.allclose(np.diff(sg), sg[1] - sg[0], rtol=1e-9, atol=0):
+            raise ValueError("spacing_grid must be an evenly spaced sequence of at least 2 values")
+        self.h = modes.h
+        self.modes = modes
+        self.freqs = np.ascontiguousarray(np.atleast_1d(frequencies), dtype=np.float64)
+        self.stack = Stack(bdry, coords, diskR, handle=self.h)
+        self.nd, self.nm = self.stack.nd, modes.nm
+        g = _lib._vp()
+        self.h.check(_lib.lib().bf_pgrid_create(self.h.ptr, self.stack._s, modes._m, len(self.freqs),
+                                                _lib.ptr(self.freqs), len(sg), float(sg[0]), float(sg[1] - sg[0]),
+                                                _prop_kind(prop), _prec(precision), ctypes.byref(g)))
+        self._g = g
+
+    def matrices(self, dist_shift):
+        """interpolate_prop_matrix: [nf][nd] (nm, nm) matrices as an array."""
+        sh = np.ascontiguousarray(dist_shift, dtype=np.float64)
+        out = np.empty((len(self.freqs), self.nd, self.nm, self.nm), dtype=np.complex128)
+        self.h.check(_lib.lib().bf_pgrid_matrices(self.h.ptr, self._g, _lib.ptr(sh), _lib.ptr(out.view(np.float64))))
+        return out.transpose(0, 1, 3, 2).copy()
+
+    def transformer(self, dist_shift, emit=None):
+        """calc_boostfactor_modes on the interpolated matrices: (boost [nf, nm], beta2 [nf])."""
+        sh = np.ascontiguousarray(dist_shift, dtype=np.float64)
+        eb = None if emit is None else np.ascontiguousarray(emit, dtype=np.complex128).reshape(self.nm)
+        boost = np.empty((len(self.freqs), self.nm), dtype=np.complex128)
+        beta2 = np.empty(len(self.freqs))
+        self.h.check(_lib.lib().bf_pgrid_transformer(self.h.ptr, self._g, _lib.ptr(sh),
+                                                     _lib.ptr(None if eb is None else eb.view(np.float64)),
+                                                     _lib.ptr(boost.view(np.float64)), _lib.ptr(beta2)))
+        return boost, beta2
+
+    def close(self):
+        if getattr(self, "_g", None) and self.h._h:
+            _lib.lib().bf_pgrid_destroy(self.h.ptr, self._g)
+        self._g = None
+        if getattr(self, "stack", None) is not None:
+            self.stack.close()
+            self.stack = None
 
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,

@@ -73,6 +73,11 @@ _SIGS = {
                                         _c_int, _p_dbl, _p_dbl]),
     "bf_transformer_1d_batch": (_c_int, [_vp, _c_int, _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl, _p_dbl, _p_dbl,
                                          _p_dbl]),
+    "bf_pgrid_create": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_dbl, _c_dbl, _c_int, _c_int,
+                                 ctypes.POINTER(_vp)]),
+    "bf_pgrid_destroy": (_c_int, [_vp, _vp]),
+    "bf_pgrid_matrices": (_c_int, [_vp, _vp, _p_dbl, _p_dbl]),
+    "bf_pgrid_transformer": (_c_int, [_vp, _vp, _p_dbl, _p_dbl, _p_dbl, _p_dbl]),
     "bf_transformer_trace_back": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _c_int,
                                            _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl]),
     "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),

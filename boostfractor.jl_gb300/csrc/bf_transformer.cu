@@ -1536,7 +1536,8 @@ template <typename PT>
 static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                     const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                     double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
-                    double* out_pm, int mode, const TraceArgs* tb = nullptr, const CoupleArgs* cp = nullptr) {
+                    double* out_pm, int mode, const TraceArgs* tb = nullptr, const CoupleArgs* cp = nullptr,
+                    const PT* P_dev = nullptr) {
   constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
@@ -1574,7 +1575,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
       TCKS(P.alloc(h, sizeof(PT) * hp.size()));
       if (bf::launch_convert(P64.p, true, P.p, false, hp.size(), st)) return bf_fail(h, BF_ERR_CUDA, "convert");
     }
-  } else {
+  } else if (!P_dev) {
     TfCache* c = nullptr;
     TCKS(tf_setup(h, s, md, mode, &c));
     const int j0 = only_matrices ? 0 : 1;
@@ -1608,7 +1609,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   // moves beta^2 by ~1e-6); the chain's T in FP64 or double-float, and the
   // boundary solve, near resonance, in FP64.
   using D2 = PT;
-  const D2* Pd = P.as<D2>();
+  const D2* Pd = P_dev ? P_dev : P.as<D2>();
   TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
   if (nm <= 16) {
     const int nmat = (nd - 1) * nf;
@@ -1664,7 +1665,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaGetLastError());
     TCK(cudaMemcpyAsync(tb->out, d_out.p, sizeof(cd) * nout, cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
-    if (mode == 2 && !pm) TCKS(tc_status(h));
+    if (mode == 2 && !pm && !P_dev) TCKS(tc_status(h));
     return BF_OK;
   }
   // T21 / T22 for the boundary solve, FP64
@@ -1737,7 +1738,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   if (cp) TCK(cudaMemcpyAsync(cp->out, d_cpl.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
-  if (mode == 2 && !pm) TCKS(tc_status(h));
+  if (mode == 2 && !pm && !P_dev) TCKS(tc_status(h));
   return BF_OK;
 }
 
@@ -1900,4 +1901,250 @@ extern "C" int bf_calc_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes*
   TCK(cudaSetDevice(h->device));
   return tf_run(h, s, md, nf, freqs, prop_kind, precision, nullptr, nullptr, nullptr, 0, nullptr,
                 nullptr, nullptr, 0, 1, out);
+}
+
+// ---------------------------------------------------------------------------
+// Propagation-matrix grid over gap spacings, with interpolation
+// (examples/transformer_optim_utilities.jl:11-91: calc_propagation_matrices_grid,
+// construct_prop_matrix_interpolation, interpolate_prop_matrix).
+// ---------------------------------------------------------------------------
+// Gaps are the regions 1, 3, ..., nd-1 (the reference's ind_gap = 2:2:n_region,
+// the last region included); the others (mirror, disks) are computed once per
+// frequency.  At grid point k every gap's distance is d0 + s0 + k ds.
+struct bf_pgrid {
+  bf_stack* s = nullptr;
+  bf_modes* md = nullptr;
+  int nf = 0, nd = 0, nm = 0, nsp = 0, ngap = 0;
+  double s0 = 0.0, ds = 0.0;
+  std::vector<double> freqs;
+  std::vector<int> gap_of;   // region -> gap slot, or -1
+  DBuf gap_d, solid, coef;   // gap_of on the device; solids [nf][nd][nm^2]; [ngap][nf][nsp + 2][nm^2]
+  DBuf thomas;               // 1/(4 - c'_{k-1}) and c'_k of the spline system, 2 (nsp + 2) doubles
+};
+
+namespace {
+
+// grid value of gap g at spacing k: coef[g][f][k + 1][e] = P_k[f][j][e]; solids at k = 0
+template <typename PT>
+__global__ void k_pgrid_gather(double2* coef, double2* solid, const PT* P, const int* gap_of, int nf, int nd, int nm2,
+                               int nsp, int k) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nf * nd * nm2) return;
+  const int e = (int)(i % nm2);
+  const int j = (int)((i / nm2) % nd);
+  const int f = (int)(i / ((size_t)nm2 * nd));
+  const double2 v = bf::to_d(P[i]);
+  const int g = gap_of[j];
+  if (g >= 0)
+    coef[(((size_t)g * nf + f) * (nsp + 2) + k + 1) * nm2 + e] = v;
+  else if (k == 0)
+    solid[i] = v;
+}
+
+// Natural cubic B-spline prefilter along the spacing axis, in place.  Data
+// y_1..y_n sit at coef[1..n]; the coefficients satisfy (c_{k-1} + 4 c_k +
+// c_{k+1}) / 6 = y_k and S'' = 0 at both end knots, so c_1 = y_1, c_n = y_n,
+// c_0 = 2 c_1 - c_2, c_{n+1} = 2 c_n - c_{n-1}; the interior is a constant
+// tridiagonal system solved with the host-computed Thomas factors.
+__global__ void k_pgrid_prefilter(double2* coef, const double* thomas, int nseq_outer, int nm2, int nsp) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nseq_outer * nm2) return;
+  const int e = (int)(i % nm2);
+  double2* c = coef + (i / nm2) * (size_t)(nsp + 2) * nm2 + e;
+  const int n = nsp;
+  auto at = [&](int k) -> double2& { return c[(size_t)k * nm2]; };
+  if (n >= 3) {
+    const double* den = thomas;            // den[k] = 1 / (4 - c'_{k-1}), k = 2..n-1
+    const double* cpr = thomas + (n + 2);  // c'_k, k = 2..n-1
+    const double2 y1 = at(1), yn = at(n);
+    // forward sweep: d'_k = (r_k - d'_{k-1}) den_k, with r_k = 6 y_k (minus the known ends)
+    double2 prev = make_double2(0.0, 0.0);
+    for (int k = 2; k <= n - 1; ++k) {
+      double2 r = make_double2(6.0 * at(k).x, 6.0 * at(k).y);
+      if (k == 2) r = bf::csub(r, y1);
+      if (k == n - 1) r = bf::csub(r, yn);
+      const double2 d = make_double2((r.x - prev.x) * den[k], (r.y - prev.y) * den[k]);
+      at(k) = d;
+      prev = d;
+    }
+    for (int k = n - 2; k >= 2; --k) {
+      const double2 nx = at(k + 1);
+      at(k) = make_double2(at(k).x - cpr[k] * nx.x, at(k).y - cpr[k] * nx.y);
+    }
+  }
+  at(0) = make_double2(2.0 * at(1).x - at(2).x, 2.0 * at(1).y - at(2).y);
+  at(n + 1) = make_double2(2.0 * at(n).x - at(n - 1).x, 2.0 * at(n).y - at(n - 1).y);
+}
+
+// P[f][j][e] at the gap positions x[j] (data coordinates 1..n): uniform cubic
+// B-spline weights on c_{i-1..i+2}, i = floor(x) (n - 1 at the last knot)
+__global__ void k_pgrid_eval(double2* P, const double2* solid, const double2* coef, const int* gap_of,
+                             const double* xpos, int nf, int nd, int nm2, int nsp) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nf * nd * nm2) return;
+  const int e = (int)(i % nm2);
+  const int j = (int)((i / nm2) % nd);
+  const int f = (int)(i / ((size_t)nm2 * nd));
+  const int g = gap_of[j];
+  if (g < 0) {
+    P[i] = solid[i];
+    return;
+  }
+  const double x = xpos[j];
+  int k = (int)floor(x);
+  if (k >= nsp) k = nsp - 1;
+  if (k < 1) k = 1;
+  const double t = x - k, t2 = t * t, t3 = t2 * t;
+  const double w0 = (1.0 - t) * (1.0 - t) * (1.0 - t) / 6.0;
+  const double w1 = (3.0 * t3 - 6.0 * t2 + 4.0) / 6.0;
+  const double w2 = (-3.0 * t3 + 3.0 * t2 + 3.0 * t + 1.0) / 6.0;
+  const double w3 = t3 / 6.0;
+  const double2* c = coef + ((size_t)g * nf + f) * (size_t)(nsp + 2) * nm2 + e;
+  const double2 a = c[(size_t)(k - 1) * nm2], b = c[(size_t)k * nm2], d = c[(size_t)(k + 1) * nm2],
+                q = c[(size_t)(k + 2) * nm2];
+  P[i] = make_double2(w0 * a.x + w1 * b.x + w2 * d.x + w3 * q.x, w0 * a.y + w1 * b.y + w2 * d.y + w3 * q.y);
+}
+
+template <typename PT>
+int pgrid_fill(bf_handle* h, bf_pgrid* G, int prop_kind, int mode) {
+  bf_stack* s = G->s;
+  cudaStream_t st = h->stream();
+  const int nm2 = G->nm * G->nm;
+  TfCache* c = nullptr;
+  TCKS(tf_setup(h, s, G->md, mode, &c));
+  std::vector<double> d0 = s->distance;
+  DBuf P;
+  int rc = BF_OK;
+  for (int k = 0; k < G->nsp && rc == BF_OK; ++k) {
+    for (int j = 0; j < G->nd; ++j)
+      if (G->gap_of[j] >= 0) s->distance[j] = d0[j] + G->s0 + k * G->ds;
+    std::vector<RegionT> regs;
+    classify(h, s, prop_kind, s->eps, regs);
+    rc = tf_propagation_matrices<PT>(h, s, G->md, *c, regs, 0, G->nf, G->freqs, prop_kind, P, mode);
+    if (rc != BF_OK) break;
+    bf::note_launch();
+    k_pgrid_gather<PT><<<blocks_for((size_t)G->nf * G->nd * nm2), 256, 0, st>>>(
+        G->coef.as<double2>(), G->solid.as<double2>(), P.as<PT>(), G->gap_d.as<int>(), G->nf, G->nd, nm2, G->nsp,
+        k);
+    if (cudaGetLastError() != cudaSuccess) rc = bf_fail(h, BF_ERR_CUDA, "pgrid gather");
+  }
+  s->distance = d0;   // the stack keeps its own distances
+  if (rc != BF_OK) return rc;
+  TCK(cudaStreamSynchronize(st));
+  return BF_OK;
+}
+
+}  // namespace
+
+extern "C" int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int nsp,
+                               double spacing_first, double spacing_step, int prop_kind, int precision,
+                               bf_pgrid** out) {
+  if (!out) return BF_ERR_INVALID;
+  *out = nullptr;
+  TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
+  if (precision == BF_PREC_TF32) return bf_fail(h, BF_ERR_INVALID, "pgrid: BF_PREC_FP64 or BF_PREC_MIXED");
+  if (nsp < 2 || nsp > BF_PGRID_MAX_SPACINGS || !(spacing_step > 0.0) || !std::isfinite(spacing_first))
+    return bf_fail(h, BF_ERR_INVALID, "pgrid: 2..64 spacings with a positive step");
+  TCK(cudaSetDevice(h->device));
+  std::unique_ptr<bf_pgrid> G(new bf_pgrid());
+  G->s = s;
+  G->md = md;
+  G->nf = nf;
+  G->nd = s->nd;
+  G->nm = md->nm;
+  G->nsp = nsp;
+  G->s0 = spacing_first;
+  G->ds = spacing_step;
+  G->freqs.assign(freqs, freqs + nf);
+  G->gap_of.assign(s->nd, -1);
+  for (int j = 1; j < s->nd; j += 2) G->gap_of[j] = G->ngap++;
+  const size_t nm2 = (size_t)G->nm * G->nm;
+  cudaStream_t st = h->stream();
+  TCKS(G->gap_d.alloc(h, sizeof(int) * s->nd));
+  TCK(cudaMemcpyAsync(G->gap_d.p, G->gap_of.data(), sizeof(int) * s->nd, cudaMemcpyHostToDevice, st));
+  TCKS(G->solid.alloc(h, sizeof(double2) * nf * s->nd * nm2));
+  TCKS(G->coef.alloc(h, sizeof(double2) * (size_t)G->ngap * nf * (nsp + 2) * nm2));
+  // Thomas factors of the interior system (1, 4, 1), unknowns c_2 .. c_{n-1}
+  std::vector<double> th(2 * (nsp + 2), 0.0);
+  double cp = 0.0;
+  for (int k = 2; k <= nsp - 1; ++k) {
+    const double den = 1.0 / (4.0 - (k == 2 ? 0.0 : cp));
+    th[k] = den;
+    cp = den;   // c'_k = 1 / (4 - c'_{k-1}) (the superdiagonal is 1)
+    th[(nsp + 2) + k] = cp;
+  }
+  TCKS(G->thomas.alloc(h, sizeof(double) * th.size()));
+  TCK(cudaMemcpyAsync(G->thomas.p, th.data(), sizeof(double) * th.size(), cudaMemcpyHostToDevice, st));
+  if (precision == BF_PREC_FP64) TCKS(pgrid_fill<double2>(h, G.get(), prop_kind, 0));
+  else TCKS(pgrid_fill<float2>(h, G.get(), prop_kind, 1));
+  const size_t nseq = (size_t)G->ngap * nf;
+  bf::note_launch();
+  k_pgrid_prefilter<<<blocks_for(nseq * nm2), 256, 0, st>>>(G->coef.as<double2>(), G->thomas.as<double>(), (int)nseq,
+                                                           (int)nm2, nsp);
+  TCK(cudaGetLastError());
+  TCK(cudaStreamSynchronize(st));
+  *out = G.release();
+  return BF_OK;
+}
+
+extern "C" int bf_pgrid_destroy(bf_handle* h, bf_pgrid* g) {
+  if (!h || !g) return BF_ERR_INVALID;
+  cudaStreamSynchronize(h->stream());
+  delete g;
+  return BF_OK;
+}
+
+// Interpolated matrices into a device buffer [nf][nd][nm][nm] (row-major).
+static int pgrid_eval(bf_handle* h, bf_pgrid* G, const double* dist_shift, DBuf& P) {
+  std::vector<double> x(G->nd, 0.0);
+  const double lo = G->s0, hi = G->s0 + (G->nsp - 1) * G->ds;
+  for (int j = 0; j < G->nd; ++j) {
+    if (G->gap_of[j] < 0) continue;
+    // the last region keeps shift 0, as interpolate_prop_matrix does (utilities :84)
+    const double sh = (j == G->nd - 1) ? 0.0 : dist_shift[(j - 1) / 2];
+    if (!std::isfinite(sh) || sh < lo - 1e-12 * G->ds || sh > hi + 1e-12 * G->ds)
+      return bf_fail(h, BF_ERR_INVALID, "pgrid: a shift lies outside the spacing grid [" + std::to_string(lo) +
+                                            ", " + std::to_string(hi) + "]");
+    x[j] = std::min(std::max(1.0 + (sh - G->s0) / G->ds, 1.0), (double)G->nsp);
+  }
+  cudaStream_t st = h->stream();
+  const size_t nm2 = (size_t)G->nm * G->nm, n = (size_t)G->nf * G->nd * nm2;
+  DBuf dx;
+  TCKS(dx.alloc(h, sizeof(double) * G->nd));
+  TCK(cudaMemcpyAsync(dx.p, x.data(), sizeof(double) * G->nd, cudaMemcpyHostToDevice, st));
+  TCKS(P.ensure(h, sizeof(double2) * n));
+  bf::note_launch();
+  k_pgrid_eval<<<blocks_for(n), 256, 0, st>>>(P.as<double2>(), G->solid.as<double2>(), G->coef.as<double2>(),
+                                             G->gap_d.as<int>(), dx.as<double>(), G->nf, G->nd, (int)nm2, G->nsp);
+  TCK(cudaGetLastError());
+  TCK(cudaStreamSynchronize(st));   // x (host) and dx may go once the kernel has read them
+  return BF_OK;
+}
+
+extern "C" int bf_pgrid_matrices(bf_handle* h, bf_pgrid* G, const double* dist_shift, double* out) {
+  if (!h || !G || !dist_shift || !out) return BF_ERR_INVALID;
+  TCK(cudaSetDevice(h->device));
+  DBuf P;
+  TCKS(pgrid_eval(h, G, dist_shift, P));
+  const size_t nm = G->nm, n = (size_t)G->nf * G->nd * nm * nm;
+  std::vector<double2> hp(n);
+  TCK(cudaMemcpy(hp.data(), P.p, sizeof(double2) * n, cudaMemcpyDeviceToHost));
+  cd* o = reinterpret_cast<cd*>(out);
+  for (size_t fj = 0; fj < (size_t)G->nf * G->nd; ++fj)
+    for (size_t r = 0; r < nm; ++r)
+      for (size_t q = 0; q < nm; ++q) {
+        const double2 v = hp[(fj * nm + r) * nm + q];
+        o[fj * nm * nm + r + nm * q] = cd(v.x, v.y);
+      }
+  return BF_OK;
+}
+
+extern "C" int bf_pgrid_transformer(bf_handle* h, bf_pgrid* G, const double* dist_shift, const double* emit,
+                                    double* out_boost, double* out_beta2) {
+  if (!h || !G || !dist_shift || (!out_boost && !out_beta2)) return BF_ERR_INVALID;
+  TCK(cudaSetDevice(h->device));
+  DBuf P;
+  TCKS(pgrid_eval(h, G, dist_shift, P));
+  return tf_run_t<double2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, emit, nullptr, nullptr, 0, out_boost,
+                           nullptr, out_beta2, 1, 0, nullptr, 0, nullptr, nullptr, P.as<double2>());
 }

@@ -288,6 +288,31 @@ int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* m, int nf, co
                               const double* emit, const double* propagation_matrices, int pm_per_freq,
                               double* out);
 
+/* ---- propagation-matrix grid for optimisers -------------------------------- */
+/* calc_propagation_matrices_grid + construct_prop_matrix_interpolation +
+ * interpolate_prop_matrix of examples/transformer_optim_utilities.jl:11-91,
+ * resident on the device.  The gaps are the regions 1, 3, ..., nd-1 (the
+ * reference's ind_gap = 2:2:n_region); at grid point k every gap's distance is
+ * the stack's distance + spacing_first + k spacing_step, k < nsp; the other
+ * regions are computed once.  The grid is interpolated along the spacing with
+ * a natural cubic B-spline (second derivative zero at the end knots, exact at
+ * the knots).  The stack and the modes must outlive the grid. */
+typedef struct bf_pgrid bf_pgrid;
+#define BF_PGRID_MAX_SPACINGS 64
+int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs, int nsp,
+                    double spacing_first, double spacing_step, int prop_kind, int precision, bf_pgrid** out);
+int bf_pgrid_destroy(bf_handle* h, bf_pgrid* g);
+/* Interpolated matrices at dist_shift (one shift per disk: gap region 2d+1
+ * takes dist_shift[d]; the last region takes 0, as interpolate_prop_matrix
+ * does).  out as bf_calc_propagation_matrices: nf x nd Julia (nm, nm) matrices.
+ * A shift outside [spacing_first, last grid spacing] gives BF_ERR_INVALID. */
+int bf_pgrid_matrices(bf_handle* h, bf_pgrid* g, const double* dist_shift, double* out);
+/* The transformer on the interpolated matrices, without leaving the device:
+ * calc_boostfactor_modes (utilities :98-110).  out_boost nf x nm complex and/or
+ * out_beta2 nf; emit nm complex or NULL (the axion-induced modes). */
+int bf_pgrid_transformer(bf_handle* h, bf_pgrid* g, const double* dist_shift, const double* emit,
+                         double* out_boost, double* out_beta2);
+
 /* ---- serving: a request loop over resident stacks ------------------------ */
 /* No counterpart in the reference, whose callers (the optimiser utilities,
  * examples/transformer_optim_utilities.jl:11-144, and @distributed frequency

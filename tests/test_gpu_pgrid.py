@@ -1,0 +1,113 @@
+"""Propagation-matrix grid with interpolation (bf_pgrid_*), the optimiser
+helper of examples/transformer_optim_utilities.jl:11-91.
+
+The interpolation is a natural cubic spline along the gap spacing (second
+derivative zero at the end knots); scipy's CubicSpline(bc_type="natural") is the
+same spline and serves as the check.  Tolerances: FP64 path 1e-10 (knots,
+interpolation against the oracle's grid values), 1e-12 where the same matrices
+go through two GPU paths.
+"""
+import numpy as np
+import pytest
+
+from oracle import bf_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def B():
+    import build as _b
+    _b.build()
+    import bfgb300
+    return bfgb300
+
+
+def rel(a, b):
+    a = np.asarray(a); b = np.asarray(b)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def setup(B):
+    from bfgb300 import workloads as W
+    rng = np.random.default_rng(61)
+    distance, eps, tx, ty = W.booster(2, rng.uniform(7.5e-3, 8.5e-3, 2))
+    tx[2] = 2e-4
+    X = W.symmetric_grid(32)
+    kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=3, Lmax=1, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=3, Lmax=1, diskR=0.15)
+    grid = np.linspace(-3e-4, 3e-4, 7)
+    freqs = np.array([19.6e9, 20.3e9])
+    return kw, cb, co, mb, mo, grid, freqs
+
+
+def shifted(kw, shift_per_disk, last=0.0):
+    d = np.array(kw["distance"], dtype=float)
+    for k, sh in enumerate(shift_per_disk):
+        d[1 + 2 * k] += sh
+    d[-1] += last
+    return dict(kw, distance=d)
+
+
+def test_pgrid_knots_and_spline_vs_oracle(B):
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
+    try:
+        nd = len(kw["distance"])
+        # oracle grid values of every region at every spacing (gaps shifted, the last region included)
+        ref = np.zeros((len(grid), len(freqs), nd, mo.nm, mo.nm), dtype=complex)
+        for k, s in enumerate(grid):
+            sb = O.seed_setup_boundaries(co, **shifted(kw, [s, s], last=s))
+            for f, fr in enumerate(freqs):
+                ref[k, f] = np.array(O.calc_propagation_matrices(sb, co, mo, f=fr))
+        from scipy.interpolate import CubicSpline
+        spl = CubicSpline(grid, ref, axis=0, bc_type="natural")
+        rng = np.random.default_rng(62)
+        for shifts in ([grid[2], grid[5]], [grid[0], grid[-1]], list(rng.uniform(grid[0], grid[-1], 2)),
+                       list(rng.uniform(grid[0], grid[-1], 2))):
+            got = pg.matrices(np.array(shifts))
+            for f in range(len(freqs)):
+                for j in range(1, nd):
+                    if j % 2 == 0:
+                        want = ref[0, f, j]                                   # solids do not move
+                    elif j == nd - 1:
+                        want = spl(0.0)[f, j]                                 # the last region keeps shift 0
+                    else:
+                        want = spl(shifts[(j - 1) // 2])[f, j]
+                    assert rel(got[f, j], want) < 1e-10, (shifts, f, j)
+    finally:
+        pg.close()
+
+
+def test_pgrid_transformer_matches_injected_and_direct(B):
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
+    try:
+        sh = np.array([1.3e-4, -2.2e-4])
+        boost, beta2 = pg.transformer(sh)
+        pm = pg.matrices(sh)
+        for f, fr in enumerate(freqs):
+            inj = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=fr, propagation_matrices=pm[f])
+            assert rel(boost[f], inj) < 1e-12
+            assert abs(beta2[f] - np.sum(np.abs(inj) ** 2)) / np.sum(np.abs(inj) ** 2) < 1e-12
+        # at knots the grid is exact: compare with a direct solve of the moved stack
+        sh = np.array([grid[1], grid[4]])
+        boost, _ = pg.transformer(sh)
+        for f, fr in enumerate(freqs):
+            direct = B.transformer(B.SeedSetupBoundaries(cb, **shifted(kw, sh)), cb, mb, f=fr)
+            assert rel(boost[f], direct) < 1e-10
+    finally:
+        pg.close()
+
+
+def test_pgrid_rejects_shift_outside_grid(B):
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
+    try:
+        with pytest.raises(B.BFError) as e:
+            pg.matrices(np.array([0.0, grid[-1] + 1e-5]))
+        assert e.value.code == 1
+    finally:
+        pg.close()
