@@ -62,6 +62,7 @@ def test_pgrid_knots_and_spline_vs_oracle(B):
             sb = O.seed_setup_boundaries(co, **shifted(kw, [s, s], last=s))
             for f, fr in enumerate(freqs):
                 ref[k, f] = np.array(O.calc_propagation_matrices(sb, co, mo, f=fr))
+        ref[:, :, 0] = 0.0   # the mirror (NaN permittivity, as the reference leaves it) is not compared
         from scipy.interpolate import CubicSpline
         spl = CubicSpline(grid, ref, axis=0, bc_type="natural")
         rng = np.random.default_rng(62)
