@@ -732,7 +732,7 @@ class PGrid:
 
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,
-            "transformer": _lib.BF_SOLVER_TRANSFORMER}
+            "transformer": _lib.BF_SOLVER_TRANSFORMER, "pgrid": _lib.BF_SOLVER_PGRID}
 
 
 class Server:
@@ -759,11 +759,16 @@ class Server:
             raise BFError(rc, msg.decode() if msg else "")
 
     def submit(self, stack, freqs, solver="cheerleader", modes=None, distance=None, nmax=400, prop=None,
-               precision="mixed", beta2_scale=0.0, want_boost=False, footprint_bytes=0):
+               precision="mixed", beta2_scale=0.0, want_boost=False, footprint_bytes=0, pgrid=None):
         """Queue one solve; returns its id.  ``stack`` is a Stack (or, dry-run, any
-        non-zero integer token), ``distance`` the stack's new region distances."""
+        non-zero integer token), ``distance`` the stack's new region distances.
+        solver="pgrid": ``pgrid`` is a PGrid, ``stack`` may be None (the grid's),
+        ``freqs`` the grid's frequencies and ``distance`` the per-disk shifts."""
+        if pgrid is not None:
+            stack = pgrid.stack if stack is None else stack
+            modes = None
         fr = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
-        nm = modes.nm if modes is not None else 0
+        nm = pgrid.nm if pgrid is not None else (modes.nm if modes is not None else 0)
         b2 = np.empty(len(fr))
         boost = np.empty((len(fr), nm), dtype=np.complex128) if want_boost and nm else None
         dist = None if distance is None else np.ascontiguousarray(distance, dtype=np.float64)
@@ -781,6 +786,7 @@ class Server:
         q.out_beta2 = _lib.ptr(b2)
         q.out_boost = _lib.ptr(None if boost is None else boost.view(np.float64))
         q.footprint_bytes = int(footprint_bytes)
+        q.pgrid = pgrid._g if pgrid is not None else None
         rid = _lib._ull()
         self._check(_lib.lib().bf_submit(self._p, ctypes.byref(q), ctypes.byref(rid)))
         self._live[rid.value] = (q, fr, dist, b2, boost)

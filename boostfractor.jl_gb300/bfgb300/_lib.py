@@ -39,6 +39,7 @@ _ull = ctypes.c_ulonglong
 BF_SOLVER_CHEERLEADER = 0
 BF_SOLVER_DANCER = 1
 BF_SOLVER_TRANSFORMER = 2
+BF_SOLVER_PGRID = 3
 BF_PENDING = -1
 BF_SERVER_DRYRUN = 1
 
@@ -48,7 +49,7 @@ class BFRequest(ctypes.Structure):
     _fields_ = [("solver", _c_int), ("stack", _vp), ("modes", _vp), ("nf", _c_int), ("freqs", _p_dbl),
                 ("distance", _p_dbl), ("nmax", _c_int), ("prop_kind", _c_int), ("precision", _c_int),
                 ("beta2_scale", _c_dbl), ("out_beta2", _p_dbl), ("out_boost", _p_dbl),
-                ("footprint_bytes", _ull)]
+                ("footprint_bytes", _ull), ("pgrid", _vp)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/boostfractor_gb300.h

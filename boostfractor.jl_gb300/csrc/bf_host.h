@@ -127,6 +127,8 @@ void bf_stack_trim(bf_stack* s);
 // Upper bound of the device bytes one solve adds to a stack (workspace,
 // per-call buffers, outputs): solver 0 cheerleader, 1 dancer, 2 transformer
 // with nm modes.
+// Frequencies, regions, modes and stack of a propagation-matrix grid.
+void bf_pgrid_shape(const bf_pgrid* g, int* nf, int* nd, int* nm, bf_stack** stack);
 size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, int prop_kind, int precision);
 
 namespace bfhost {

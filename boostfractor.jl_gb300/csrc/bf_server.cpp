@@ -83,9 +83,9 @@ struct bf_server {
   std::string err;
   Clock::time_point t0;
   // statistics (per solver)
-  std::vector<double> lat[3];
-  double fpts[3] = {0, 0, 0};
-  unsigned long long failed[3] = {0, 0, 0}, batched[3] = {0, 0, 0};
+  std::vector<double> lat[4];
+  double fpts[4] = {0, 0, 0, 0};
+  unsigned long long failed[4] = {0, 0, 0, 0}, batched[4] = {0, 0, 0, 0};
   unsigned long long evictions = 0;
   double t_first = -1.0, t_last = 0.0;
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
@@ -183,14 +183,20 @@ int run_batch(bf_server* S, int w, Batch& b, std::string& err) {
   bf_handle* h = S->hs[w];
   bf_stack* st = R0->r.stack;
   int rc = BF_OK;
-  if (!R0->distance.empty()) rc = bf_stack_set_distance(h, st, R0->distance.data());
+  // an optimiser step moves the disks; a grid step only selects the interpolation point
+  if (!R0->distance.empty() && R0->r.solver != BF_SOLVER_PGRID) rc = bf_stack_set_distance(h, st, R0->distance.data());
   if (rc != BF_OK) { err = h->err; return rc; }
   std::vector<double> freqs;
   for (Req* R : b.reqs) freqs.insert(freqs.end(), R->freqs.begin(), R->freqs.end());
   const int nf = (int)freqs.size();
   std::vector<double> b2(nf, 0.0);
   const bf_request& q = R0->r;
-  if (q.solver == BF_SOLVER_TRANSFORMER) {
+  if (q.solver == BF_SOLVER_PGRID) {
+    std::vector<double> boost(q.out_boost ? (size_t)nf * R0->nm * 2 : 0);
+    rc = bf_pgrid_transformer(h, q.pgrid, R0->distance.data(), nullptr, q.out_boost ? boost.data() : nullptr,
+                              b2.data());
+    if (rc == BF_OK && q.out_boost) std::memcpy(q.out_boost, boost.data(), sizeof(double) * boost.size());
+  } else if (q.solver == BF_SOLVER_TRANSFORMER) {
     bool want = false;
     for (Req* R : b.reqs) want |= R->r.out_boost != nullptr;
     std::vector<double> boost(want ? (size_t)nf * R0->nm * 2 : 0);
@@ -363,7 +369,7 @@ extern "C" int bf_server_destroy(bf_server* S) {
 extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* id) {
   if (!S || !q || !id) return BF_ERR_INVALID;
   *id = 0;
-  if (q->solver < BF_SOLVER_CHEERLEADER || q->solver > BF_SOLVER_TRANSFORMER)
+  if (q->solver < BF_SOLVER_CHEERLEADER || q->solver > BF_SOLVER_PGRID)
     return server_fail(S, BF_ERR_INVALID, "unknown solver");
   if (!q->stack || q->nf < 1 || !q->freqs || !q->out_beta2)
     return server_fail(S, BF_ERR_INVALID, "request needs a stack, frequencies and out_beta2");
@@ -373,7 +379,9 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
       return server_fail(S, BF_ERR_INVALID, "frequencies must be finite and positive");
   if (q->solver == BF_SOLVER_TRANSFORMER && !q->modes)
     return server_fail(S, BF_ERR_INVALID, "a transformer request needs a mode basis");
-  if (q->solver != BF_SOLVER_TRANSFORMER && q->nmax < 0) return server_fail(S, BF_ERR_INVALID, "nmax < 0");
+  if (q->solver < BF_SOLVER_TRANSFORMER && q->nmax < 0) return server_fail(S, BF_ERR_INVALID, "nmax < 0");
+  if (q->solver == BF_SOLVER_PGRID && (!q->pgrid || !q->distance))
+    return server_fail(S, BF_ERR_INVALID, "a grid request needs the grid and the per-disk shifts (distance)");
   if (q->precision != BF_PREC_FP64 && q->precision != BF_PREC_MIXED)
     return server_fail(S, BF_ERR_INVALID, "unknown precision");
   if (S->dry() && !q->footprint_bytes)
@@ -381,7 +389,25 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
   Req* R = new Req();
   R->r = *q;
   R->freqs.assign(q->freqs, q->freqs + q->nf);
-  if (!S->dry()) {
+  if (!S->dry() && q->solver == BF_SOLVER_PGRID) {
+    int gnf = 0, gnd = 0, gnm = 0;
+    bf_stack* gs = nullptr;
+    bf_pgrid_shape(q->pgrid, &gnf, &gnd, &gnm, &gs);
+    if (gnf != q->nf) {
+      delete R;
+      return server_fail(S, BF_ERR_INVALID, "a grid request's frequencies must be the grid's");
+    }
+    R->r.stack = gs;   // requests on one grid run one at a time, like those on one stack
+    R->nm = gnm;
+    R->distance.assign(q->distance, q->distance + (gnd - 2) / 2);
+    for (double d : R->distance)
+      if (!std::isfinite(d)) {
+        delete R;
+        return server_fail(S, BF_ERR_INVALID, "non-finite shift");
+      }
+    R->est = q->footprint_bytes ? (size_t)q->footprint_bytes
+                                : (size_t)gnf * gnd * gnm * gnm * 16 * 6 + (size_t)gnf * gnm * 64 + 4096;
+  } else if (!S->dry()) {
     if (q->distance) {
       R->distance.assign(q->distance, q->distance + q->stack->nd);
       for (double d : R->distance)
@@ -446,11 +472,11 @@ extern "C" int bf_wait(bf_server* S, unsigned long long id, int timeout_ms, int*
 }
 
 extern "C" int bf_server_stats(bf_server* S, int solver, double* out) {
-  if (!S || !out || solver < -1 || solver > 2) return BF_ERR_INVALID;
+  if (!S || !out || solver < -1 || solver > 3) return BF_ERR_INVALID;
   std::lock_guard<std::mutex> lock(S->mu);
   std::vector<double> lat;
   double fp = 0, nf_ = 0, nb = 0;
-  for (int k = 0; k < 3; ++k)
+  for (int k = 0; k < 4; ++k)
     if (solver < 0 || solver == k) {
       lat.insert(lat.end(), S->lat[k].begin(), S->lat[k].end());
       fp += S->fpts[k];

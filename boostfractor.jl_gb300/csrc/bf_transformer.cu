@@ -1920,6 +1920,8 @@ struct bf_pgrid {
   std::vector<int> gap_of;   // region -> gap slot, or -1
   DBuf gap_d, solid, coef;   // gap_of on the device; solids [nf][nd][nm^2]; [ngap][nf][nsp + 2][nm^2]
   DBuf thomas;               // 1/(4 - c'_{k-1}) and c'_k of the spline system, 2 (nsp + 2) doubles
+  int precision = BF_PREC_FP64;
+  std::vector<cd> emit;      // the default emission (axion-induced modes), computed once
 };
 
 namespace {
@@ -2075,8 +2077,11 @@ extern "C" int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* md, int nf, 
   }
   TCKS(G->thomas.alloc(h, sizeof(double) * th.size()));
   TCK(cudaMemcpyAsync(G->thomas.p, th.data(), sizeof(double) * th.size(), cudaMemcpyHostToDevice, st));
+  G->precision = precision;
   if (precision == BF_PREC_FP64) TCKS(pgrid_fill<double2>(h, G.get(), prop_kind, 0));
   else TCKS(pgrid_fill<float2>(h, G.get(), prop_kind, 1));
+  G->emit.resize(G->nm);
+  TCKS(bf_axion_induced_modes(h, md, nullptr, 0.0, s->diskR, 10e9, reinterpret_cast<double*>(G->emit.data())));
   const size_t nseq = (size_t)G->ngap * nf;
   bf::note_launch();
   k_pgrid_prefilter<<<blocks_for(nseq * nm2), 256, 0, st>>>(G->coef.as<double2>(), G->thomas.as<double>(), (int)nseq,
@@ -2085,6 +2090,13 @@ extern "C" int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* md, int nf, 
   TCK(cudaStreamSynchronize(st));
   *out = G.release();
   return BF_OK;
+}
+
+void bf_pgrid_shape(const bf_pgrid* g, int* nf, int* nd, int* nm, bf_stack** stack) {
+  *nf = g->nf;
+  *nd = g->nd;
+  *nm = g->nm;
+  *stack = g->s;
 }
 
 extern "C" int bf_pgrid_destroy(bf_handle* h, bf_pgrid* g) {
@@ -2145,6 +2157,15 @@ extern "C" int bf_pgrid_transformer(bf_handle* h, bf_pgrid* G, const double* dis
   TCK(cudaSetDevice(h->device));
   DBuf P;
   TCKS(pgrid_eval(h, G, dist_shift, P));
-  return tf_run_t<double2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, emit, nullptr, nullptr, 0, out_boost,
-                           nullptr, out_beta2, 1, 0, nullptr, 0, nullptr, nullptr, P.as<double2>());
+  const double* em = emit ? emit : reinterpret_cast<const double*>(G->emit.data());
+  if (G->precision == BF_PREC_FP64)
+    return tf_run_t<double2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, em, nullptr, nullptr, 0,
+                             out_boost, nullptr, out_beta2, 1, 0, nullptr, 0, nullptr, nullptr, P.as<double2>());
+  // mixed grid: complex64 matrices, double-float chain, FP64 boundary solve
+  const size_t n = (size_t)G->nf * G->nd * G->nm * G->nm;
+  DBuf P32;
+  TCKS(P32.alloc(h, sizeof(float2) * n));
+  if (bf::launch_convert(P.p, true, P32.p, false, n, h->stream())) return bf_fail(h, BF_ERR_CUDA, "convert");
+  return tf_run_t<float2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, em, nullptr, nullptr, 0, out_boost,
+                          nullptr, out_beta2, 1, 0, nullptr, 1, nullptr, nullptr, P32.as<float2>());
 }

@@ -339,6 +339,8 @@ typedef struct bf_server bf_server;
 #define BF_SOLVER_CHEERLEADER 0
 #define BF_SOLVER_DANCER      1
 #define BF_SOLVER_TRANSFORMER 2
+#define BF_SOLVER_PGRID       3  /* bf_pgrid_transformer at the per-disk shifts in `distance`
+                                    (the grid's frequencies; `freqs` must match them) */
 
 #define BF_PENDING (-1)          /* request status: queued or running */
 #define BF_SERVER_DRYRUN 1       /* schedule without device work: a request
@@ -361,6 +363,7 @@ typedef struct bf_request {
   double* out_beta2;           /* host, nf doubles, written before completion is reported */
   double* out_boost;           /* transformer: host nf x nm complex, or NULL */
   unsigned long long footprint_bytes;  /* 0 = the server's estimate */
+  bf_pgrid* pgrid;             /* BF_SOLVER_PGRID: the grid (its stack is `stack`); else NULL */
 } bf_request;
 
 int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_workers, int flags,

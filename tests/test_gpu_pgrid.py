@@ -112,3 +112,45 @@ def test_pgrid_rejects_shift_outside_grid(B):
         assert e.value.code == 1
     finally:
         pg.close()
+
+
+def test_pgrid_mixed_within_bar(B):
+    """A grid built at BF_PREC_MIXED (complex64 matrices, double-float chain)
+    gives beta^2 within 1e-4 of the FP64 grid at the same shifts."""
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    p64 = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
+    p32 = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid, precision="mixed")
+    try:
+        for sh in (np.array([1.3e-4, -2.2e-4]), np.array([grid[3], grid[6]])):
+            _, b64 = p64.transformer(sh)
+            _, b32 = p32.transformer(sh)
+            assert np.max(np.abs(b32 - b64) / b64) < 1e-4
+    finally:
+        p64.close()
+        p32.close()
+
+
+def test_pgrid_requests_through_the_server(B):
+    """Grid steps queued on the serving engine (solver "pgrid", the shifts in
+    distance) run in submission order and equal PGrid.transformer."""
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid, precision="mixed")
+    try:
+        rng = np.random.default_rng(31)
+        shifts = [rng.uniform(grid[0], grid[-1], 2) for _ in range(5)]
+        ref = [pg.transformer(sh) for sh in shifts]
+        srv = B.Server(n_workers=2)
+        try:
+            ids = [srv.submit(None, freqs, "pgrid", distance=sh, pgrid=pg, want_boost=True) for sh in shifts]
+            res = [srv.wait(i, timeout_ms=120000) for i in ids]
+            for r, (bo, b2) in zip(res, ref):
+                assert np.max(np.abs(r["beta2"] - b2) / np.abs(b2)) < 1e-12
+                assert rel(r["boost"], bo) < 1e-12
+            for a, b in zip(res, res[1:]):
+                assert b["t_start"] >= a["t_done"]
+            with pytest.raises(B.BFError):
+                srv.submit(None, freqs[:1], "pgrid", distance=shifts[0], pgrid=pg)
+        finally:
+            srv.close()
+    finally:
+        pg.close()
