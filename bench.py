@@ -629,6 +629,87 @@ def run_serve(args, optimiser_class=False):
          "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
 
 
+def run_serve_pgrid(args):
+    """Serving loop on propagation-matrix grids: 32 optimiser clients, each
+    with its own resident grid (20 disks, 256 frequencies, 8 Laguerre-Gauss
+    modes, 128x128 over 1 m, 9 spacings from -200 um to +200 um, built at
+    mixed precision).  Every step random-walks the per-disk shifts by
+    N(0, 10 um) inside the grid, submits a "pgrid" request, waits for beta^2
+    and thinks for an exponential time of mean 32/2000 s.  This is the
+    interpolated-matrix optimiser loop: a step solves the stack at the
+    interpolated matrices instead of recomputing them."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    nclients, n, nf, ndisk, M = 32, 128, 256, 20, 8
+    sgrid = np.linspace(-2e-4, 2e-4, 9)
+    freqs = np.linspace(19.5e9, 20.5e9, nf)
+    h = B.Handle(0)
+    X = W.symmetric_grid(n)
+    c = B.SeedCoordinateSystem(X=X, Y=X)
+    pats, kt = W.lg_modes(c.X, c.Y, M, 0.03, 0.15)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=M, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt, handle=h)
+    grids = []
+    t0 = time.perf_counter()
+    for k in range(nclients):
+        rng = np.random.default_rng(500 + k)
+        distance, eps, tx, ty = W.booster(ndisk, rng.uniform(7.5e-3, 8.5e-3, ndisk))
+        sb = B.SeedSetupBoundaries(c, diskno=ndisk, distance=distance, epsilon=eps, relative_tilt_x=tx,
+                                   relative_tilt_y=ty)
+        grids.append(B.PGrid(sb, c, modes, freqs, sgrid, precision="mixed"))
+    t_create = (time.perf_counter() - t0) / nclients
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    for g in grids:   # one warm-up step per client, untimed
+        srv.wait(srv.submit(None, freqs, "pgrid", distance=np.zeros(ndisk), pgrid=g))
+    srv.close()
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    deadline = time.perf_counter() + args.serve_seconds
+    errors = []
+    lo, hi = sgrid[0], sgrid[-1]
+
+    def client(k):
+        rng = np.random.default_rng(1000 + k)
+        sh = np.zeros(ndisk)
+        try:
+            while time.perf_counter() < deadline:
+                sh = np.clip(sh + rng.normal(0.0, 10e-6, ndisk), lo, hi)
+                srv.wait(srv.submit(None, freqs, "pgrid", distance=sh, pgrid=grids[k]))
+                time.sleep(rng.exponential(nclients / 2000.0))
+        except Exception as e:  # reported in the JSON line
+            errors.append(repr(e))
+
+    clock = ClockSampler(0)
+    clock.start()
+    t0 = time.perf_counter()
+    threads = [threading.Thread(target=client, args=(k,)) for k in range(nclients)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    wall = time.perf_counter() - t0
+    clocks = clock.stop()
+    st_all = srv.stats()
+    srv.close()
+    for g in grids:
+        g.close()
+    modes.close()
+    h.close()
+    _server_line(
+        "beta2 freq-points/s and p50/p99 latency, 32 optimiser clients, interpolated propagation-matrix grids "
+        "(20 disks, 256 freqs, 8 LG modes, 128x128)", st_all["freq_points"] / wall, st_all["completed"], wall,
+        {"config": {"workload": "serve-pgrid-optimiser-class", "clients": nclients, "disks": ndisk, "freqs": nf,
+                    "modes": M, "grid": n, "spacings": len(sgrid), "spacing_range_um": [-200, 200],
+                    "think_mean_ms": 1000.0 * nclients / 2000.0, "seconds": args.serve_seconds,
+                    "workers": args.workers, "gap_step_um": 10, "precision": "mixed"},
+         "latency_ms": {"p50": st_all["p50_ms"], "p99": st_all["p99_ms"], "mean": st_all["mean_ms"],
+                        "max": st_all["max_ms"]},
+         "requests_per_s": st_all["completed"] / wall, "grid_create_s_per_client": t_create,
+         "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
+
+
 def run_1d(args):
     """Batched 1D model: 4096 spacing configurations of the 20-disk booster
     (each gap moved by N(0, 10 um) from the seeded geometry) x 256 frequencies
@@ -741,7 +822,7 @@ def main():
     ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cheerleader",
-                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "1d"])
+                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
@@ -752,6 +833,8 @@ def main():
         run_uneven(args)
     elif args.workload == "1d" and args.impl == "ours":
         run_1d(args)
+    elif args.workload == "serve-pgrid" and args.impl == "ours":
+        run_serve_pgrid(args)
     elif args.workload in ("serve", "serve-opt") and args.impl == "ours":
         run_serve(args, optimiser_class=args.workload == "serve-opt")
     elif args.impl == "reference":
