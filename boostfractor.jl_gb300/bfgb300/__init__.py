@@ -698,6 +698,8 @@ class PGrid:
         self.freqs = np.ascontiguousarray(np.atleast_1d(frequencies), dtype=np.float64)
         self.stack = Stack(bdry, coords, diskR, handle=self.h)
         self.nd, self.nm = self.stack.nd, modes.nm
+        self.spacing_first, self.spacing_step = float(sg[0]), float(sg[1] - sg[0])
+        self.spacing_last = self.spacing_first + (len(sg) - 1) * self.spacing_step
         g = _lib._vp()
         self.h.check(_lib.lib().bf_pgrid_create(self.h.ptr, self.stack._s, modes._m, len(self.freqs),
                                                 _lib.ptr(self.freqs), len(sg), float(sg[0]), float(sg[1] - sg[0]),
@@ -722,6 +724,23 @@ class PGrid:
                                                      _lib.ptr(boost.view(np.float64)), _lib.ptr(beta2)))
         return boost, beta2
 
+    @property
+    def bounds(self):
+        """The spacing axis' bounds, Interpolations.bounds(itp)[3] of the
+        reference's OnCell interpolation: half a step beyond the end spacings."""
+        return (self.spacing_first - 0.5 * self.spacing_step, self.spacing_last + 0.5 * self.spacing_step)
+
+    def cost(self, dist_shift, m_reflect, p=-20.0):
+        """calc_boostfactor_cost (utilities :130-144): (cost, coupled power per
+        frequency, or None on the hard out-of-bounds penalty)."""
+        sh = np.ascontiguousarray(dist_shift, dtype=np.float64)
+        mr = np.ascontiguousarray(m_reflect, dtype=np.complex128).reshape(self.nm)
+        c = np.zeros(1)
+        cpl = np.full(len(self.freqs), np.nan)
+        self.h.check(_lib.lib().bf_pgrid_cost(self.h.ptr, self._g, _lib.ptr(sh), _lib.ptr(mr.view(np.float64)),
+                                              float(p), _lib.ptr(c), _lib.ptr(cpl)))
+        return float(c[0]), (None if np.isnan(cpl).all() else cpl)
+
     def close(self):
         if getattr(self, "_g", None) and self.h._h:
             _lib.lib().bf_pgrid_destroy(self.h.ptr, self._g)
@@ -733,6 +752,49 @@ class PGrid:
 
 _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_DANCER,
             "transformer": _lib.BF_SOLVER_TRANSFORMER, "pgrid": _lib.BF_SOLVER_PGRID}
+
+
+def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, prop=propagator, diskR=0.15,
+                                   precision="fp64"):
+    """examples/transformer_optim_utilities.jl:10-50 (without tilt grids): the
+    grid of propagation matrices over gap spacings x frequencies, kept on the
+    device as a PGrid instead of a 7-D host array."""
+    return PGrid(sbdry, coords, modes, frequencies, spacing_grid, prop=prop, diskR=diskR, precision=precision)
+
+
+def construct_prop_matrix_interpolation(prop_matrix_grid, spacing_grid=None):
+    """utilities :56-73.  The PGrid is prefiltered for its cubic B-spline when it
+    is built, so it is its own interpolation object."""
+    if not isinstance(prop_matrix_grid, PGrid):
+        raise TypeError("expects the PGrid of calc_propagation_matrices_grid")
+    return prop_matrix_grid
+
+
+def interpolate_prop_matrix(itp, dist_shift):
+    """utilities :78-91: [region, frequency, nm, nm] matrices at the shifts."""
+    return itp.matrices(dist_shift).transpose(1, 0, 2, 3).copy()
+
+
+def calc_boostfactor_modes(sbdry, coords, modes, frequencies, prop_matrices_set, prop=propagator, diskR=0.15,
+                           precision="fp64"):
+    """utilities :99-110: EoutModes0[1, mode, frequency] of the transformer on
+    per-frequency matrices prop_matrices_set[region, frequency] (one batched
+    solve)."""
+    pm = np.asarray(prop_matrices_set, dtype=np.complex128)
+    fr = np.atleast_1d(np.asarray(frequencies, dtype=np.float64))
+    boost = transformer(sbdry, coords, modes, f=fr, prop=prop, diskR=diskR,
+                        propagation_matrices=pm.transpose(1, 0, 2, 3), precision=precision)
+    return np.asarray(boost).T[None, :, :]
+
+
+def calc_boostfactor_cost(dist_shift, itp, frequencies, sbdry, coords, modes, m_reflect, prop=propagator, diskR=0.15):
+    """utilities :130-144 on the device: -p_norm(coupled power, -20) x the soft
+    box penalty, 1000.0 outside the interpolation bounds.  sbdry, coords, modes,
+    prop and diskR are those the grid was built with."""
+    fr = np.atleast_1d(np.asarray(frequencies, dtype=np.float64))
+    if fr.shape != itp.freqs.shape or np.any(fr != itp.freqs):
+        raise ValueError("frequencies must be the grid's")
+    return itp.cost(dist_shift, m_reflect, p=-20.0)[0]
 
 
 class Server:

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstring>
 #include <complex>
 #include <map>
 #include <memory>
@@ -1943,11 +1944,18 @@ __global__ void k_pgrid_gather(double2* coef, double2* solid, const PT* P, const
     solid[i] = v;
 }
 
-// Natural cubic B-spline prefilter along the spacing axis, in place.  Data
-// y_1..y_n sit at coef[1..n]; the coefficients satisfy (c_{k-1} + 4 c_k +
-// c_{k+1}) / 6 = y_k and S'' = 0 at both end knots, so c_1 = y_1, c_n = y_n,
-// c_0 = 2 c_1 - c_2, c_{n+1} = 2 c_n - c_{n-1}; the interior is a constant
-// tridiagonal system solved with the host-computed Thomas factors.
+// Cubic B-spline prefilter along the spacing axis, in place, with the
+// boundary conditions of Interpolations.jl's Cubic(Natural(OnCell())): the
+// spline interpolates y_1..y_n at the knots 1..n, (c_{k-1} + 4 c_k + c_{k+1})
+// / 6 = y_k, and its second derivative vanishes at the cell edges 1/2 and
+// n + 1/2, half a step outside the end knots.  With the end segments'
+// polynomials extended there, S''(1/2) = 0 reads 3 c_0 - 7 c_1 + 5 c_2 - c_3
+// = 0; eliminating c_0 and c_3 with the first two knot rows leaves
+//   3 c_1 - c_2 = 3 y_1 - y_2,   c_{k-1} + 4 c_k + c_{k+1} = 6 y_k (k = 2..n-1),
+//   -c_{n-1} + 3 c_n = 3 y_n - y_{n-1}
+// (tridiagonal, diagonally dominant), then c_0 = 6 y_1 - 4 c_1 - c_2 and
+// c_{n+1} = 6 y_n - 4 c_n - c_{n-1}.  Data y_k sit at coef[k]; the host
+// supplies the Thomas factors 1/m_k and c'_k of this constant matrix.
 __global__ void k_pgrid_prefilter(double2* coef, const double* thomas, int nseq_outer, int nm2, int nsp) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= (size_t)nseq_outer * nm2) return;
@@ -1955,31 +1963,39 @@ __global__ void k_pgrid_prefilter(double2* coef, const double* thomas, int nseq_
   double2* c = coef + (i / nm2) * (size_t)(nsp + 2) * nm2 + e;
   const int n = nsp;
   auto at = [&](int k) -> double2& { return c[(size_t)k * nm2]; };
-  if (n >= 3) {
-    const double* den = thomas;            // den[k] = 1 / (4 - c'_{k-1}), k = 2..n-1
-    const double* cpr = thomas + (n + 2);  // c'_k, k = 2..n-1
-    const double2 y1 = at(1), yn = at(n);
-    // forward sweep: d'_k = (r_k - d'_{k-1}) den_k, with r_k = 6 y_k (minus the known ends)
-    double2 prev = make_double2(0.0, 0.0);
-    for (int k = 2; k <= n - 1; ++k) {
-      double2 r = make_double2(6.0 * at(k).x, 6.0 * at(k).y);
-      if (k == 2) r = bf::csub(r, y1);
-      if (k == n - 1) r = bf::csub(r, yn);
-      const double2 d = make_double2((r.x - prev.x) * den[k], (r.y - prev.y) * den[k]);
-      at(k) = d;
-      prev = d;
+  const double* inv_m = thomas;          // 1 / m_k, k = 1..n
+  const double* cpr = thomas + (n + 2);  // c'_k, k = 1..n-1
+  const double2 y1 = at(1), y2 = at(2), yn = at(n), yn1 = at(n - 1);
+  // forward sweep: d'_k = (r_k - a_k d'_{k-1}) / m_k; sub-diagonal a_k = 1 inside, -1 in row n
+  double2 prev = make_double2(0.0, 0.0);
+  for (int k = 1; k <= n; ++k) {
+    double2 r;
+    double a;
+    if (k == 1) {
+      r = make_double2(3.0 * y1.x - y2.x, 3.0 * y1.y - y2.y);
+      a = 0.0;
+    } else if (k == n) {
+      r = make_double2(3.0 * yn.x - yn1.x, 3.0 * yn.y - yn1.y);
+      a = -1.0;
+    } else {
+      r = make_double2(6.0 * at(k).x, 6.0 * at(k).y);
+      a = 1.0;
     }
-    for (int k = n - 2; k >= 2; --k) {
-      const double2 nx = at(k + 1);
-      at(k) = make_double2(at(k).x - cpr[k] * nx.x, at(k).y - cpr[k] * nx.y);
-    }
+    const double2 d = make_double2((r.x - a * prev.x) * inv_m[k], (r.y - a * prev.y) * inv_m[k]);
+    at(k) = d;
+    prev = d;
   }
-  at(0) = make_double2(2.0 * at(1).x - at(2).x, 2.0 * at(1).y - at(2).y);
-  at(n + 1) = make_double2(2.0 * at(n).x - at(n - 1).x, 2.0 * at(n).y - at(n - 1).y);
+  for (int k = n - 1; k >= 1; --k) {
+    const double2 nx = at(k + 1);
+    at(k) = make_double2(at(k).x - cpr[k] * nx.x, at(k).y - cpr[k] * nx.y);
+  }
+  at(0) = make_double2(6.0 * y1.x - 4.0 * at(1).x - at(2).x, 6.0 * y1.y - 4.0 * at(1).y - at(2).y);
+  at(n + 1) = make_double2(6.0 * yn.x - 4.0 * at(n).x - at(n - 1).x, 6.0 * yn.y - 4.0 * at(n).y - at(n - 1).y);
 }
 
-// P[f][j][e] at the gap positions x[j] (data coordinates 1..n): uniform cubic
-// B-spline weights on c_{i-1..i+2}, i = floor(x) (n - 1 at the last knot)
+// P[f][j][e] at the gap positions x[j] (data coordinates 1/2..n+1/2): uniform
+// cubic B-spline weights on c_{i-1..i+2}, i = floor(x) clamped to 1..n-1, so
+// the end segments' polynomials cover the half cells beyond the end knots
 __global__ void k_pgrid_eval(double2* P, const double2* solid, const double2* coef, const int* gap_of,
                              const double* xpos, int nf, int nd, int nm2, int nsp) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -2066,13 +2082,17 @@ extern "C" int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* md, int nf, 
   TCK(cudaMemcpyAsync(G->gap_d.p, G->gap_of.data(), sizeof(int) * s->nd, cudaMemcpyHostToDevice, st));
   TCKS(G->solid.alloc(h, sizeof(double2) * nf * s->nd * nm2));
   TCKS(G->coef.alloc(h, sizeof(double2) * (size_t)G->ngap * nf * (nsp + 2) * nm2));
-  // Thomas factors of the interior system (1, 4, 1), unknowns c_2 .. c_{n-1}
+  // Thomas factors of the prefilter matrix (k_pgrid_prefilter): rows
+  // (3, -1), (1, 4, 1) ..., (-1, 3); m_k = b_k - a_k c'_{k-1}, c'_k = u_k / m_k
   std::vector<double> th(2 * (nsp + 2), 0.0);
   double cp = 0.0;
-  for (int k = 2; k <= nsp - 1; ++k) {
-    const double den = 1.0 / (4.0 - (k == 2 ? 0.0 : cp));
-    th[k] = den;
-    cp = den;   // c'_k = 1 / (4 - c'_{k-1}) (the superdiagonal is 1)
+  for (int k = 1; k <= nsp; ++k) {
+    const double a = (k == 1) ? 0.0 : (k == nsp ? -1.0 : 1.0);
+    const double b = (k == 1 || k == nsp) ? 3.0 : 4.0;
+    const double u = (k == 1) ? -1.0 : (k == nsp ? 0.0 : 1.0);
+    const double m = b - a * cp;
+    th[k] = 1.0 / m;
+    cp = u / m;
     th[(nsp + 2) + k] = cp;
   }
   TCKS(G->thomas.alloc(h, sizeof(double) * th.size()));
@@ -2109,7 +2129,8 @@ extern "C" int bf_pgrid_destroy(bf_handle* h, bf_pgrid* g) {
 // Interpolated matrices into a device buffer [nf][nd][nm][nm] (row-major).
 static int pgrid_eval(bf_handle* h, bf_pgrid* G, const double* dist_shift, DBuf& P) {
   std::vector<double> x(G->nd, 0.0);
-  const double lo = G->s0, hi = G->s0 + (G->nsp - 1) * G->ds;
+  // the domain of an OnCell interpolation: half a step beyond the first and last spacing
+  const double lo = G->s0 - 0.5 * G->ds, hi = G->s0 + (G->nsp - 0.5) * G->ds;
   for (int j = 0; j < G->nd; ++j) {
     if (G->gap_of[j] < 0) continue;
     // the last region keeps shift 0, as interpolate_prop_matrix does (utilities :84)
@@ -2117,7 +2138,7 @@ static int pgrid_eval(bf_handle* h, bf_pgrid* G, const double* dist_shift, DBuf&
     if (!std::isfinite(sh) || sh < lo - 1e-12 * G->ds || sh > hi + 1e-12 * G->ds)
       return bf_fail(h, BF_ERR_INVALID, "pgrid: a shift lies outside the spacing grid [" + std::to_string(lo) +
                                             ", " + std::to_string(hi) + "]");
-    x[j] = std::min(std::max(1.0 + (sh - G->s0) / G->ds, 1.0), (double)G->nsp);
+    x[j] = std::min(std::max(1.0 + (sh - G->s0) / G->ds, 0.5), G->nsp + 0.5);
   }
   cudaStream_t st = h->stream();
   const size_t nm2 = (size_t)G->nm * G->nm, n = (size_t)G->nf * G->nd * nm2;
@@ -2151,21 +2172,74 @@ extern "C" int bf_pgrid_matrices(bf_handle* h, bf_pgrid* G, const double* dist_s
   return BF_OK;
 }
 
-extern "C" int bf_pgrid_transformer(bf_handle* h, bf_pgrid* G, const double* dist_shift, const double* emit,
-                                    double* out_boost, double* out_beta2) {
-  if (!h || !G || !dist_shift || (!out_boost && !out_beta2)) return BF_ERR_INVALID;
-  TCK(cudaSetDevice(h->device));
+static int pgrid_solve(bf_handle* h, bf_pgrid* G, const double* dist_shift, const double* emit, double* out_boost,
+                       double* out_beta2, const CoupleArgs* cp) {
   DBuf P;
   TCKS(pgrid_eval(h, G, dist_shift, P));
   const double* em = emit ? emit : reinterpret_cast<const double*>(G->emit.data());
   if (G->precision == BF_PREC_FP64)
     return tf_run_t<double2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, em, nullptr, nullptr, 0,
-                             out_boost, nullptr, out_beta2, 1, 0, nullptr, 0, nullptr, nullptr, P.as<double2>());
+                             out_boost, nullptr, out_beta2, 1, 0, nullptr, 0, nullptr, cp, P.as<double2>());
   // mixed grid: complex64 matrices, double-float chain, FP64 boundary solve
   const size_t n = (size_t)G->nf * G->nd * G->nm * G->nm;
   DBuf P32;
   TCKS(P32.alloc(h, sizeof(float2) * n));
   if (bf::launch_convert(P.p, true, P32.p, false, n, h->stream())) return bf_fail(h, BF_ERR_CUDA, "convert");
   return tf_run_t<float2>(h, G->s, G->md, G->nf, G->freqs.data(), BF_PROP_3D, em, nullptr, nullptr, 0, out_boost,
-                          nullptr, out_beta2, 1, 0, nullptr, 1, nullptr, nullptr, P32.as<float2>());
+                          nullptr, out_beta2, 1, 0, nullptr, 1, nullptr, cp, P32.as<float2>());
+}
+
+extern "C" int bf_pgrid_transformer(bf_handle* h, bf_pgrid* G, const double* dist_shift, const double* emit,
+                                    double* out_boost, double* out_beta2) {
+  if (!h || !G || !dist_shift || (!out_boost && !out_beta2)) return BF_ERR_INVALID;
+  TCK(cudaSetDevice(h->device));
+  return pgrid_solve(h, G, dist_shift, emit, out_boost, out_beta2, nullptr);
+}
+
+// soft_box_penalty (utilities :150-160): 1 - (excess / depth)^6, the excess of
+// the largest of the shifts and their sum over the upper soft bound (or of the
+// lower soft bound over the smallest), depth 5 % of the box
+static double soft_box_penalty(const double* shift, int n, double lo, double hi) {
+  const double depth = (hi - lo) * 0.05, l = lo + depth, u = hi - depth;
+  double mx = -INFINITY, mn = INFINITY, sum = 0.0;
+  for (int k = 0; k < n; ++k) {
+    mx = std::max(mx, shift[k]);
+    mn = std::min(mn, shift[k]);
+    sum += shift[k];
+  }
+  mx = std::max(mx, sum);
+  mn = std::min(mn, sum);
+  const double excess = std::max(std::max(mx - u, -(mn - l)), 0.0);
+  return 1.0 - std::pow(excess / depth, 6);
+}
+
+// p_norm (utilities :211-215): max(X) (mean((X / max X)^p))^(1/p)
+static double p_norm(const double* x, int n, double p) {
+  double mag = -INFINITY;
+  for (int k = 0; k < n; ++k) mag = std::max(mag, x[k]);
+  double acc = 0.0;
+  for (int k = 0; k < n; ++k) acc += std::pow(x[k] / mag, p);
+  return mag * std::pow(acc / n, 1.0 / p);
+}
+
+extern "C" int bf_pgrid_cost(bf_handle* h, bf_pgrid* G, const double* dist_shift, const double* m_reflect, double p,
+                             double* out_cost, double* out_coupled) {
+  if (!h || !G || !dist_shift || !m_reflect || !out_cost) return BF_ERR_INVALID;
+  if (!std::isfinite(p) || p == 0.0) return bf_fail(h, BF_ERR_INVALID, "pgrid cost: p must be finite and non-zero");
+  TCK(cudaSetDevice(h->device));
+  const int ndisk = G->ngap - 1;
+  const double lo = G->s0 - 0.5 * G->ds, hi = G->s0 + (G->nsp - 0.5) * G->ds;
+  // hard penalty outside the interpolation bounds (utilities :131-135)
+  for (int k = 0; k < ndisk; ++k)
+    if (!(lo < dist_shift[k] && dist_shift[k] < hi)) {
+      *out_cost = 1000.0;
+      return BF_OK;
+    }
+  const double penalty = soft_box_penalty(dist_shift, ndisk, lo, hi);
+  std::vector<double> cpl(G->nf);
+  CoupleArgs cp{m_reflect, cpl.data()};
+  TCKS(pgrid_solve(h, G, dist_shift, nullptr, nullptr, nullptr, &cp));
+  if (out_coupled) std::memcpy(out_coupled, cpl.data(), sizeof(double) * G->nf);
+  *out_cost = -p_norm(cpl.data(), G->nf, p) * penalty;
+  return BF_OK;
 }

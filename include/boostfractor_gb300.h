@@ -295,8 +295,10 @@ int bf_transformer_trace_back(bf_handle* h, bf_stack* s, bf_modes* m, int nf, co
  * reference's ind_gap = 2:2:n_region); at grid point k every gap's distance is
  * the stack's distance + spacing_first + k spacing_step, k < nsp; the other
  * regions are computed once.  The grid is interpolated along the spacing with
- * a natural cubic B-spline (second derivative zero at the end knots, exact at
- * the knots).  The stack and the modes must outlive the grid. */
+ * the cubic B-spline of Interpolations.jl's BSpline(Cubic(Natural(OnCell())))
+ * (utilities :64): exact at the grid spacings, second derivative zero at the
+ * cell edges half a step beyond the first and last spacing, and defined up to
+ * those edges.  The stack and the modes must outlive the grid. */
 typedef struct bf_pgrid bf_pgrid;
 #define BF_PGRID_MAX_SPACINGS 64
 int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double* freqs, int nsp,
@@ -305,13 +307,23 @@ int bf_pgrid_destroy(bf_handle* h, bf_pgrid* g);
 /* Interpolated matrices at dist_shift (one shift per disk: gap region 2d+1
  * takes dist_shift[d]; the last region takes 0, as interpolate_prop_matrix
  * does).  out as bf_calc_propagation_matrices: nf x nd Julia (nm, nm) matrices.
- * A shift outside [spacing_first, last grid spacing] gives BF_ERR_INVALID. */
+ * A shift outside [spacing_first - step/2, last spacing + step/2] (the bounds
+ * of the reference's interpolation object) gives BF_ERR_INVALID. */
 int bf_pgrid_matrices(bf_handle* h, bf_pgrid* g, const double* dist_shift, double* out);
 /* The transformer on the interpolated matrices, without leaving the device:
  * calc_boostfactor_modes (utilities :98-110).  out_boost nf x nm complex and/or
  * out_beta2 nf; emit nm complex or NULL (the axion-induced modes). */
 int bf_pgrid_transformer(bf_handle* h, bf_pgrid* g, const double* dist_shift, const double* emit,
                          double* out_boost, double* out_beta2);
+/* calc_boostfactor_cost (utilities :130-144, with soft_box_penalty :150-160 and
+ * p_norm :211-215): the coupled power cpld[f] = |sum_m conj(boost[f][m])
+ * m_reflect[m]|^2 (fused after the boundary solve) and *out_cost =
+ * -p_norm(cpld, p) * penalty; 1000.0 without a solve when a shift is not
+ * strictly inside the interpolation bounds.  m_reflect nm complex; the
+ * reference uses p = -20; out_coupled nf or NULL (not written on the hard
+ * penalty). */
+int bf_pgrid_cost(bf_handle* h, bf_pgrid* g, const double* dist_shift, const double* m_reflect, double p,
+                  double* out_cost, double* out_coupled);
 
 /* ---- serving: a request loop over resident stacks ------------------------ */
 /* No counterpart in the reference, whose callers (the optimiser utilities,

@@ -673,3 +673,140 @@ def gauss_profile(coords, z=1e-9, omega0=0.1, f=10e9):
 def unnormalized_match(Eout, Eantenna, dx=0.01, dy=0.01):
     """src/beam_coupling.jl:13-15."""
     return np.sum(np.asarray(Eout) * np.conj(Eantenna)) * dx * dy
+
+
+# --------------------------------------------------------------------------
+# Optimiser utilities (examples/transformer_optim_utilities.jl)
+# --------------------------------------------------------------------------
+def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, prop=propagator, diskR=0.15):
+    """examples/transformer_optim_utilities.jl:10-50, without tilt grids.
+
+    Returns [region, frequency, spacing, nm, nm].  The gaps are the regions
+    1, 3, ..., nd-1 (0-based; the reference's ind_gap = 2:2:n_region, the
+    exit region included) and move by spacing_grid[s]; the mirror and the
+    disks (ind_solid) are computed once per frequency.  The reference splits
+    the setup into a gap setup and a solid setup; a region's matrix depends
+    only on that region's parameters, so shifting the gaps of one copy of the
+    setup gives the same matrices.
+    """
+    nd = len(sbdry.distance)
+    gaps = np.arange(1, nd, 2)
+    nm = modes.M * (2 * modes.L + 1)
+    sg = np.asarray(spacing_grid, dtype=float)
+    out = np.empty((nd, len(frequencies), len(sg), nm, nm), dtype=complex)
+    for f, fr in enumerate(frequencies):
+        solid = calc_propagation_matrices(sbdry, coords, modes, f=fr, prop=prop, diskR=diskR)
+        for s, sp in enumerate(sg):
+            sb = copy.deepcopy(sbdry)
+            sb.distance = np.array(sbdry.distance, dtype=float)
+            sb.distance[gaps] += sp
+            pm = calc_propagation_matrices(sb, coords, modes, f=fr, prop=prop, diskR=diskR)
+            for r in range(nd):
+                out[r, f, s] = pm[r] if r % 2 == 1 else solid[r]
+    return out
+
+
+class SpacingSpline:
+    """construct_prop_matrix_interpolation (utilities :56-73): cubic B-spline
+    along the spacing axis, Interpolations.jl BSpline(Cubic(Natural(OnCell()))).
+
+    Interpolations.jl (an unpinned dependency of the example, not vendored)
+    documents Natural (= Line) as a zero second derivative at the boundary, and
+    OnCell as placing that boundary at the cell edges, half a grid step beyond
+    the first and last point, where the interpolation's domain ends too.
+    Restated from that definition: with knot coordinates u = 1..n and
+    coefficients c_0..c_{n+1},
+        s(u) = sum_k c_k B3(u - k),   s(j) = y_j (j = 1..n),
+        s''(1/2) = s''(n + 1/2) = 0,
+    the end segments' polynomials extended over the half cells; the
+    (n+2) x (n+2) system is solved densely with numpy.linalg.solve.
+    """
+
+    def __init__(self, grid, spacing_grid):
+        sg = np.asarray(spacing_grid, dtype=float)
+        self.first, self.step, self.n = sg[0], sg[1] - sg[0], len(sg)
+        n = self.n
+        A = np.zeros((n + 2, n + 2))
+
+        def d2_row(i, t):   # s''(i + t) from the four coefficients c_{i-1..i+2}
+            row = np.zeros(n + 2)
+            row[i - 1:i + 2] += (1 - t) * np.array([1.0, -2.0, 1.0])
+            row[i:i + 3] += t * np.array([1.0, -2.0, 1.0])
+            return row
+
+        A[0] = d2_row(1, -0.5)
+        for j in range(1, n + 1):
+            A[j, j - 1:j + 2] = np.array([1.0, 4.0, 1.0]) / 6.0
+        A[n + 1] = d2_row(n - 1, 1.5)
+        y = np.moveaxis(np.asarray(grid), 2, 0)            # spacing axis first
+        rhs = np.zeros((n + 2,) + y.shape[1:], dtype=complex)
+        rhs[1:n + 1] = y
+        self.coef = np.linalg.solve(A, rhs.reshape(n + 2, -1)).reshape(rhs.shape)
+
+    @property
+    def bounds(self):
+        """Interpolations.bounds(itp)[3]: half a step beyond the end spacings."""
+        return (self.first - 0.5 * self.step, self.first + (self.n - 0.5) * self.step)
+
+    def __call__(self, r, f, shift):
+        lo, hi = self.bounds
+        if not (lo <= shift <= hi):
+            raise IndexError("shift outside the interpolation bounds")
+        u = 1.0 + (shift - self.first) / self.step
+        i = min(max(int(math.floor(u)), 1), self.n - 1)
+        t = u - i
+        w = np.array([(1 - t) ** 3, 3 * t ** 3 - 6 * t ** 2 + 4, -3 * t ** 3 + 3 * t ** 2 + 3 * t + 1, t ** 3]) / 6.0
+        return np.tensordot(w, self.coef[i - 1:i + 3, r, f], axes=1)
+
+
+def construct_prop_matrix_interpolation(prop_matrix_grid, spacing_grid):
+    """utilities :56-73."""
+    return SpacingSpline(prop_matrix_grid, spacing_grid)
+
+
+def interpolate_prop_matrix(itp, dist_shift):
+    """utilities :78-91: matrices [region][frequency] at the per-disk shifts;
+    solids and the exit region take shift 0 (:84)."""
+    nd = itp.coef.shape[1]
+    nf = itp.coef.shape[2]
+    shift_all = [0.0 if (r % 2 == 0 or r == nd - 1) else dist_shift[(r - 1) // 2] for r in range(nd)]
+    return [[itp(r, f, shift_all[r]) for f in range(nf)] for r in range(nd)]
+
+
+def calc_boostfactor_modes(sbdry, coords, modes, frequencies, prop_matrices_set, prop=propagator, diskR=0.15):
+    """utilities :99-110: EoutModes0[0, mode, frequency]."""
+    nm = modes.M * (2 * modes.L + 1)
+    out = np.empty((1, nm, len(frequencies)), dtype=complex)
+    for f, fr in enumerate(frequencies):
+        out[0, :, f] = transformer(sbdry, coords, modes, prop=prop, diskR=diskR, f=fr,
+                                   propagation_matrices=[prop_matrices_set[r][f] for r in range(len(prop_matrices_set))])
+    return out
+
+
+def soft_box_penalty(shift, bound_hard):
+    """utilities :150-160."""
+    depth = (bound_hard[1] - bound_hard[0]) * 0.05
+    l_soft, u_soft = bound_hard[0] + depth, bound_hard[1] - depth
+    ext = np.concatenate([np.asarray(shift, dtype=float), [np.sum(shift)]])
+    excess = max(np.max(ext) - u_soft, -(np.min(ext) - l_soft), 0.0)
+    return 1.0 - (excess / depth) ** 6
+
+
+def p_norm(X, p):
+    """utilities :211-215."""
+    X = np.asarray(X, dtype=float)
+    mag = np.max(X)
+    return mag * (np.sum((X / mag) ** p) / len(X)) ** (1.0 / p)
+
+
+def calc_boostfactor_cost(dist_shift, itp, frequencies, sbdry, coords, modes, m_reflect, prop=propagator,
+                          diskR=0.15):
+    """utilities :130-144."""
+    lo, hi = itp.bounds
+    if any(not (lo < s < hi) for s in dist_shift):
+        return 1000.0
+    penalty = soft_box_penalty(dist_shift, (lo, hi))
+    pm = interpolate_prop_matrix(itp, dist_shift)
+    Eout = calc_boostfactor_modes(sbdry, coords, modes, frequencies, pm, prop=prop, diskR=diskR)
+    cpld = np.abs(np.sum(np.conj(Eout[0]) * np.asarray(m_reflect)[:, None], axis=0)) ** 2
+    return -p_norm(cpld, -20) * penalty

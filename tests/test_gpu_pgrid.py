@@ -52,32 +52,29 @@ def shifted(kw, shift_per_disk, last=0.0):
 
 
 def test_pgrid_knots_and_spline_vs_oracle(B):
+    """The device grid and its spline against the oracle's
+    calc_propagation_matrices_grid + construct_prop_matrix_interpolation +
+    interpolate_prop_matrix, at knots, between them and in the half cells
+    beyond the end spacings (the OnCell domain)."""
     kw, cb, co, mb, mo, grid, freqs = setup(B)
     pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
     try:
         nd = len(kw["distance"])
-        # oracle grid values of every region at every spacing (gaps shifted, the last region included)
-        ref = np.zeros((len(grid), len(freqs), nd, mo.nm, mo.nm), dtype=complex)
-        for k, s in enumerate(grid):
-            sb = O.seed_setup_boundaries(co, **shifted(kw, [s, s], last=s))
-            for f, fr in enumerate(freqs):
-                ref[k, f] = np.array(O.calc_propagation_matrices(sb, co, mo, f=fr))
-        ref[:, :, 0] = 0.0   # the mirror (NaN permittivity, as the reference leaves it) is not compared
-        from scipy.interpolate import CubicSpline
-        spl = CubicSpline(grid, ref, axis=0, bc_type="natural")
+        sb = O.seed_setup_boundaries(co, **kw)
+        ref = O.calc_propagation_matrices_grid(sb, co, mo, grid, freqs)
+        ref[0] = 0.0   # the mirror (NaN permittivity, as the reference leaves it) is not compared
+        itp = O.construct_prop_matrix_interpolation(ref, grid)
+        step = grid[1] - grid[0]
+        assert np.allclose(pg.bounds, itp.bounds, rtol=0, atol=1e-15)
         rng = np.random.default_rng(62)
-        for shifts in ([grid[2], grid[5]], [grid[0], grid[-1]], list(rng.uniform(grid[0], grid[-1], 2)),
-                       list(rng.uniform(grid[0], grid[-1], 2))):
+        for shifts in ([grid[2], grid[5]], [grid[0], grid[-1]], [grid[0] - 0.4 * step, grid[-1] + 0.45 * step],
+                       [grid[0] - 0.5 * step, grid[-1] + 0.5 * step], list(rng.uniform(grid[0], grid[-1], 2)),
+                       list(rng.uniform(*itp.bounds, 2))):
             got = pg.matrices(np.array(shifts))
+            want = O.interpolate_prop_matrix(itp, shifts)
             for f in range(len(freqs)):
                 for j in range(1, nd):
-                    if j % 2 == 0:
-                        want = ref[0, f, j]                                   # solids do not move
-                    elif j == nd - 1:
-                        want = spl(0.0)[f, j]                                 # the last region keeps shift 0
-                    else:
-                        want = spl(shifts[(j - 1) // 2])[f, j]
-                    assert rel(got[f, j], want) < 1e-10, (shifts, f, j)
+                    assert rel(got[f, j], want[j][f]) < 1e-10, (shifts, f, j)
     finally:
         pg.close()
 
@@ -108,7 +105,7 @@ def test_pgrid_rejects_shift_outside_grid(B):
     pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
     try:
         with pytest.raises(B.BFError) as e:
-            pg.matrices(np.array([0.0, grid[-1] + 1e-5]))
+            pg.matrices(np.array([0.0, grid[-1] + 0.51 * (grid[1] - grid[0])]))
         assert e.value.code == 1
     finally:
         pg.close()
@@ -152,5 +149,34 @@ def test_pgrid_requests_through_the_server(B):
                 srv.submit(None, freqs[:1], "pgrid", distance=shifts[0], pgrid=pg)
         finally:
             srv.close()
+    finally:
+        pg.close()
+
+
+def test_pgrid_cost_vs_oracle(B):
+    """calc_boostfactor_cost on the device (coupled power fused after the
+    solve, p-norm and soft box penalty on the host) against the oracle's,
+    inside the box, in the soft-penalty band and outside the hard bounds."""
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    pg = B.PGrid(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, grid)
+    try:
+        sb = O.seed_setup_boundaries(co, **kw)
+        ref = O.calc_propagation_matrices_grid(sb, co, mo, grid, freqs)
+        itp = O.construct_prop_matrix_interpolation(ref, grid)
+        rng = np.random.default_rng(64)
+        m_reflect = rng.standard_normal(mo.nm) + 1j * rng.standard_normal(mo.nm)
+        lo, hi = itp.bounds
+        depth = 0.05 * (hi - lo)
+        for sh in ([1.3e-4, -2.2e-4], [hi - 0.4 * depth, -1e-4], [lo + 0.3 * depth, 0.0], [0.0, hi + 1e-9]):
+            sb_c = O.seed_setup_boundaries(co, **kw)
+            want = O.calc_boostfactor_cost(sh, itp, freqs, sb_c, co, mo, m_reflect)
+            got = B.calc_boostfactor_cost(np.array(sh), pg, freqs, None, cb, mb, m_reflect)
+            if want == 1000.0:
+                assert got == 1000.0
+            else:
+                assert abs(got - want) < 1e-10 * abs(want), (sh, got, want)
+        cost, cpl = pg.cost(np.array([1.3e-4, -2.2e-4]), m_reflect)
+        boost, _ = pg.transformer(np.array([1.3e-4, -2.2e-4]))
+        assert rel(cpl, np.abs(boost.conj() @ m_reflect) ** 2) < 1e-13
     finally:
         pg.close()
