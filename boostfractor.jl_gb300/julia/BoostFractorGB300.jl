@@ -212,4 +212,95 @@ function transformer_trace_back(reflected_beam, input_beam, bdry::SetupBoundarie
     return out
 end
 
+# ---- optimiser utilities (examples/transformer_optim_utilities.jl) ----------
+
+function modes_create(handle::Handle, coords::CoordinateSystem, modes::Modes, diskR)
+    mref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(handle, ccall((:bf_modes_create, lib), Cint,
+        (Ptr{Cvoid}, Cint, Cint, Ptr{Float64}, Ptr{Float64}, Cint, Cint, Cint, Float64,
+         Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{Ptr{Cvoid}}),
+        handle.ptr, length(coords.X), length(coords.Y), collect(Float64, coords.X),
+        collect(Float64, coords.Y), 1, modes.M, modes.L, diskR, modes.mode_patterns, modes.mode_kt, mref))
+    return mref[]
+end
+
+"""Propagation matrices over gap spacings x frequencies, resident on the GPU and
+prefiltered for the spacing spline of Interpolations' BSpline(Cubic(Natural(OnCell())))."""
+mutable struct PGrid
+    handle::Handle
+    stack::Ptr{Cvoid}
+    modes::Ptr{Cvoid}
+    grid::Ptr{Cvoid}
+    freqs::Vector{Float64}
+    nd::Int
+    nm::Int
+end
+
+function release(g::PGrid)
+    g.grid == C_NULL && return nothing
+    ccall((:bf_pgrid_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), g.handle.ptr, g.grid)
+    stack_destroy(g.handle, g.stack)
+    ccall((:bf_modes_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), g.handle.ptr, g.modes)
+    g.grid = C_NULL
+    return nothing
+end
+
+"""
+    calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies;
+                                   prop=propagator, diskR=0.15, precision=:fp64)
+
+examples/transformer_optim_utilities.jl:10 (without tilt grids) on the GPU.
+Returns a PGrid, which is also the interpolation object.
+"""
+function calc_propagation_matrices_grid(sbdry::SetupBoundaries, coords::CoordinateSystem, modes::Modes,
+                                        spacing_grid::AbstractRange, frequencies; prop=propagator, diskR=0.15,
+                                        precision=:fp64, handle=default_handle())
+    freqs = Float64.(collect(frequencies))
+    m = modes_create(handle, coords, modes, diskR)
+    s = stack(handle, sbdry, coords, diskR)
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:bf_pgrid_create, lib), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Float64, Cint, Cint,
+         Ptr{Ptr{Cvoid}}),
+        handle.ptr, s, m, length(freqs), freqs, length(spacing_grid), Float64(first(spacing_grid)),
+        Float64(step(spacing_grid)), BF_PROP[prop], BF_PREC[precision], ref)
+    if rc != 0
+        stack_destroy(handle, s)
+        ccall((:bf_modes_destroy, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}), handle.ptr, m)
+        check(handle, rc)
+    end
+    g = PGrid(handle, s, m, ref[], freqs, length(sbdry.distance), modes.M * (2modes.L + 1))
+    finalizer(release, g)
+    return g
+end
+
+"""utilities :56: the PGrid is its own interpolation object."""
+construct_prop_matrix_interpolation(g::PGrid, spacing_grid=nothing) = g
+
+"""utilities :78: Array{Matrix{ComplexF64}}(n_region, n_freq) at the shifts."""
+function interpolate_prop_matrix(g::PGrid, dist_shift::AbstractVector)
+    nf = length(g.freqs)
+    out = Array{ComplexF64}(undef, g.nm, g.nm, g.nd, nf)
+    check(g.handle, ccall((:bf_pgrid_matrices, lib), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{ComplexF64}),
+                          g.handle.ptr, g.grid, Float64.(dist_shift), out))
+    return [out[:, :, r, f] for r in 1:g.nd, f in 1:nf]
+end
+
+"""
+    calc_boostfactor_cost(dist_shift, itp::PGrid, frequencies, sbdry, coords, modes, m_reflect;
+                          prop=propagator, diskR=0.15)
+
+utilities :130 on the GPU: -p_norm(coupled power, -20) x soft_box_penalty, or
+1000.0 outside the interpolation bounds.
+"""
+function calc_boostfactor_cost(dist_shift::AbstractVector, g::PGrid, frequencies, sbdry, coords, modes, m_reflect;
+                               prop=propagator, diskR=0.15)
+    Float64.(collect(frequencies)) == g.freqs || throw(ArgumentError("frequencies must be the grid's"))
+    cost = Ref{Float64}(0.0)
+    check(g.handle, ccall((:bf_pgrid_cost, lib), Cint,
+        (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}, Ptr{ComplexF64}, Float64, Ptr{Float64}, Ptr{Float64}),
+        g.handle.ptr, g.grid, Float64.(dist_shift), ComplexF64.(collect(m_reflect)), -20.0, cost, C_NULL))
+    return cost[]
+end
+
 end # module
