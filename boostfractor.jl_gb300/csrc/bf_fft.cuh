@@ -26,6 +26,26 @@ template <typename C> __device__ __forceinline__ C root1024(int k);
 template <> __device__ __forceinline__ float2 root1024<float2>(int k) { return c_root1024_f[k]; }
 template <> __device__ __forceinline__ double2 root1024<double2>(int k) { return c_root1024_d[k]; }
 
+// Butterfly adds.  For complex64 both halves go through one packed FP32x2
+// instruction (add/sub.rn.f32x2, Blackwell): an FFT is mostly complex adds, so
+// this halves its add instructions.  Each lane rounds exactly like a scalar add.
+template <typename C> __device__ __forceinline__ C vadd(C a, C b) { return cadd(a, b); }
+template <typename C> __device__ __forceinline__ C vsub(C a, C b) { return csub(a, b); }
+template <> __device__ __forceinline__ float2 vadd<float2>(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+template <> __device__ __forceinline__ float2 vsub<float2>(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+      "sub.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+      : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+
 // v[i] *= W_M^k (forward) or conj(W_M^k) (inverse), k compile-time after unrolling.
 template <int M, bool INV, typename C>
 __device__ __forceinline__ C twiddle_mul(C a, int k) {
@@ -61,8 +81,8 @@ __device__ __forceinline__ void reg_dft(C (&v)[LEN]) {
         for (int j = 0; j < half; ++j) {
           C a = v[OFF + i + j];
           C b = v[OFF + i + j + half];
-          v[OFF + i + j] = cadd(a, b);
-          v[OFF + i + j + half] = twiddle_mul<M, INV>(csub(a, b), j * (M / len));
+          v[OFF + i + j] = vadd(a, b);
+          v[OFF + i + j + half] = twiddle_mul<M, INV>(vsub(a, b), j * (M / len));
         }
       }
     }
