@@ -331,8 +331,190 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
   }
 }
 
-// One bounce stage: grid = (steps of the stage, frequencies).
-template <typename R, int N>
+// ---- joint step: both slots propagated, processed together ----------------
+// The rows of A and of B form one task list (2 nby rows), and so do their
+// columns (2 N), so the teams stay busy where a single field's nby rows leave
+// most of them idle in the last round; the propagated fields stay in shared
+// memory (MA, MB) and the boundary mix runs as one pass over the box.
+
+// Phase 1, joint: forward FFT along x of the box rows of A (tasks < nby) and B.
+template <typename C, int N>
+__device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
+                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
+  const int rv = (nbx + G - 1) / G;
+  for (int base = 0; base < ntask; base += NTEAM) {
+    const int t = base + team;
+    const bool act = t < ntask;
+    if (!__any_sync(0xffffffffu, act)) continue;
+    const bool isb = act && t >= nby;
+    const int y = act ? (isb ? t - nby : t) : 0;
+    const int slot = isb ? sd.sb : sd.sa, exitk = isb ? sd.exitB : sd.exitA;
+    const C* row = a.state + (((size_t)f * a.nslots + slot) * nby + y) * (size_t)nbx;
+    double2* arow = exitk >= 0 ? a.exitacc + (((size_t)exitk * a.nfreq + f) * nby + y) * (size_t)nbx : nullptr;
+    C v[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      v[r] = czero<C>();
+      if (r < rv) {
+        const int x = g + G * r;
+        if (act && x < nbx) {
+          const C val = row[x];
+          v[r] = val;
+          if (arow) {
+            double2 o = arow[x];
+            double2 d = to_d(val);
+            arow[x] = make_double2(o.x + d.x, o.y + d.y);
+          }
+        }
+      }
+    }
+    X::T::forward(v, tw, scr, g);
+    if (act) {
+      C* M = isb ? MB : MA;
+#pragma unroll
+      for (int j = 0; j < CC; ++j)
+#pragma unroll
+        for (int q = 0; q < G; ++q) M[y * P + g * CC + j + RR * q] = v[j * G + q];
+    }
+  }
+  __syncthreads();
+}
+
+// Phase 2, joint: columns of A (tasks < N) and of B, each with its region's phasor.
+template <typename C, int N>
+__device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
+                                             const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nby = a.nby;
+  const int QW = a.fold ? N / 2 : N;
+  const int rv = (nby + G - 1) / G;
+  static_assert((2 * N) % NTEAM == 0 || NTEAM > 2 * N, "column tasks");
+  for (int base = 0; base < 2 * N; base += NTEAM) {
+    const int t = base + team;
+    const bool act = t < 2 * N;
+    if (!__any_sync(0xffffffffu, act)) continue;
+    const bool isb = act && t >= N;
+    const int kx = act ? (isb ? t - N : t) : 0;
+    C* M = isb ? MB : MA;
+    const C* Q = isb ? QB : QA;
+    C v[RR];
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      v[r] = czero<C>();
+      if (r < rv) {
+        const int y = g + G * r;
+        if (act && y < nby) v[r] = M[y * P + kx];
+      }
+    }
+    X::T::forward(v, tw, scr, g);
+    if (act) {
+      if (a.fold) {
+        const C* Qrow = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
+#pragma unroll
+        for (int j = 0; j < CC; ++j)
+#pragma unroll
+          for (int q = 0; q < G; ++q) {
+            const int ky = g * CC + j + RR * q;
+            v[j * G + q] = cmul(v[j * G + q], Qrow[q < G / 2 ? ky : N - 1 - ky]);
+          }
+      } else {
+        const C* Qrow = Q + (size_t)kx * QW;
+#pragma unroll
+        for (int j = 0; j < CC; ++j)
+#pragma unroll
+          for (int q = 0; q < G; ++q) v[j * G + q] = cmul(v[j * G + q], Qrow[g * CC + j + RR * q]);
+      }
+    }
+    X::T::inverse(v, tw, scr, g);
+    if (act) {
+#pragma unroll
+      for (int r = 0; r < RR; ++r) {
+        if (r < rv) {
+          const int y = g + G * r;
+          if (y < nby) M[y * P + kx] = v[r];
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Phase 3, joint: inverse FFT along x of the box rows of A and B, times the
+// region's tilt/surface map, written back in place into the row's first nbx
+// entries (the team's exchange has already consumed the row).
+template <typename C, int N>
+__device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
+                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
+  const size_t plane = (size_t)nby * nbx;
+  const int tiA = a.tilt_idx[sd.ra], tiB = a.tilt_idx[sd.rb];
+  const C* tA = tiA >= 0 ? a.tilt + ((size_t)f * a.ntilt + tiA) * plane : nullptr;
+  const C* tB = tiB >= 0 ? a.tilt + ((size_t)f * a.ntilt + tiB) * plane : nullptr;
+  const int rv = (nbx + G - 1) / G;
+  for (int base = 0; base < ntask; base += NTEAM) {
+    const int t = base + team;
+    const bool act = t < ntask;
+    if (!__any_sync(0xffffffffu, act)) continue;
+    const bool isb = act && t >= nby;
+    const int y = act ? (isb ? t - nby : t) : 0;
+    C* M = isb ? MB : MA;
+    const C* tmap = isb ? tB : tA;
+    C v[RR];
+#pragma unroll
+    for (int j = 0; j < CC; ++j)
+#pragma unroll
+      for (int q = 0; q < G; ++q) v[j * G + q] = act ? M[y * P + g * CC + j + RR * q] : czero<C>();
+    X::T::inverse(v, tw, scr, g);
+    if (!act) continue;
+#pragma unroll
+    for (int r = 0; r < RR; ++r) {
+      if (r >= rv) continue;
+      const int x = g + G * r;
+      if (x >= nbx) continue;
+      C p = v[r];
+      if (tmap) p = cmul(p, tmap[y * nbx + x]);
+      M[y * P + x] = p;
+    }
+  }
+  __syncthreads();
+}
+
+// Boundary mix of a joint step over the whole box: A' = cAA A~ + cAB B~ (+ add),
+// B' = cBA A~ + cBB B~, stored masked.
+template <typename C, int N>
+__device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc& sd, int f, const C* MA,
+                                          const C* MB) {
+  constexpr int P = FusedCtx<C, N>::P;
+  const int nbx = a.nbx, nby = a.nby;
+  const size_t plane = (size_t)nby * nbx;
+  C* stA = sd.sa >= 0 ? a.state + ((size_t)f * a.nslots + sd.sa) * plane : nullptr;
+  C* stB = sd.sb >= 0 ? a.state + ((size_t)f * a.nslots + sd.sb) * plane : nullptr;
+  const C* add = sd.addA >= 0 ? a.addbuf + (size_t)sd.addA * plane : nullptr;
+  const double2* cf = a.coefs + 4 * sd.coef;
+  const C cAA = from_d<C>(cf[0]), cAB = from_d<C>(cf[1]), cBA = from_d<C>(cf[2]), cBB = from_d<C>(cf[3]);
+  for (int i = threadIdx.x; i < (int)plane; i += blockDim.x) {
+    const int y = i / nbx, x = i - y * nbx;
+    const C A = MA[y * P + x], B = MB[y * P + x];
+    const bool in = a.mask[i] != 0;
+    if (stA) {
+      C o = cadd(cmul(cAA, A), cmul(cAB, B));
+      if (add) o = cadd(o, add[i]);
+      stA[i] = in ? o : czero<C>();
+    }
+    if (stB) stB[i] = in ? cadd(cmul(cBA, A), cmul(cBB, B)) : czero<C>();
+  }
+}
+
+// One bounce stage: grid = (steps of the stage, frequencies).  JOINT: steps
+// with both slots propagated take the joint path (twice the row tile in
+// shared memory).
+template <typename R, int N, bool JOINT>
 __global__ void __launch_bounds__(kFusedThreads, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
 k_fused_stage(FusedArgs<cplx_t<R>> a) {
   using C = cplx_t<R>;
@@ -341,7 +523,7 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nby = a.nby;
   C* M = reinterpret_cast<C*>(smem_raw + kSmemHeader);
-  C* scr_all = M + nby * P;
+  C* scr_all = M + (JOINT ? 2 : 1) * nby * P;
   const int tid = threadIdx.x, team = tid / G, g = tid % G;
   C* scr = scr_all + team * X::T::SCR;
   const StepDesc sd = a.steps[blockIdx.x];
@@ -353,7 +535,13 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
     return a.phasor + ((size_t)f * a.ntab + region) * (size_t)(QW * QW);
   };
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
-  if (pa && pb) {
+  if (JOINT && pa && pb) {
+    C* MB = M + nby * P;
+    joint_phase1<C, N>(a, sd, f, M, MB, scr, tw, team, g);
+    joint_phase2<C, N>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g);
+    joint_phase3<C, N>(a, sd, f, M, MB, scr, tw, team, g);
+    joint_mix<C, N>(a, sd, f, M, MB);
+  } else if (pa && pb) {
     // A~ is parked in the A slot itself until the boundary mix
     C* obuf = a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * a.nbx);
     fused_phase1<C, N>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
@@ -375,9 +563,9 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
 }
 
 template <int N>
-static size_t fused_smem_for(int nby, size_t csz) {
+static size_t fused_smem_for(int nby, size_t csz, int tiles = 1) {
   const size_t nteam = kFusedThreads / Team<N>::G;
-  return kSmemHeader + csz * ((size_t)nby * fused_pitch<N>() + nteam * Team<N>::SCR);
+  return kSmemHeader + csz * ((size_t)tiles * nby * fused_pitch<N>() + nteam * Team<N>::SCR);
 }
 
 static size_t smem_for(int N, int nby, size_t csz) {
@@ -405,16 +593,32 @@ bool fused_supported(int N, int nbx, int nby, bool fp64) {
   return fused_smem_bytes(N, nbx, nby, fp64) <= kMaxSmem;
 }
 
+// Shared memory of one SM (bytes) and what the driver reserves per CTA.
+static const size_t kSmemPerSM = 228 * 1024, kSmemReservedPerCta = 1024;
+
 template <typename R, int N>
 static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
-  const size_t smem = smem_for(N, a.nby, sizeof(cplx_t<R>));
+  const size_t csz = sizeof(cplx_t<R>);
+  const size_t smem = fused_smem_for<N>(a.nby, csz, 1);
   if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
-  if (e != cudaSuccess) return (int)e;
+  // the joint path when the doubled row tile keeps as many CTAs per SM
+  const int ctas = (sizeof(R) == 4 && N <= 128) ? 2 : 1;
+  const size_t smem_j = fused_smem_for<N>(a.nby, csz, 2);
+  const bool joint = smem_j <= kMaxSmem && (size_t)ctas * (smem_j + kSmemReservedPerCta) <= kSmemPerSM &&
+                     (size_t)ctas * (smem + kSmemReservedPerCta) <= kSmemPerSM;
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
-  k_fused_stage<R, N><<<grid, kFusedThreads, smem, st>>>(a);
+  if (joint) {
+    cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem_j);
+    if (e != cudaSuccess) return (int)e;
+    k_fused_stage<R, N, true><<<grid, kFusedThreads, smem_j, st>>>(a);
+  } else {
+    cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return (int)e;
+    k_fused_stage<R, N, false><<<grid, kFusedThreads, smem, st>>>(a);
+  }
   return (int)cudaGetLastError();
 }
 
