@@ -38,6 +38,8 @@ __host__ __device__ __forceinline__ C cmul_mi(C a) {
 }
 template <typename C>
 __host__ __device__ __forceinline__ C cconj(C a) { return mk(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 czero_of(float2) { return make_float2(0.0f, 0.0f); }
+__host__ __device__ __forceinline__ double2 czero_of(double2) { return make_double2(0.0, 0.0); }
 
 __device__ __forceinline__ float2 to_c(double2 v, float2) { return make_float2((float)v.x, (float)v.y); }
 __device__ __forceinline__ double2 to_c(double2 v, double2) { return v; }

@@ -18,6 +18,8 @@
 #include <math.h>
 #include <stdio.h>
 
+#include <algorithm>
+
 #include "bf_common.cuh"
 #include "bf_device.cuh"
 #include "bf_fft.cuh"
@@ -165,7 +167,7 @@ struct FusedCtx {
 // are stored pre-masked, so only register slots r < ceil(nbx/G) can hold box
 // pixels.  A slot feeding an exit adds its (masked) input to the FP64 exit
 // accumulator on the way.
-template <typename C, int N>
+template <typename C, int N, int NZ>
 __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int slot, int exitk, C* M,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
@@ -184,7 +186,7 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       v[r] = czero<C>();
-      if (r < rv) {
+      if (r < NZ && r < rv) {
         const int x = g + G * r;
         if (act && x < nbx) {
           const C val = row[x];
@@ -197,7 +199,7 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
         }
       }
     }
-    X::T::forward(v, tw, scr, g);
+    X::T::template forward<NZ>(v, tw, scr, g);
     if (act) {
 #pragma unroll
       for (int j = 0; j < CC; ++j)
@@ -210,7 +212,7 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
 
 // Phase 2: per column kx, forward FFT along y, phasor, inverse FFT along y,
 // in place in M (only the nby box rows are read and written).
-template <typename C, int N>
+template <typename C, int N, int NZ>
 __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, C* M, C* scr,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
@@ -226,12 +228,12 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       v[r] = czero<C>();
-      if (r < rv) {
+      if (r < NZ && r < rv) {
         const int y = g + G * r;
         if (act && y < nby) v[r] = M[y * P + kx];
       }
     }
-    X::T::forward(v, tw, scr, g);
+    X::T::template forward<NZ>(v, tw, scr, g);
     if (act) {
       if (a.fold) {
         // bins k and N-1-k share a phasor; ky = g*CC + j + RR*q < N/2 exactly when q < G/2
@@ -255,7 +257,7 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
     if (act) {
 #pragma unroll
       for (int r = 0; r < RR; ++r) {
-        if (r < rv) {
+        if (r < NZ && r < rv) {
           const int y = g + G * r;
           if (y < nby) M[y * P + kx] = v[r];
         }
@@ -268,7 +270,7 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
 // Phase 3: inverse FFT along x of every box row, tilt/surface map, then the
 // epilogue: store the propagated field into obuf (first of two propagations)
 // or apply the boundary mix and write the new (masked) fields.
-template <typename C, int N, bool MIX>
+template <typename C, int N, bool MIX, int NZ>
 __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, int region,
                                              bool prop_is_b, C* M, C* scr, C* obuf,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
@@ -300,7 +302,7 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
     if (!act) continue;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
-      if (r >= rv) continue;
+      if (r >= NZ || r >= rv) continue;
       const int x = g + G * r;
       if (x >= nbx) continue;
       const int i = y * nbx + x;
@@ -338,7 +340,7 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
 // memory (MA, MB) and the boundary mix runs as one pass over the box.
 
 // Phase 1, joint: forward FFT along x of the box rows of A (tasks < nby) and B.
-template <typename C, int N>
+template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
@@ -358,7 +360,7 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       v[r] = czero<C>();
-      if (r < rv) {
+      if (r < NZ && r < rv) {
         const int x = g + G * r;
         if (act && x < nbx) {
           const C val = row[x];
@@ -371,7 +373,7 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
         }
       }
     }
-    X::T::forward(v, tw, scr, g);
+    X::T::template forward<NZ>(v, tw, scr, g);
     if (act) {
       C* M = isb ? MB : MA;
 #pragma unroll
@@ -384,7 +386,7 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
 }
 
 // Phase 2, joint: columns of A (tasks < N) and of B, each with its region's phasor.
-template <typename C, int N>
+template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
@@ -405,12 +407,12 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
       v[r] = czero<C>();
-      if (r < rv) {
+      if (r < NZ && r < rv) {
         const int y = g + G * r;
         if (act && y < nby) v[r] = M[y * P + kx];
       }
     }
-    X::T::forward(v, tw, scr, g);
+    X::T::template forward<NZ>(v, tw, scr, g);
     if (act) {
       if (a.fold) {
         const C* Qrow = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
@@ -433,7 +435,7 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
     if (act) {
 #pragma unroll
       for (int r = 0; r < RR; ++r) {
-        if (r < rv) {
+        if (r < NZ && r < rv) {
           const int y = g + G * r;
           if (y < nby) M[y * P + kx] = v[r];
         }
@@ -446,7 +448,7 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
 // Phase 3, joint: inverse FFT along x of the box rows of A and B, times the
 // region's tilt/surface map, written back in place into the row's first nbx
 // entries (the team's exchange has already consumed the row).
-template <typename C, int N>
+template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
@@ -474,7 +476,7 @@ __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDe
     if (!act) continue;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
-      if (r >= rv) continue;
+      if (r >= NZ || r >= rv) continue;
       const int x = g + G * r;
       if (x >= nbx) continue;
       C p = v[r];
@@ -513,8 +515,10 @@ __device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc&
 
 // One bounce stage: grid = (steps of the stage, frequencies).  JOINT: steps
 // with both slots propagated take the joint path (twice the row tile in
-// shared memory).
-template <typename R, int N, bool JOINT>
+// shared memory).  NZ: box lines occupy at most NZ of a thread's RR register
+// slots (x = g + G r < nbx, y = g + G r < nby only for r < NZ), so the first
+// forward pass is pruned and the inverse stores only NZ slots.
+template <typename R, int N, bool JOINT, int NZ>
 __global__ void __launch_bounds__(kFusedThreads, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
 k_fused_stage(FusedArgs<cplx_t<R>> a) {
   using C = cplx_t<R>;
@@ -537,28 +541,28 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
   if (JOINT && pa && pb) {
     C* MB = M + nby * P;
-    joint_phase1<C, N>(a, sd, f, M, MB, scr, tw, team, g);
-    joint_phase2<C, N>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g);
-    joint_phase3<C, N>(a, sd, f, M, MB, scr, tw, team, g);
+    joint_phase1<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
+    joint_phase2<C, N, NZ>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g);
+    joint_phase3<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
     joint_mix<C, N>(a, sd, f, M, MB);
   } else if (pa && pb) {
     // A~ is parked in the A slot itself until the boundary mix
     C* obuf = a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * a.nbx);
-    fused_phase1<C, N>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, false>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, false, NZ>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
     __syncthreads();
-    fused_phase1<C, N>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
   } else if (pa) {
-    fused_phase1<C, N>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, true>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
   } else if (pb) {
-    fused_phase1<C, N>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
   }
 }
 
@@ -596,6 +600,20 @@ bool fused_supported(int N, int nbx, int nby, bool fp64) {
 // Shared memory of one SM (bytes) and what the driver reserves per CTA.
 static const size_t kSmemPerSM = 228 * 1024, kSmemReservedPerCta = 1024;
 
+template <typename R, int N, bool JOINT, int NZ>
+static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  k_fused_stage<R, N, JOINT, NZ><<<grid, kFusedThreads, smem, st>>>(a);
+  return (int)cudaGetLastError();
+}
+
+// Register slots a box line may occupy in the pruned complex64 variants: 5 of
+// 16 (3 of 8) covers boxes up to 5/16 of the grid, the disk of radius 0.15 m
+// in the reference's 1 m window.
+template <int N> constexpr int pruned_slots() { return (5 * Team<N>::RR + 15) / 16; }
+
 template <typename R, int N>
 static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
   const size_t csz = sizeof(cplx_t<R>);
@@ -606,20 +624,16 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
   const size_t smem_j = fused_smem_for<N>(a.nby, csz, 2);
   const bool joint = smem_j <= kMaxSmem && (size_t)ctas * (smem_j + kSmemReservedPerCta) <= kSmemPerSM &&
                      (size_t)ctas * (smem + kSmemReservedPerCta) <= kSmemPerSM;
+  constexpr int G = Team<N>::G, RR = Team<N>::RR;
+  const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
-  if (joint) {
-    cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem_j);
-    if (e != cudaSuccess) return (int)e;
-    k_fused_stage<R, N, true><<<grid, kFusedThreads, smem_j, st>>>(a);
-  } else {
-    cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    k_fused_stage<R, N, false><<<grid, kFusedThreads, smem, st>>>(a);
+  if constexpr (sizeof(R) == 4 && N >= 64) {
+    if (rv <= pruned_slots<N>())
+      return joint ? launch_fused_v<R, N, true, pruned_slots<N>()>(a, grid, smem_j, st)
+                   : launch_fused_v<R, N, false, pruned_slots<N>()>(a, grid, smem, st);
   }
-  return (int)cudaGetLastError();
+  return joint ? launch_fused_v<R, N, true, RR>(a, grid, smem_j, st) : launch_fused_v<R, N, false, RR>(a, grid, smem, st);
 }
 
 template <typename R>

@@ -98,6 +98,73 @@ __device__ __forceinline__ void reg_dft(C (&v)[LEN]) {
   }
 }
 
+// Zero pattern (bit p = point p is exactly zero) at the input of the stage of
+// length len of an M-point DIF DFT whose inputs NZ .. M-1 are zero: a
+// butterfly output is zero only if both of its inputs were.
+template <int M, int NZ>
+__host__ __device__ constexpr unsigned long long dif_zero_mask(int len) {
+  unsigned long long z = 0;
+  for (int p = NZ; p < M; ++p) z |= 1ull << p;
+  for (int l = M; l > len; l >>= 1) {
+    const int half = l >> 1;
+    unsigned long long n = 0;
+    for (int p = 0; p < M; ++p)
+      if (((z >> p) & 1ull) && ((z >> (p ^ half)) & 1ull)) n |= 1ull << p;
+    z = n;
+  }
+  return z;
+}
+
+// One DIF stage (length LEN) of reg_dft_nz, then the next.
+template <int M, bool INV, int NZ, int LEN, int VLEN, typename C>
+__device__ __forceinline__ void dif_stage_nz(C (&v)[VLEN]) {
+  constexpr unsigned long long zm = dif_zero_mask<M, NZ>(LEN);
+  constexpr int half = LEN / 2;
+#pragma unroll
+  for (int i = 0; i < M; i += LEN) {
+#pragma unroll
+    for (int j = 0; j < half; ++j) {
+      const int pa = i + j, pb = pa + half;
+      const bool za = (zm >> pa) & 1ull, zb = (zm >> pb) & 1ull;
+      const int k = j * (M / LEN);
+      if (za && zb) continue;
+      const C a = v[pa], b = v[pb];
+      if (zb) {
+        v[pb] = twiddle_mul<M, INV>(a, k);
+      } else if (za) {
+        v[pa] = b;
+        v[pb] = twiddle_mul<M, INV>(csub(czero_of(b), b), k);
+      } else {
+        v[pa] = vadd(a, b);
+        v[pb] = twiddle_mul<M, INV>(vsub(a, b), k);
+      }
+    }
+  }
+  if constexpr (LEN > 2) dif_stage_nz<M, INV, NZ, LEN / 2>(v);
+}
+
+// reg_dft<M, INV, 0> of v[0 .. M-1] whose inputs v[NZ ..] are zero: butterflies
+// with a zero input reduce to a copy and a twiddle, those with two zero inputs
+// vanish.  The results are those of the dense DFT (adding an exact zero
+// changes nothing but the sign of a zero).
+template <int M, bool INV, int NZ, int LEN, typename C>
+__device__ __forceinline__ void reg_dft_nz(C (&v)[LEN]) {
+  if constexpr (NZ >= M || M < 2) {
+    reg_dft<M, INV, 0>(v);
+  } else {
+    dif_stage_nz<M, INV, NZ, M>(v);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      const int r = bitrev<M>(i);
+      if (r > i) {
+        C t = v[i];
+        v[i] = v[r];
+        v[r] = t;
+      }
+    }
+  }
+}
+
 template <int N> struct TeamShape;
 template <> struct TeamShape<8>   { static constexpr int G = 2,  RR = 4;  };
 template <> struct TeamShape<16>  { static constexpr int G = 4,  RR = 4;  };
@@ -119,10 +186,11 @@ struct Team {
 
   __device__ static __forceinline__ int swz(int s, int g) { return s * G + (g ^ (s / C)); }
 
-  // forward: v[r] = x[g + G r]  ->  v[j*G + q] = X[(g*C + j) + RR*q]
-  template <typename Cx>
+  // forward: v[r] = x[g + G r]  ->  v[j*G + q] = X[(g*C + j) + RR*q];
+  // NZ < RR: the caller guarantees v[NZ ..] == 0 (pruned first pass)
+  template <int NZ = RR, typename Cx>
   __device__ static __forceinline__ void forward(Cx (&v)[RR], const Cx (&tw)[RR], Cx* scr, int g) {
-    reg_dft<RR, false, 0>(v);
+    reg_dft_nz<RR, false, NZ>(v);
 #pragma unroll
     for (int s = 1; s < RR; ++s) v[s] = cmul(v[s], tw[s]);
 #pragma unroll
