@@ -385,6 +385,19 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
   __syncthreads();
 }
 
+// Ask L2 for the phasor row of column task t (rows of 128-byte lines, one per
+// thread g of the team), so that it is there when the team reaches that task.
+template <typename C, int N>
+__device__ __forceinline__ void prefetch_qrow(const FusedArgs<C>& a, const C* QA, const C* QB, int t, int g) {
+  if (t >= 2 * N) return;
+  const int QW = a.fold ? N / 2 : N;
+  const int kx = t < N ? t : t - N;
+  const C* Q = t < N ? QA : QB;
+  const C* row = Q + (size_t)(a.fold ? (kx < N / 2 ? kx : N - 1 - kx) : kx) * QW;
+  const int lines = (int)((sizeof(C) * QW + 127) / 128);
+  if (g < lines) asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(row) + 128 * g));
+}
+
 // Phase 2, joint: columns of A (tasks < N) and of B, each with its region's phasor.
 template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
@@ -403,6 +416,7 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
     const int kx = act ? (isb ? t - N : t) : 0;
     C* M = isb ? MB : MA;
     const C* Q = isb ? QB : QA;
+    prefetch_qrow<C, N>(a, QA, QB, t + NTEAM, g);
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -541,6 +555,7 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
   if (JOINT && pa && pb) {
     C* MB = M + nby * P;
+    prefetch_qrow<C, N>(a, qptr(sd.ra), qptr(sd.rb), team, g);
     joint_phase1<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
     joint_phase2<C, N, NZ>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g);
     joint_phase3<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
