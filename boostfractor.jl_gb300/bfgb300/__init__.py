@@ -289,6 +289,12 @@ class Stack:
         d = np.ascontiguousarray(distance, dtype=np.float64)
         self.h.check(_lib.lib().bf_stack_set_distance(self.h.ptr, self._s, _lib.ptr(d)))
 
+    def graph_stats(self):
+        """(solves replayed from the captured stage graph, kernels in it)."""
+        r, n = _lib._ull(), _lib._ull()
+        self.h.check(_lib.lib().bf_stack_graph_stats(self._s, ctypes.byref(r), ctypes.byref(n)))
+        return r.value, n.value
+
     def beta2_scale(self):
         X, Y = self.coords.X, self.coords.Y
         dx = X[1] - X[0] if len(X) > 1 else 1.0

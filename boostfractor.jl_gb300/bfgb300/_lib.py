@@ -80,6 +80,7 @@ _SIGS = {
     "bf_pgrid_matrices": (_c_int, [_vp, _vp, _p_dbl, _p_dbl]),
     "bf_pgrid_transformer": (_c_int, [_vp, _vp, _p_dbl, _p_dbl, _p_dbl, _p_dbl]),
     "bf_pgrid_cost": (_c_int, [_vp, _vp, _p_dbl, _p_dbl, ctypes.c_double, _p_dbl, _p_dbl]),
+    "bf_stack_graph_stats": (_c_int, [_vp, ctypes.POINTER(_ull), ctypes.POINTER(_ull)]),
     "bf_transformer_trace_back": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _c_int,
                                            _c_int, _p_dbl, _p_dbl, _c_int, _p_dbl]),
     "bf_server_create": (_c_int, [_c_int, _ull, _c_int, _c_int, ctypes.POINTER(_vp)]),

@@ -500,6 +500,13 @@ size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, in
   return std::max(fused, full) + F * 64;
 }
 
+extern "C" int bf_stack_graph_stats(bf_stack* s, unsigned long long* replays, unsigned long long* launches) {
+  if (!s || !replays || !launches) return BF_ERR_INVALID;
+  *replays = s->ws ? s->ws->graph.replays : 0;
+  *launches = s->ws && s->ws->graph.exec ? s->ws->graph.launches : 0;
+  return BF_OK;
+}
+
 extern "C" int bf_stack_set_distance(bf_handle* h, bf_stack* s, const double* distance) {
   if (!h || !s || !distance) return BF_ERR_INVALID;
   if (!all_finite(distance, s->nd)) return fail(h, BF_ERR_INVALID, "non-finite distance");
@@ -1025,12 +1032,71 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
   CK(cudaMemsetAsync(a.err, 0, sizeof(int), st));
   prof_mark(h, 1);
   const unsigned long long l1 = bf::launch_count();
-  for (size_t k = 0; k < w.stage_off.size(); ++k) {
-    a.steps = w.steps.as<StepDesc>() + w.stage_off[k];
-    int e;
-    if (fp64) e = bf::launch_fused_stage_d(N, *reinterpret_cast<bf::FusedArgs<double2>*>(&a), (int)w.stage_len[k], st);
-    else e = bf::launch_fused_stage_f(N, *reinterpret_cast<bf::FusedArgs<float2>*>(&a), (int)w.stage_len[k], st);
-    if (e) return fail(h, BF_ERR_CUDA, std::string("fused stage: ") + cudaGetErrorString((cudaError_t)e));
+  auto run_stages = [&]() -> int {
+    for (size_t k = 0; k < w.stage_off.size(); ++k) {
+      a.steps = w.steps.as<StepDesc>() + w.stage_off[k];
+      int e;
+      if (fp64) e = bf::launch_fused_stage_d(N, *reinterpret_cast<bf::FusedArgs<double2>*>(&a), (int)w.stage_len[k], st);
+      else e = bf::launch_fused_stage_f(N, *reinterpret_cast<bf::FusedArgs<float2>*>(&a), (int)w.stage_len[k], st);
+      if (e) return fail(h, BF_ERR_CUDA, std::string("fused stage: ") + cudaGetErrorString((cudaError_t)e));
+    }
+    return BF_OK;
+  };
+  // The stage launches depend only on the request kind, the batch, the
+  // precision, the workspace buffers, the handle and the stage sizes (not on
+  // the distances, which reach the kernels through the tables): the second
+  // solve with the same ones is captured into a CUDA graph and later solves,
+  // optimiser steps included, replay it.
+  std::string gkey = key + (fp64 ? "|d" : "|f");
+  {
+    const void* ptrs[] = {a.state, a.phasor, a.tilt, a.tilt_idx, a.mask, a.coefs, a.exitacc, a.addbuf,
+                          a.err, w.steps.p};
+    const long long ints[] = {nf, a.nbx, a.nby, a.nslots, a.ntab, a.fold, a.ntilt, N, (long long)fp64,
+                              (long long)w.stage_off.size(), h->device};
+    gkey.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
+    gkey.append(reinterpret_cast<const char*>(ints), sizeof(ints));
+    gkey.append(reinterpret_cast<const char*>(w.stage_off.data()), sizeof(size_t) * w.stage_off.size());
+    gkey.append(reinterpret_cast<const char*>(w.stage_len.data()), sizeof(size_t) * w.stage_len.size());
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &cap));
+  if (key.empty() || cap != cudaStreamCaptureStatusNone) {
+    // no cached plan, or the caller is capturing this stream: plain launches
+    CKS(run_stages());
+  } else if (w.graph.exec && w.graph.key == gkey) {
+    CK(cudaGraphLaunch(w.graph.exec, st));
+    bf::note_launches(w.graph.launches);
+    ++w.graph.replays;
+  } else if (w.graph.pending == gkey) {
+    w.graph.reset();
+    w.graph.pending.clear();
+    const unsigned long long c0 = bf::launch_count();
+    int rc = BF_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      rc = run_stages();   // recorded, not run
+      ce = cudaStreamEndCapture(st, &g);
+    }
+    cudaGraphExec_t ex = nullptr;
+    const bool ok = rc == BF_OK && ce == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (ok) {
+      w.graph.exec = ex;
+      w.graph.key = gkey;
+      w.graph.device = h->device;
+      w.graph.launches = bf::launch_count() - c0;
+      CK(cudaGraphLaunch(ex, st));
+    } else {
+      // capture unavailable here: clear its error and launch directly
+      cudaGetLastError();
+      h->err.clear();
+      bf::unnote_launches(bf::launch_count() - c0);   // recorded, never run
+      CKS(run_stages());
+    }
+  } else {
+    CKS(run_stages());
+    w.graph.pending = gkey;
   }
   const unsigned long long l2 = bf::launch_count();
   prof_mark(h, 2);

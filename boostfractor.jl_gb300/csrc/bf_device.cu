@@ -32,6 +32,8 @@ namespace bf {
 static thread_local unsigned long long g_launches = 0;
 unsigned long long launch_count() { return g_launches; }
 void note_launch() { ++g_launches; }
+void note_launches(unsigned long long n) { g_launches += n; }
+void unnote_launches(unsigned long long n) { g_launches -= n; }
 #define COUNT_LAUNCH() (++g_launches)
 
 // Round an FP64 complex value to complex64 so that the modulus error is as

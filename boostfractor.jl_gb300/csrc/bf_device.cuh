@@ -138,5 +138,7 @@ void init_constant_roots();  // host: fill the unit-root tables (once per device
 // Kernel launches issued by this library since load (for launch accounting).
 unsigned long long launch_count();
 void note_launch();   // count a launch made outside bf_device.cu
+void note_launches(unsigned long long n);   // kernels run by a replayed graph
+void unnote_launches(unsigned long long n); // launches recorded into a graph that never ran
 
 }  // namespace bf

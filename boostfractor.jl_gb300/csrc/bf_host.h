@@ -75,6 +75,33 @@ struct DBuf {
   template <typename T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 
+// The bounce-stage launches of one solve, captured as a CUDA graph when the
+// same launch sequence (plan, frequency batch, precision, buffers, handle)
+// comes a second time, and replayed from then on with one graph launch.
+struct StageGraph {
+  cudaGraphExec_t exec = nullptr;
+  int device = 0;
+  std::string key;      // launch sequence that exec replays
+  std::string pending;  // sequence run once uncaptured
+  unsigned long long launches = 0;
+  unsigned long long replays = 0;
+  StageGraph() = default;
+  StageGraph(const StageGraph&) = delete;
+  StageGraph& operator=(const StageGraph&) = delete;
+  void reset() {
+    if (exec) {
+      int prev = 0;
+      cudaGetDevice(&prev);
+      cudaSetDevice(device);
+      cudaGraphExecDestroy(exec);
+      cudaSetDevice(prev);
+    }
+    exec = nullptr;
+    key.clear();
+  }
+  ~StageGraph() { reset(); }
+};
+
 // Per-stack device workspace reused across solves (no allocation on the
 // steady-state path) and the cached bounce plan.
 struct Workspace {
@@ -91,6 +118,7 @@ struct Workspace {
   int tables_fp64 = -1;
   unsigned long long tables_version = ~0ull;
   long long props_per_freq = 0;  // propagations in the fused stages, per frequency
+  StageGraph graph;              // declared last: destroyed before the buffers it reads
 };
 
 struct bf_stack {

@@ -162,6 +162,13 @@ int bf_stack_create(bf_handle* h, int nd, const double* distance, const double* 
 int bf_stack_destroy(bf_handle* h, bf_stack* s);
 /* Replace the region distances of a resident stack (optimiser step). */
 int bf_stack_set_distance(bf_handle* h, bf_stack* s, const double* distance);
+/* No counterpart in the reference.  The bounce-stage launches of a fused
+ * solve are captured as a CUDA graph the second time the same launch sequence
+ * comes (same plan, frequency batch, precision, workspace and handle) and
+ * replayed by later solves, including after bf_stack_set_distance.  replays:
+ * solves served by the graph so far; launches: kernels in the graph (0 when
+ * none is held).  A stream that the caller is capturing gets plain launches. */
+int bf_stack_graph_stats(bf_stack* s, unsigned long long* replays, unsigned long long* launches);
 
 /* ---- recursive Fourier propagation -------------------------------------- */
 /* cheerleader for nf frequencies of one resident stack, batched in one solve.

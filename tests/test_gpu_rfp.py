@@ -191,6 +191,37 @@ def test_batch_equals_single(B):
     st.close()
 
 
+def test_stage_graph_replay(B):
+    """Repeated solves with the same launch sequence are captured into a CUDA
+    graph (second solve) and replayed (third on): bit-identical to the plain
+    launches, and a replay after an optimiser step (set_distance) equals a
+    fresh stack's solve at the new distances."""
+    distance, eps, tx, ty, X, _ = _stack_case(64, 3, seed=21)
+    cb, co = coords_pair(B, X)
+    sbb, _ = bdry_pair(B, cb, co, distance, eps, tx, ty)
+    st = B.Stack(sbb, cb, 0.15)
+    freqs = np.linspace(19.6e9, 20.4e9, 5)
+    try:
+        for prec in ("mixed", "fp64"):
+            runs = [st.cheerleader(freqs, nmax=25, precision=prec) for _ in range(4)]
+            for R, L, b in runs[1:]:
+                assert np.array_equal(R, runs[0][0]) and np.array_equal(b, runs[0][2])
+        replays, launches = st.graph_stats()
+        assert replays >= 4 and launches > 0
+        d2 = np.array(distance, dtype=float)
+        d2[1:-1:2] += 7e-6
+        st.set_distance(d2)
+        R2, _, b2 = st.cheerleader(freqs, nmax=25, precision="fp64")
+        assert st.graph_stats()[0] == replays + 1
+        sb_new, _ = bdry_pair(B, cb, co, d2, eps, tx, ty)
+        fresh = B.Stack(sb_new, cb, 0.15)
+        Rf, _, bf = fresh.cheerleader(freqs, nmax=25, precision="fp64")
+        fresh.close()
+        assert np.array_equal(R2, Rf) and np.array_equal(b2, bf)
+    finally:
+        st.close()
+
+
 # ------------------------------------------------- exact full-grid mode -----
 def test_amin_nonzero_and_dancer_per_bounce(B):
     distance, eps, tx, ty, X, _ = _stack_case(32, 1, seed=5)
