@@ -741,11 +741,21 @@ def run_1d(args):
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
+    clock = ClockSampler(0)
+    clock.start()
+    kern_ms = []
+    prof = np.zeros(8)
+    L.bf_set_profiling(h.ptr, 1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
+        h.check(L.bf_last_profile(h.ptr, _lib.ptr(prof)))
+        kern_ms.append(prof[1])
     torch.cuda.synchronize()
     wall = (time.perf_counter() - t0) / args.steps
+    L.bf_set_profiling(h.ptr, 0)
+    clocks = clock.stop()
+    kms = float(np.mean(kern_ms))
     # plain: the 1D transformer per configuration (frequencies batched), 32 configurations
     c1 = B.SeedCoordinateSystem(X=np.array([1e-7]), Y=np.array([1e-7]))
     m1 = B.SeedModes(c1, ThreeDim=False, handle=h)
@@ -766,13 +776,25 @@ def run_1d(args):
         errs.append(abs(b2[c, k] - ref) / ref)
     m1.close()
     h.close()
+    # FP64 roofline of k_tf1d: the explicit arithmetic of one region (complex
+    # products 6 flops, sums 2: axion term 10, boundary factors 28, propagation
+    # 12, phase argument 2 = 52 flops), not counting sincospi, over the nominal
+    # FP64 rate of GB300 (1.25 TFLOP/s; no measured figure for FP64)
+    nregions = len(eps) - 1
+    flops = 52.0 * nregions * nconf * nf
     line = {"metric": "beta2 freq-points/s (batched 1D model, 20-disk booster, spacing configurations x frequencies)",
-            "value": nconf * nf / wall, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded geometry, gap steps N(0, 10 um))",
+            "value": nconf * nf / (kms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": kms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded geometry, gap steps N(0, 10 um))",
             "config": {"workload": f"1d-20disk-{nconf}configs-{nf}f", "configs": nconf, "freqs": nf,
-                       "timing": "host wall clock around the C ABI call (host buffers in and out)"},
+                       "timing": "value: k_tf1d device time (CUDA events, inputs resident); e2e: host wall clock "
+                                 "around the C ABI call (host buffers in and out)",
+                       "l2": "no flush: 9 MB working set, compute-bound"},
             "plain_freqpts_per_s": plain, "beta2_rel_err_vs_oracle_max": float(max(errs)),
+            "roofline": {"bound": "fp64 (nominal peak)", "achieved": flops / (kms / 1000.0) / 1e12,
+                         "peak": 1.25, "unit": "TFLOP/s", "frac": flops / (kms / 1000.0) / 1e12 / 1.25,
+                         "kernel": "k_tf1d", "flops_per_region": 52, "note": "sincospi/exp not counted"},
+            "gpu_launches": args.steps, "clocks": clocks,
             "e2e": {"value": nconf * nf / wall, "unit": UNIT, "h2d_bytes_per_step": int(confs.nbytes + freqs.nbytes),
                     "d2h_bytes_per_step": int(b2.nbytes)}}
     print(json.dumps(line), flush=True)

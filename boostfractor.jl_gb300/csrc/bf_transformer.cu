@@ -1786,29 +1786,41 @@ extern "C" int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* md, int nf, c
 // with every matrix a scalar: P_j = exp(-i k0_j dz_j), T21' = s_j P_j (a_j T21 +
 // b_j T22), T22' = s_j / P_j (b_j T21 + a_j T22), axion_beam += S_j (T21 + T22)
 // emit, boost = -axion_beam / T22 (src/boost_fractor_transformer.jl:285-359).
+// GB300's FP64 rate is 1/64 of FP32, so the per-region work is kept small:
+// the boundary factors carry 1/(2 n_j) and the emission carries S_j (folded on
+// the host); the phase k0 dz = pi (2 f / c) n dz goes through sincospi, whose
+// argument reduction is exact and cheap; a lossless region (real eps, held as
+// re - 0.0im, so Im n = -0.0 and exp(Im k0 dz) = 1 exactly) needs no exp, and
+// its 1/P is conj(P).
 struct Region1D {
-  double2 a, b, inv2n, S;   // as ChainRegion
-  double2 n;                // sqrt(eps_j) of the propagated region
+  double2 a, b;   // (n_{j-1} + n_j) / (2 n_{j-1}),  (n_{j-1} - n_j) / (2 n_{j-1})
+  double2 Se;     // S_j * emit
+  double2 n;      // sqrt(eps_j) of the propagated region
 };
 
 __global__ void k_tf1d(const double* dist, int nd, const Region1D* rg, const double* freqs, int nf, int nconf,
-                       double2 emit, double2* boost, double* beta2) {
+                       double2* boost, double* beta2) {
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= (long)nconf * nf) return;
   const int c = (int)(i / nf), f = (int)(i % nf);
   const double* dz = dist + (size_t)c * nd;
-  const double kc = 2.0 * M_PI / (kC / freqs[f]);
+  const double x2 = 2.0 * freqs[f] / kC;   // 2 / lambda: k0 = pi x2 n
   double2 t21 = make_double2(0.0, 0.0), t22 = make_double2(1.0, 0.0), ax = make_double2(0.0, 0.0);
   for (int j = 1; j < nd; ++j) {
     const Region1D g = rg[j];
-    ax = bf::cadd(ax, bf::cmul(g.S, bf::cmul(bf::cadd(t21, t22), emit)));
-    const double kr = kc * g.n.x, ki = kc * g.n.y;
-    const double2 P = dexp_c(ki * dz[j], -kr * dz[j]);
-    const double2 Pi = bf::crecip(P);
+    ax = bf::cadd(ax, bf::cmul(g.Se, bf::cadd(t21, t22)));
+    double sn, cs;
+    sincospi(x2 * g.n.x * dz[j], &sn, &cs);
+    double2 P = make_double2(cs, -sn), Pi = make_double2(cs, sn);
+    if (g.n.y != 0.0) {   // uniform across the warp: every thread is at region j
+      const double m = exp(M_PI * x2 * g.n.y * dz[j]), mi = 1.0 / m;
+      P = make_double2(m * cs, -m * sn);
+      Pi = make_double2(mi * cs, mi * sn);
+    }
     const double2 u = bf::cadd(bf::cmul(g.a, t21), bf::cmul(g.b, t22));
     const double2 v = bf::cadd(bf::cmul(g.b, t21), bf::cmul(g.a, t22));
-    t21 = bf::cmul(g.inv2n, bf::cmul(u, P));
-    t22 = bf::cmul(g.inv2n, bf::cmul(v, Pi));
+    t21 = bf::cmul(u, P);
+    t22 = bf::cmul(v, Pi);
   }
   const double d = t22.x * t22.x + t22.y * t22.y;
   const double2 q = make_double2(-(ax.x * t22.x + ax.y * t22.y) / d, -(ax.y * t22.x - ax.x * t22.y) / d);
@@ -1839,15 +1851,15 @@ extern "C" int bf_transformer_1d_batch(bf_handle* h, int nconf, int nd, const do
   std::vector<Region1D> rg(nd);
   for (int j = 1; j < nd; ++j) {
     const cd nl = std::sqrt(e[j]), nr = std::sqrt(e[j - 1]);
-    rg[j].a = make_double2((nr + nl).real(), (nr + nl).imag());
-    rg[j].b = make_double2((nr - nl).real(), (nr - nl).imag());
     const cd inv = 1.0 / (2.0 * nr);
-    rg[j].inv2n = make_double2(inv.real(), inv.imag());
+    const cd a = (nr + nl) * inv, b = (nr - nl) * inv;
+    rg[j].a = make_double2(a.real(), a.imag());
+    rg[j].b = make_double2(b.real(), b.imag());
     const cd S = (1.0 / (nr * nr) - 1.0 / (nl * nl)) / 2.0;
-    rg[j].S = make_double2(S.real(), S.imag());
+    const cd Se = S * (emit ? cd(emit[0], emit[1]) : cd(1.0, 0.0));
+    rg[j].Se = make_double2(Se.real(), Se.imag());
     rg[j].n = make_double2(nl.real(), nl.imag());
   }
-  const double2 em = emit ? make_double2(emit[0], emit[1]) : make_double2(1.0, 0.0);
   const size_t npts = (size_t)nconf * nf;
   DBuf d_dist, d_rg, d_f, d_b, d_b2;
   TCKS(d_dist.alloc(h, sizeof(double) * (size_t)nconf * nd));
@@ -1859,10 +1871,23 @@ extern "C" int bf_transformer_1d_batch(bf_handle* h, int nconf, int nd, const do
   if (out_boost) TCKS(d_b.alloc(h, sizeof(double2) * npts));
   TCKS(d_b2.alloc(h, sizeof(double) * npts));
   bf::note_launch();
+  tf_mark(h, 0);
   k_tf1d<<<(unsigned)((npts + 255) / 256), 256, 0, st>>>(d_dist.as<double>(), nd, d_rg.as<Region1D>(),
-                                                          d_f.as<double>(), nf, nconf, em,
+                                                          d_f.as<double>(), nf, nconf,
                                                           out_boost ? d_b.as<double2>() : nullptr, d_b2.as<double>());
   TCK(cudaGetLastError());
+  tf_mark(h, 1);
+  if (h->profiling) {
+    TCK(cudaEventSynchronize(h->ev[1]));
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+    for (double& v : h->prof) v = 0.0;
+    h->prof[0] = ms;   // the k_tf1d launch (inputs resident)
+    h->prof[1] = ms;
+    h->prof[5] = 1;
+    h->prof[7] = nf;
+    h->prof_valid = 1;
+  }
   if (out_boost) TCK(cudaMemcpyAsync(out_boost, d_b.p, sizeof(double2) * npts, cudaMemcpyDeviceToHost, st));
   TCK(cudaMemcpyAsync(out_beta2, d_b2.p, sizeof(double) * npts, cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));

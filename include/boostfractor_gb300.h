@@ -87,6 +87,9 @@ int bf_set_stream(bf_handle* h, void* cuda_stream);
  *   [2] device ms of table setup, [3] device ms of the exit fields and beta^2,
  *   [4] bounce-stage kernel launches, [5] kernel launches of the solve,
  *   [6] propagations run in the bounce stages, [7] frequencies.
+ * bf_transformer_1d_batch records [0] = [1] = device ms of its kernel, [5] = 1,
+ * [7] = frequencies.  The transformer records [0] whole solve, [1] propagation
+ * matrices, [2] inverses, chain and boundary solve, [5] launches, [7] frequencies.
  * Returns BF_ERR_INVALID when the last solve did not record a profile.
  * No reference counterpart (the reference only times with @time). */
 int bf_set_profiling(bf_handle* h, int enable);
