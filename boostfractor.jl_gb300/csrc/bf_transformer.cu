@@ -610,7 +610,8 @@ __global__ void __launch_bounds__(256) k_chain(const C* P, const C* Pinv, const 
 // component (~48 bits): products of its hi part with the complex64 P are made
 // exact with FMA error terms and summed with TwoSum, its lo part is summed in
 // FP32, and the scalar steps use double-float arithmetic -- all on the FP32
-// pipes.  One CTA per frequency; U, V, P_j and inverse(P_j) in shared memory.
+// pipes.  One CTA of 1024 threads per frequency; U, V, P_j and inverse(P_j)
+// in shared memory.
 struct DFc { float rh, rl, ih, il; };   // complex double-float
 
 __device__ __forceinline__ void df_two_sum(float a, float b, float& s, float& e) {
@@ -675,7 +676,7 @@ __device__ __forceinline__ DFc dfc_add(DFc x, DFc y) {
   return r;
 }
 
-__global__ void __launch_bounds__(256) k_chain_df(const float2* P, const float2* Pinv, const ChainRegion* cr,
+__global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2* Pinv, const ChainRegion* cr,
                                                   int nd, int nm, const double2* emit, DFc* T21g, DFc* T22g,
                                                   double2* axg, double2* T21out, double2* T22out) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -1687,7 +1688,10 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     const size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
     TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bf::note_launch();
-    k_chain_df<<<nf, 256, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
+    // one thread per matrix entry up to 1024 (at 64 modes one CTA per frequency
+    // owns the SM's shared memory, and 32 warps hide the serial TwoSum chains)
+    const int nthr = std::min(1024, std::max(128, (nm * nm + 31) / 32 * 32));
+    k_chain_df<<<nf, nthr, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                       T21df.as<DFc>(), T22df.as<DFc>(), ax.as<double2>(), T21.as<double2>(),
                                       T22.as<double2>());
     TCK(cudaGetLastError());
