@@ -85,6 +85,41 @@ def cpu_baseline(w, nmax_s=60, workers=None):
                        f"pool wall {wall:.1f}s")
 
 
+def _cpu_tf_worker(fi):
+    """The oracle's transformer at the full transformer workload for frequency
+    index fi (the workload is regenerated from its seed in the process)."""
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, os.path.join(REPO, "boostfractor.jl_gb300"))
+    from oracle import bf_oracle as O  # the CPU baseline leg may run the oracle
+    from bfgb300 import workloads as W
+    w = W.config3_transformer()
+    t = time.perf_counter()
+    c = O.seed_coordinate_system(X=w["X"], Y=w["Y"])
+    m = O.seed_modes(c, ThreeDim=True, Mmax=w["M"], Lmax=w["L"], diskR=w["diskR"],
+                     pattern_input=w["pattern_input"], kT_arr=w["kT_arr"])
+    sb = O.seed_setup_boundaries(c, diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"],
+                                 epsilon=w["eps"].copy(), relative_tilt_x=w["relative_tilt_x"],
+                                 relative_tilt_y=w["relative_tilt_y"], relative_surfaces=w["relative_surfaces"])
+    b = O.transformer(sb, c, m, f=float(w["freqs"][fi]), diskR=w["diskR"])
+    return time.perf_counter() - t, float(np.sum(np.abs(b) ** 2))
+
+
+def cpu_baseline_transformer(nf, workers=None):
+    """The oracle's transformer on `workers` host cores, one frequency each
+    (spawned processes), at the full size; freq-points/s = workers / slowest."""
+    P = workers or os.cpu_count() or 1
+    idx = [int(i) for i in np.linspace(0, nf - 1, P).astype(int)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(P) as pool:
+        res = pool.map(_cpu_tf_worker, idx)
+    wall = time.perf_counter() - t0
+    per_point = max(r[0] for r in res)
+    return dict(value=P / per_point, unit=UNIT, cores=P, kind="port",
+                sample=f"FP64 numpy oracle transformer, {P} of the {nf} frequencies at full size "
+                       f"({P} spawned processes, one per core, mode set-up included); pool wall {wall:.1f}s")
+
+
 # --------------------------------------------------------------------------
 # clocks during the timed region
 # --------------------------------------------------------------------------
@@ -148,8 +183,24 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def simt_peaks():
+    """FP32 / FP64 / TF32 rates measured on this machine's GB300 by
+    `bench.py --workload peaks` (profiles/simt_peaks.json), or None."""
+    p = os.path.join(REPO, "profiles", "simt_peaks.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
 def measured_tf32_peak():
-    """Dense TF32 tensor peak taken as half the measured bf16 GEMM rate (burst)."""
+    """Dense TF32 tensor peak: the measured cuBLAS TF32 GEMM rate, else half the
+    measured bf16 GEMM rate (burst)."""
+    sp = simt_peaks()
+    if sp and sp.get("tf32_cublas_tflops"):
+        return float(sp["tf32_cublas_tflops"]), "measured (cuBLAS TF32 GEMM, bench.py --workload peaks)"
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
@@ -427,7 +478,11 @@ def run_transformer(args):
     # three MMAs (hi*hi, hi*lo, lo*hi) per product of the real-form GEMM
     tc_tensor = 3.0 * tc_fl / (tc_ms / 1000.0) / 1e12
     N = len(w["X"])
-    peak_fp32 = 152 * 128 * 2 * 2.07e9 / 1e12
+    sp = simt_peaks()
+    if sp and sp.get("fp32_ffma_tflops"):
+        peak_fp32, fp32_src = float(sp["fp32_ffma_tflops"]), "measured (FFMA probe, bench.py --workload peaks)"
+    else:
+        peak_fp32, fp32_src = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)"
     line = {"metric": f"beta2 freq-points/s (transformer, 20 disks + surface maps, {nm} LG modes, {N}x{N}, {nf} freqs)",
             "value": nf / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -439,8 +494,9 @@ def run_transformer(args):
             "plain_fp64_freqpts_per_s": len(sub) / t_fp64,
             "setup_s": {"modes_host": t_modes, "first_solve_with_overlaps": t_setup},
             "gpu_launches": launches,
-            "roofline": {"bound": "fp32-simt (nominal peak)", "achieved": gemm_fl / (gemm_ms / 1000.0) / 1e12,
-                         "peak": peak_fp32, "unit": "TFLOP/s",
+            "cpu_baseline": (None if args.no_cpu or args.nf else cpu_baseline_transformer(nf)),
+            "roofline": {"bound": "fp32-simt", "achieved": gemm_fl / (gemm_ms / 1000.0) / 1e12,
+                         "peak": peak_fp32, "peak_source": fp32_src, "unit": "TFLOP/s",
                          "frac": gemm_fl / (gemm_ms / 1000.0) / 1e12 / peak_fp32, "kernel": "k_cgemm_c64",
                          "phase_ms": gemm_ms / args.steps},
             "tensor_core_tf32": {
@@ -710,6 +766,98 @@ def run_serve_pgrid(args):
          "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
 
 
+def run_c1(args):
+    """The reference's own CPU-runnable case: the plain dancer, complex128,
+    mirror + 1 disk, 64x64 over 1 m, 20 GHz, 201 bounces, the default emission.
+    GPU: the FP64 dancer through the C ABI (host buffers) per call; CPU: the FP64
+    oracle's dancer on one core; the exit fields compared."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    sys.path.insert(0, REPO)
+    from oracle import bf_oracle as O
+    w = W.config1_dancer()
+    cb = B.SeedCoordinateSystem(X=w["X"], Y=w["Y"])
+    co = O.seed_coordinate_system(X=w["X"], Y=w["Y"])
+    kw = dict(diskno=1, distance=w["distance"], epsilon=w["eps"])
+    sbb = B.SeedSetupBoundaries(cb, **kw)
+    sbo = O.seed_setup_boundaries(co, **kw)
+    for _ in range(args.warmup):
+        B.dancer(0, w["nmax"], sbb, cb, f=20e9, diskR=w["diskR"])
+    torch.cuda.synchronize()
+    clock = ClockSampler(0)
+    clock.start()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        got = B.dancer(0, w["nmax"], sbb, cb, f=20e9, diskR=w["diskR"])
+        ts.append(time.perf_counter() - t0)
+    clocks = clock.stop()
+    t_gpu = float(np.median(ts))
+    t0 = time.perf_counter()
+    ref = O.dancer(0, w["nmax"], sbo, co, f=20e9, diskR=w["diskR"])
+    t_cpu = time.perf_counter() - t0
+    err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    print(json.dumps({"metric": "beta2 freq-points/s (plain dancer, complex128, 1 disk, 64x64, 201 bounces)",
+                      "value": 1.0 / t_gpu, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1000.0 * t_gpu, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f64", "data": "synthetic (the reference's own 1-disk setup)",
+                      "config": {"workload": "dancer-1disk-64-201bounces", "timing": "host wall clock per C ABI call"},
+                      "exit_field_rel_err_vs_oracle": err,
+                      "cpu_baseline": {"value": 1.0 / t_cpu, "unit": UNIT, "cores": 1, "kind": "port",
+                                       "sample": "the FP64 oracle's dancer, the whole case, one core"},
+                      "clocks": clocks}), flush=True)
+
+
+def run_peaks(args):
+    """Measured arithmetic peaks of this GPU, the denominators of the SIMT and
+    TF32 rooflines: FP32 FFMA, packed FP32x2 FFMA and FP64 DFMA from the
+    probes in boostfractor.jl_gb300/peaks/bf_peaks.cu (8 independent chains per
+    thread, 8 CTAs of 256 threads per SM, best of 5 launches), and the TF32
+    tensor-core rate of a cuBLAS 8192^3 FP32 GEMM with TF32 allowed."""
+    import ctypes
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    path = _b.build_peaks()
+    L = ctypes.CDLL(path)
+    L.bf_peak_probe.restype = ctypes.c_int
+    L.bf_peak_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    clock = ClockSampler(0)
+    clock.start()
+    out = {}
+    for name, kind, iters in (("fp32_ffma_tflops", 0, 20000), ("fp32x2_ffma2_tflops", 1, 10000), ("fp64_dfma_tflops", 2, 400)):
+        v = ctypes.c_double(0.0)
+        if L.bf_peak_probe(kind, iters, 5, 8, ctypes.byref(v)) != 0:
+            raise RuntimeError(f"peak probe {name} failed")
+        out[name] = v.value
+    torch.backends.cuda.matmul.allow_tf32 = True
+    n = 8192
+    a = torch.randn(n, n, device="cuda")
+    b = torch.randn(n, n, device="cuda")
+    for _ in range(3):
+        a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(5):
+        e0.record()
+        for _ in range(10):
+            a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 10 * 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    out["tf32_cublas_tflops"] = best
+    out["clocks"] = clock.stop()
+    out["method"] = ("FFMA/FFMA2/DFMA: hand-written probes, 8 chains per thread, SMs x 8 CTAs x 256 threads, "
+                     "best of 5; TF32: torch.matmul 8192^3 FP32 with allow_tf32, best of 5 x 10")
+    print(json.dumps({"metric": "measured arithmetic peaks", "value": out["fp32_ffma_tflops"], "unit": "TFLOP/s",
+                      "peaks": out}), flush=True)
+
+
 def run_1d(args):
     """Batched 1D model: 4096 spacing configurations of the 20-disk booster
     (each gap moved by N(0, 10 um) from the seeded geometry) x 256 frequencies
@@ -778,10 +926,14 @@ def run_1d(args):
     h.close()
     # FP64 roofline of k_tf1d: the explicit arithmetic of one region (complex
     # products 6 flops, sums 2: axion term 10, boundary factors 28, propagation
-    # 12, phase argument 2 = 52 flops), not counting sincospi, over the nominal
-    # FP64 rate of GB300 (1.25 TFLOP/s; no measured figure for FP64)
+    # 12, phase argument 2 = 52 flops), not counting sincospi, over the FP64
+    # DFMA rate measured by `bench.py --workload peaks` (nominal 1.25 TFLOP/s
+    # without it)
     nregions = len(eps) - 1
     flops = 52.0 * nregions * nconf * nf
+    sp = simt_peaks()
+    fp64_peak, fp64_src = ((float(sp["fp64_dfma_tflops"]), "measured (DFMA probe, bench.py --workload peaks)")
+                           if sp and sp.get("fp64_dfma_tflops") else (1.25, "nominal"))
     line = {"metric": "beta2 freq-points/s (batched 1D model, 20-disk booster, spacing configurations x frequencies)",
             "value": nconf * nf / (kms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": kms, "higher_is_better": True, "scaling": "weak",
@@ -791,8 +943,9 @@ def run_1d(args):
                                  "around the C ABI call (host buffers in and out)",
                        "l2": "no flush: 9 MB working set, compute-bound"},
             "plain_freqpts_per_s": plain, "beta2_rel_err_vs_oracle_max": float(max(errs)),
-            "roofline": {"bound": "fp64 (nominal peak)", "achieved": flops / (kms / 1000.0) / 1e12,
-                         "peak": 1.25, "unit": "TFLOP/s", "frac": flops / (kms / 1000.0) / 1e12 / 1.25,
+            "roofline": {"bound": "fp64", "achieved": flops / (kms / 1000.0) / 1e12,
+                         "peak": fp64_peak, "peak_source": fp64_src, "unit": "TFLOP/s",
+                         "frac": flops / (kms / 1000.0) / 1e12 / fp64_peak,
                          "kernel": "k_tf1d", "flops_per_region": 52, "note": "sincospi/exp not counted"},
             "gpu_launches": args.steps, "clocks": clocks,
             "e2e": {"value": nconf * nf / wall, "unit": UNIT, "h2d_bytes_per_step": int(confs.nbytes + freqs.nbytes),
@@ -844,7 +997,8 @@ def main():
     ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cheerleader",
-                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d"])
+                    choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d", "peaks",
+                             "c1"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
@@ -855,6 +1009,10 @@ def main():
         run_uneven(args)
     elif args.workload == "1d" and args.impl == "ours":
         run_1d(args)
+    elif args.workload == "c1" and args.impl == "ours":
+        run_c1(args)
+    elif args.workload == "peaks" and args.impl == "ours":
+        run_peaks(args)
     elif args.workload == "serve-pgrid" and args.impl == "ours":
         run_serve_pgrid(args)
     elif args.workload in ("serve", "serve-opt") and args.impl == "ours":
