@@ -41,6 +41,25 @@ def dist_env():
     return ws, rank, local
 
 
+def slowest_rank_ms(ms_local):
+    """Max over ranks of a rank's timed-region milliseconds (identity for one
+    process).  The reduction runs on the device for NCCL, on the host for gloo."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(ms_local)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(ms_local)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_total_max, steps, nf, world_size):
+    """Whole-job freq-points/s of `world_size` replicas, each solving one
+    nf-frequency request per step, timed by the slowest rank."""
+    return nf * world_size / (ms_total_max / steps / 1000.0)
+
+
 def workload(rank=0, **over):
     from bfgb300 import workloads as W
     w = W.config2_cheerleader(seed=2 + rank, **over)
@@ -301,12 +320,9 @@ def run_ours(args):
     ms_total = e0.elapsed_time(e1)
     clk = clocks.stop()
     h.set_profiling(False)
-    if ws > 1:
-        t = torch.tensor([ms_total], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = slowest_rank_ms(ms_total)
     ms_step = ms_total / args.steps
-    value = nf * ws / (ms_step / 1000.0)
+    value = replica_value(ms_total, args.steps, nf, ws)
 
     # roofline of the fused stage kernel (bytes per propagation: read + write of
     # the complex64 field, 2*N^2*8)
