@@ -626,9 +626,9 @@ static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem,
   return (int)cudaGetLastError();
 }
 
-// Register slots a box line may occupy in the pruned complex64 variants: 5 of
-// 16 (3 of 8) covers boxes up to 5/16 of the grid, the disk of radius 0.15 m
-// in the reference's 1 m window.
+// Register slots a box line may occupy in the pruned variants (complex64 for
+// N >= 64, complex128 for N = 64, 128): 5 of 16 (3 of 8) covers boxes up to
+// 5/16 of the grid, the disk of radius 0.15 m in the reference's 1 m window.
 template <int N> constexpr int pruned_slots() { return (5 * Team<N>::RR + 15) / 16; }
 
 template <typename R, int N>
@@ -645,7 +645,7 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
   const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
-  if constexpr (sizeof(R) == 4 && N >= 64) {
+  if constexpr ((sizeof(R) == 4 && N >= 64) || (sizeof(R) == 8 && (N == 64 || N == 128))) {
     if (rv <= pruned_slots<N>())
       return joint ? launch_fused_v<R, N, true, pruned_slots<N>()>(a, grid, smem_j, st)
                    : launch_fused_v<R, N, false, pruned_slots<N>()>(a, grid, smem, st);
