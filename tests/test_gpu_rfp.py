@@ -222,6 +222,19 @@ def test_stage_graph_replay(B):
         st.close()
 
 
+@pytest.mark.parametrize("n", [300, 512])
+def test_grids_beyond_the_fused_kernel(B, n):
+    """Grids the fused kernel does not take (above 256, or not a power of two
+    above 256) run the exact full-grid path: FP64 parity with the oracle."""
+    distance, eps, tx, ty, X, _ = _stack_case(n, 1, seed=n)
+    cb, co = coords_pair(B, X)
+    sbb, sbo = bdry_pair(B, cb, co, distance, eps, tx, ty)
+    refL, refR = O.cheerleader(0, 3, sbo, co, f=20.1e9, diskR=0.15, returnboth=True)
+    gotL, gotR = B.cheerleader(0, 3, sbb, cb, f=20.1e9, diskR=0.15, returnboth=True)
+    assert rel(gotR, refR) < FP64_TOL
+    assert rel(gotL, refL) < FP64_TOL
+
+
 # ------------------------------------------------- exact full-grid mode -----
 def test_amin_nonzero_and_dancer_per_bounce(B):
     distance, eps, tx, ty, X, _ = _stack_case(32, 1, seed=5)
