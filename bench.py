@@ -782,6 +782,71 @@ def run_serve_pgrid(args):
          "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
 
 
+def run_pgrid(args):
+    """One optimiser on an interpolated propagation-matrix grid: 20 disks, 256
+    frequencies, 8 Laguerre-Gauss modes, 128x128, 9 spacings, mixed precision;
+    a step is bf_pgrid_transformer at new per-disk shifts (random walk N(0, 10
+    um) inside the grid).  Device time with CUDA events on the library's
+    stream; e2e is the host wall clock of the same calls (shifts in, beta^2
+    out)."""
+    import torch
+    torch.cuda.set_device(0)
+    import build as _b
+    _b.build()
+    import bfgb300 as B
+    from bfgb300 import workloads as W
+    n, nf, ndisk, M = 128, 256, 20, 8
+    sgrid = np.linspace(-2e-4, 2e-4, 9)
+    freqs = np.linspace(19.5e9, 20.5e9, nf)
+    h = B.Handle(0)
+    stream = torch.cuda.current_stream()
+    h.set_stream(stream.cuda_stream)
+    X = W.symmetric_grid(n)
+    c = B.SeedCoordinateSystem(X=X, Y=X)
+    pats, kt = W.lg_modes(c.X, c.Y, M, 0.03, 0.15)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=M, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt, handle=h)
+    rng = np.random.default_rng(500)
+    distance, eps, tx, ty = W.booster(ndisk, rng.uniform(7.5e-3, 8.5e-3, ndisk))
+    sb = B.SeedSetupBoundaries(c, diskno=ndisk, distance=distance, epsilon=eps, relative_tilt_x=tx,
+                               relative_tilt_y=ty)
+    t0 = time.perf_counter()
+    g = B.PGrid(sb, c, modes, freqs, sgrid, precision="mixed")
+    t_create = time.perf_counter() - t0
+    shifts = [np.zeros(ndisk)]
+    for _ in range(args.warmup + args.steps):
+        shifts.append(np.clip(shifts[-1] + rng.normal(0.0, 10e-6, ndisk), sgrid[0], sgrid[-1]))
+    for k in range(args.warmup):
+        g.transformer(shifts[k])
+    torch.cuda.synchronize()
+    clock = ClockSampler(0)
+    clock.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    for k in range(args.steps):
+        g.transformer(shifts[args.warmup + k])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = (time.perf_counter() - t0) / args.steps
+    clocks = clock.stop()
+    dev_ms = e0.elapsed_time(e1) / args.steps
+    g.close()
+    modes.close()
+    h.close()
+    print(json.dumps({"metric": "beta2 freq-points/s of one optimiser on an interpolated propagation-matrix grid "
+                                "(20 disks, 256 freqs, 8 LG modes, 128x128)",
+                      "value": nf / (dev_ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": dev_ms, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "c64 matrices, double-float chain, f64 spline and solve",
+                      "data": "synthetic (seeded geometry)",
+                      "config": {"workload": "pgrid-step-20disk-256f-8LG-128", "spacings": len(sgrid),
+                                 "l2": "no flush: a step reads the grid's 2.8 MB of coefficients per frequency"},
+                      "grid_create_s": t_create,
+                      "e2e": {"value": nf / wall, "unit": UNIT, "ms_per_step": 1000.0 * wall,
+                              "h2d_bytes_per_step": 8 * ndisk, "d2h_bytes_per_step": 8 * nf + 16 * nf * M},
+                      "clocks": clocks}), flush=True)
+
+
 def run_c1(args):
     """The reference's own CPU-runnable case: the plain dancer, complex128,
     mirror + 1 disk, 64x64 over 1 m, 20 GHz, 201 bounces, the default emission.
@@ -1014,7 +1079,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cheerleader",
                     choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d", "peaks",
-                             "c1"])
+                             "c1", "pgrid"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
     ap.add_argument("--serve-seconds", type=float, default=30.0)
@@ -1025,6 +1090,8 @@ def main():
         run_uneven(args)
     elif args.workload == "1d" and args.impl == "ours":
         run_1d(args)
+    elif args.workload == "pgrid" and args.impl == "ours":
+        run_pgrid(args)
     elif args.workload == "c1" and args.impl == "ours":
         run_c1(args)
     elif args.workload == "peaks" and args.impl == "ours":

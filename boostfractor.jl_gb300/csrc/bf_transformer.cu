@@ -453,6 +453,9 @@ __global__ void k_copy_modes(C* out, const double2* pat, int nm, int npix, int r
 // registers (the column loop is unrolled, so every index is static); the
 // pivot is a warp argmax (largest |a|^2, lowest row on ties), row swaps and
 // the pivot-row broadcast are shuffles.  Rows nm..NM-1 are identity padding.
+// The pivot magnitudes and the pivot reciprocal are computed in the matrix's
+// own precision: FP32 for complex64 (a warp-wide FP64 instruction costs the
+// same with one lane active, at 1/64 of the FP32 rate), FP64 for complex128.
 template <typename C, int NM>
 __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd, int j0, int nm, int nmat) {
   using R = decltype(C().x);
@@ -472,11 +475,11 @@ __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd
   }
 #pragma unroll
   for (int c = 0; c < NM; ++c) {
-    double v = (lane >= c && lane < NM) ? bf::cabs2(a[c]) : -1.0;
+    R v = (lane >= c && lane < NM) ? a[c].x * a[c].x + a[c].y * a[c].y : R(-1);
     int p = lane;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const double vo = __shfl_xor_sync(FULL, v, o);
+      const R vo = __shfl_xor_sync(FULL, v, o);
       const int po = __shfl_xor_sync(FULL, p, o);
       if (vo > v || (vo == v && po < p)) {
         v = vo;
@@ -492,7 +495,8 @@ __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd
       b[k].y = __shfl_sync(FULL, b[k].y, src);
     }
     if (lane == c) {
-      const C inv = bf::crecip(a[c]);
+      const R d = a[c].x * a[c].x + a[c].y * a[c].y;
+      const C inv = bf::mk(a[c].x / d, -a[c].y / d);
 #pragma unroll
       for (int k = 0; k < NM; ++k) {
         a[k] = bf::cmul(a[k], inv);
