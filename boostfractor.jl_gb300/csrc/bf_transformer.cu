@@ -692,8 +692,10 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
   double2* ax = reinterpret_cast<double2*>(Qs + n2);
   DFc* em = reinterpret_cast<DFc*>(ax + nm);
   const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
-  DFc* T21 = T21g + (size_t)f * n2;
-  DFc* T22 = T22g + (size_t)f * n2;
+  // T lives in shared memory when the launch gave room for it (T21g null):
+  // the axion sum reads a row of T per step, one dependent load per entry
+  DFc* T21 = T21g ? T21g + (size_t)f * n2 : em + nm;
+  DFc* T22 = T21g ? T22g + (size_t)f * n2 : em + nm + n2;
   const DFc zero = {0.f, 0.f, 0.f, 0.f}, one = {1.f, 0.f, 0.f, 0.f};
   for (int e = tid; e < n2; e += nt) {
     T21[e] = zero;
@@ -1687,16 +1689,22 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaGetLastError());
   } else {
     DBuf T21df, T22df;
-    TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
-    TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
-    const size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
+    size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
+    const bool t_in_smem = smem + sizeof(DFc) * 2 * nm * nm <= 160 * 1024;
+    if (t_in_smem) {
+      smem += sizeof(DFc) * 2 * nm * nm;
+    } else {
+      TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
+      TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
+    }
     TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bf::note_launch();
     // one thread per matrix entry up to 1024 (at 64 modes one CTA per frequency
     // owns the SM's shared memory, and 32 warps hide the serial TwoSum chains)
     const int nthr = std::min(1024, std::max(128, (nm * nm + 31) / 32 * 32));
     k_chain_df<<<nf, nthr, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
-                                      T21df.as<DFc>(), T22df.as<DFc>(), ax.as<double2>(), T21.as<double2>(),
+                                      t_in_smem ? nullptr : T21df.as<DFc>(), t_in_smem ? nullptr : T22df.as<DFc>(),
+                                      ax.as<double2>(), T21.as<double2>(),
                                       T22.as<double2>());
     TCK(cudaGetLastError());
   }
