@@ -511,6 +511,14 @@ def run_transformer(args):
             "setup_s": {"modes_host": t_modes, "first_solve_with_overlaps": t_setup},
             "gpu_launches": launches,
             "cpu_baseline": (None if args.no_cpu or args.nf else cpu_baseline_transformer(nf)),
+            # the work of the direct formulation (overlap GEMMs over all pixels
+            # 8 nm^2 Npix per region and frequency, air-region mode FFTs, chain,
+            # inverses: ~104 GFLOP per freq-point here) at the split-TF32 rate
+            # (measured TF32 / 3); the Parseval/orbit folding executes far less
+            "alg_roofline": {"gflop_per_freq_point": 104.0, "peak_tflops": tf32_peak / 3.0,
+                             "freqpts_per_s": tf32_peak / 3.0 * 1e3 / 104.0,
+                             "frac": (nf / (ms / 1000.0)) / (tf32_peak / 3.0 * 1e3 / 104.0),
+                             "executed_gemm_tflop_per_request": gemm_fl / args.steps / 1e12},
             "roofline": {"bound": "fp32-simt", "achieved": gemm_fl / (gemm_ms / 1000.0) / 1e12,
                          "peak": peak_fp32, "peak_source": fp32_src, "unit": "TFLOP/s",
                          "frac": gemm_fl / (gemm_ms / 1000.0) / 1e12 / peak_fp32, "kernel": "k_cgemm_c64",
