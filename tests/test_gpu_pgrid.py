@@ -180,3 +180,33 @@ def test_pgrid_cost_vs_oracle(B):
         assert rel(cpl, np.abs(boost.conj() @ m_reflect) ** 2) < 1e-13
     finally:
         pg.close()
+
+
+def test_optimiser_utility_mirrors_vs_oracle(B):
+    """The reference-named mirrors: calc_propagation_matrices_grid ->
+    construct_prop_matrix_interpolation -> interpolate_prop_matrix ->
+    calc_boostfactor_modes, against the oracle's (1e-10, FP64)."""
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    itp = B.construct_prop_matrix_interpolation(
+        B.calc_propagation_matrices_grid(B.SeedSetupBoundaries(cb, **kw), cb, mb, grid, freqs), grid)
+    try:
+        sbo = O.seed_setup_boundaries(co, **kw)
+        ref_grid = O.calc_propagation_matrices_grid(sbo, co, mo, grid, freqs)
+        ref_grid[0] = 0.0   # the mirror (NaN permittivity) is not compared
+        oitp = O.construct_prop_matrix_interpolation(ref_grid, grid)
+        sh = [0.7e-4, -2.6e-4]
+        pm = B.interpolate_prop_matrix(itp, np.array(sh))
+        opm = O.interpolate_prop_matrix(oitp, sh)
+        nd = len(kw["distance"])
+        assert pm.shape == (nd, len(freqs), mo.nm, mo.nm)
+        for r in range(1, nd):
+            for f in range(len(freqs)):
+                assert rel(pm[r, f], opm[r][f]) < 1e-10
+        # the transformer on per-frequency injected matrices (the mirror's own grid values)
+        E = B.calc_boostfactor_modes(B.SeedSetupBoundaries(cb, **kw), cb, mb, freqs, pm)
+        assert E.shape == (1, mo.nm, len(freqs))
+        opm_own = [[pm[r, f] for f in range(len(freqs))] for r in range(nd)]
+        Eo = O.calc_boostfactor_modes(O.seed_setup_boundaries(co, **kw), co, mo, freqs, opm_own)
+        assert rel(E, Eo) < 1e-10
+    finally:
+        itp.close()
