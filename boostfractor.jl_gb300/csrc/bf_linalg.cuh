@@ -190,38 +190,59 @@ __device__ __forceinline__ C crecip(C v) {
 
 // In-place Gauss-Jordan inversion with partial pivoting of the n x n matrix
 // at M (row-major, leading dimension n) using the augmented buffer W
-// (n x 2n, shared memory).  One CTA.  Returns nothing; singular pivots give
-// inf/NaN like LAPACK's inv would report an error (the host checks).
+// (n x 2n, shared memory).  One CTA of up to 1024 threads; red_v / red_i hold
+// at least 160 doubles / 80 ints of shared scratch.  The pivot (largest
+// |W[p][c]|^2, lowest row on ties) is a warp-shuffle argmax, then one over
+// the warps; its reciprocal is computed once and broadcast.  Magnitudes and
+// the reciprocal use the matrix's own precision: a warp-wide FP64 instruction
+// costs the same with one lane active, at 1/64 of the FP32 rate.  Singular
+// pivots give inf/NaN like LAPACK's inv would report an error (the host
+// checks).
 template <typename C>
 __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* red_i) {
-  const int tid = threadIdx.x, nt = blockDim.x;
+  using R = decltype(C().x);
+  constexpr unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = (nt + 31) >> 5;
   const int w2 = 2 * n;
+  C* inv_s = reinterpret_cast<C*>(red_v + 64);   // the broadcast reciprocal
   for (int e = tid; e < n * w2; e += nt) {
     const int r = e / w2, c = e % w2;
-    W[e] = c < n ? M[r * n + c] : mk((decltype(C().x))(c - n == r ? 1 : 0), (decltype(C().x))0);
+    W[e] = c < n ? M[r * n + c] : mk((R)(c - n == r ? 1 : 0), (R)0);
   }
   __syncthreads();
   for (int c = 0; c < n; ++c) {
     // pivot: row p >= c with the largest |W[p][c]|
-    double best = -1.0;
-    int bi = c;
+    R best = (R)-1;
+    int bi = n;
     for (int r = c + tid; r < n; r += nt) {
-      const double v = cabs2(W[r * w2 + c]);
+      const C w = W[r * w2 + c];
+      const R v = w.x * w.x + w.y * w.y;
       if (v > best) { best = v; bi = r; }
     }
-    red_v[tid] = best;
-    red_i[tid] = bi;
-    __syncthreads();
-    for (int s = nt / 2; s > 0; s >>= 1) {
-      if (tid < s) {
-        if (red_v[tid + s] > red_v[tid] || (red_v[tid + s] == red_v[tid] && red_i[tid + s] < red_i[tid])) {
-          red_v[tid] = red_v[tid + s];
-          red_i[tid] = red_i[tid + s];
-        }
-      }
-      __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const R vo = __shfl_xor_sync(FULL, best, o);
+      const int io = __shfl_xor_sync(FULL, bi, o);
+      if (vo > best || (vo == best && io < bi)) { best = vo; bi = io; }
     }
-    const int p = red_i[0];
+    if (lane == 0) {
+      red_v[warp] = (double)best;
+      red_i[warp] = bi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double v = lane < nwarp ? red_v[lane] : -1.0;
+      int i = lane < nwarp ? red_i[lane] : n;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double vo = __shfl_xor_sync(FULL, v, o);
+        const int io = __shfl_xor_sync(FULL, i, o);
+        if (vo > v || (vo == v && io < i)) { v = vo; i = io; }
+      }
+      if (lane == 0) red_i[64] = i < n ? i : c;
+    }
+    __syncthreads();
+    const int p = red_i[64];
     if (p != c)
       for (int k = tid; k < w2; k += nt) {
         C t = W[c * w2 + k];
@@ -229,8 +250,13 @@ __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* re
         W[p * w2 + k] = t;
       }
     __syncthreads();
-    const C inv = crecip(W[c * w2 + c]);
+    if (tid == 0) {
+      const C w = W[c * w2 + c];
+      const R d = w.x * w.x + w.y * w.y;
+      *inv_s = mk(w.x / d, -w.y / d);
+    }
     __syncthreads();
+    const C inv = *inv_s;
     for (int k = tid; k < w2; k += nt) W[c * w2 + k] = cmul(W[c * w2 + k], inv);
     __syncthreads();
     // eliminate column c from every other row
@@ -242,7 +268,7 @@ __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* re
     }
     __syncthreads();
     for (int r = tid; r < n; r += nt)
-      if (r != c) W[r * w2 + c] = mk((decltype(C().x))0, (decltype(C().x))0);
+      if (r != c) W[r * w2 + c] = mk((R)0, (R)0);
     __syncthreads();
   }
   for (int e = tid; e < n * n; e += nt) M[e] = W[(e / n) * w2 + n + (e % n)];
