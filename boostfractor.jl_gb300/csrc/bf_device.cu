@@ -162,7 +162,6 @@ struct FusedCtx {
   using T = Team<N>;
   static constexpr int G = T::G, RR = T::RR, CC = T::C;
   static constexpr int P = fused_pitch<N>();
-  static constexpr int NTEAM = kFusedThreads / G;
 };
 
 // Phase 1 of one propagation: forward FFT along x of every box row.  Fields
@@ -173,7 +172,8 @@ template <typename C, int N, int NZ>
 __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int slot, int exitk, C* M,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby;
   const C* src = a.state + ((size_t)f * a.nslots + slot) * (size_t)(nby * nbx);
   double2* acc = exitk >= 0 ? a.exitacc + ((size_t)exitk * a.nfreq + f) * (size_t)(nby * nbx) : nullptr;
@@ -218,7 +218,8 @@ template <typename C, int N, int NZ>
 __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, C* M, C* scr,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
@@ -277,7 +278,8 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
                                              bool prop_is_b, C* M, C* scr, C* obuf,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby;
   const size_t plane = (size_t)nby * nbx;
   const int ti = a.tilt_idx[region];
@@ -346,7 +348,8 @@ template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
   const int rv = (nbx + G - 1) / G;
   for (int base = 0; base < ntask; base += NTEAM) {
@@ -405,11 +408,11 @@ template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
-  static_assert((2 * N) % NTEAM == 0 || NTEAM > 2 * N, "column tasks");
   for (int base = 0; base < 2 * N; base += NTEAM) {
     const int t = base + team;
     const bool act = t < 2 * N;
@@ -468,7 +471,8 @@ template <typename C, int N, int NZ>
 __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
-  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P, NTEAM = X::NTEAM;
+  constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
   const size_t plane = (size_t)nby * nbx;
   const int tiA = a.tilt_idx[sd.ra], tiB = a.tilt_idx[sd.rb];
@@ -534,8 +538,8 @@ __device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc&
 // shared memory).  NZ: box lines occupy at most NZ of a thread's RR register
 // slots (x = g + G r < nbx, y = g + G r < nby only for r < NZ), so the first
 // forward pass is pruned and the inverse stores only NZ slots.
-template <typename R, int N, bool JOINT, int NZ>
-__global__ void __launch_bounds__(kFusedThreads, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
+template <typename R, int N, bool JOINT, int NZ, int THREADS>
+__global__ void __launch_bounds__(THREADS, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
 k_fused_stage(FusedArgs<cplx_t<R>> a) {
   using C = cplx_t<R>;
   using X = FusedCtx<C, N>;
@@ -584,8 +588,8 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
 }
 
 template <int N>
-static size_t fused_smem_for(int nby, size_t csz, int tiles = 1) {
-  const size_t nteam = kFusedThreads / Team<N>::G;
+static size_t fused_smem_for(int nby, size_t csz, int tiles = 1, int threads = kFusedThreads) {
+  const size_t nteam = threads / Team<N>::G;
   return kSmemHeader + csz * ((size_t)tiles * nby * fused_pitch<N>() + nteam * Team<N>::SCR);
 }
 
@@ -617,12 +621,12 @@ bool fused_supported(int N, int nbx, int nby, bool fp64) {
 // Shared memory of one SM (bytes) and what the driver reserves per CTA.
 static const size_t kSmemPerSM = 228 * 1024, kSmemReservedPerCta = 1024;
 
-template <typename R, int N, bool JOINT, int NZ>
+template <typename R, int N, bool JOINT, int NZ, int THREADS = kFusedThreads>
 static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ, THREADS>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_fused_stage<R, N, JOINT, NZ><<<grid, kFusedThreads, smem, st>>>(a);
+  k_fused_stage<R, N, JOINT, NZ, THREADS><<<grid, THREADS, smem, st>>>(a);
   return (int)cudaGetLastError();
 }
 
@@ -645,6 +649,14 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
   const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
+  if constexpr (sizeof(R) == 4 && N == 256) {
+    // one CTA per SM (the 256-point row tile): 512 threads (32 teams, at most
+    // 128 registers each) when the team scratch still fits beside the tile
+    const size_t smem512 = fused_smem_for<N>(a.nby, csz, 1, 512);
+    if (!joint && smem512 <= kMaxSmem)
+      return rv <= pruned_slots<N>() ? launch_fused_v<R, N, false, pruned_slots<N>(), 512>(a, grid, smem512, st)
+                                     : launch_fused_v<R, N, false, Team<N>::RR, 512>(a, grid, smem512, st);
+  }
   if constexpr ((sizeof(R) == 4 && N >= 64) || (sizeof(R) == 8 && (N == 64 || N == 128))) {
     if (rv <= pruned_slots<N>())
       return joint ? launch_fused_v<R, N, true, pruned_slots<N>()>(a, grid, smem_j, st)

@@ -160,7 +160,7 @@ def test_dancer_config1_fp64_vs_oracle(B):
     assert abs(b_got - b_ref) / b_ref < FP64_TOL
 
 
-@pytest.mark.parametrize("n,ndisk", [(64, 3), (128, 2)])
+@pytest.mark.parametrize("n,ndisk", [(64, 3), (128, 2), (256, 2)])
 def test_cheerleader_mixed_beta2(B, n, ndisk):
     distance, eps, tx, ty, X, surf = _stack_case(n, ndisk, seed=3 * n + ndisk)
     cb, co = coords_pair(B, X)
