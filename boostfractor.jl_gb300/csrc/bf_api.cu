@@ -465,7 +465,7 @@ size_t bf_stack_device_bytes(const bf_stack* s) {
   if (s->d_surf) b += sizeof(double2) * s->nd * npix;
   if (const Workspace* w = s->ws) {
     for (const DBuf* d : {&w->freq, &w->reg, &w->phasor, &w->tidx, &w->tregs, &w->tilt, &w->init, &w->state,
-                          &w->add, &w->coef, &w->exitacc, &w->steps, &w->tmp, &w->beta, &w->exit_full[0],
+                          &w->add, &w->coef, &w->exitacc, &w->steps, &w->tmp, &w->beta, &w->mg, &w->exit_full[0],
                           &w->exit_full[1], &w->direct[0], &w->direct[1]})
       b += dbuf_bytes(*d);
   }
@@ -495,7 +495,10 @@ size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, in
   }
   if (prop_kind == BF_PROP_1D) return F * (16 * 4 * nd * npix + 64);
   const size_t slots = 2 * nd + 2;
-  const size_t fused = F * (csz * (slots * plane + nd * npix + nd * plane) + 16 * (2 * plane + 3 * npix));
+  // split-phase row tiles: at most (SMs = 160 here, an upper bound) step x
+  // frequency pairs of two nby x (N + 2) tiles
+  const size_t split = 160 * 2 * (size_t)s->nby * (s->nx + 2) * csz;
+  const size_t fused = F * (csz * (slots * plane + nd * npix + nd * plane) + 16 * (2 * plane + 3 * npix)) + split;
   const size_t full = F * (csz * (slots + 1) * npix + 16 * 3 * npix);
   return std::max(fused, full) + F * 64;
 }
@@ -1030,6 +1033,18 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
   a.addbuf = w.nadd ? w.add.as<C>() : nullptr;
   a.err = reinterpret_cast<int*>(h->d_scalar + 1);
   CK(cudaMemsetAsync(a.err, 0, sizeof(int), st));
+  // row tiles for the stages that take the split-phase path (fewer steps x
+  // frequencies than SMs: short stacks, few frequencies, the wavefront's ends)
+  {
+    size_t split_len = 0;
+    for (size_t len : w.stage_len)
+      if (bf::split_stage((int)len, nf)) split_len = std::max(split_len, len);
+    a.mg = nullptr;
+    if (split_len && N >= 64) {
+      CKS(w.mg.ensure(h, bf::split_tile_bytes(N, s->nby, nf, (int)split_len, fp64)));
+      a.mg = w.mg.as<C>();
+    }
+  }
   prof_mark(h, 1);
   const unsigned long long l1 = bf::launch_count();
   auto run_stages = [&]() -> int {
@@ -1050,7 +1065,7 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
   std::string gkey = key + (fp64 ? "|d" : "|f");
   {
     const void* ptrs[] = {a.state, a.phasor, a.tilt, a.tilt_idx, a.mask, a.coefs, a.exitacc, a.addbuf,
-                          a.err, w.steps.p};
+                          a.err, w.steps.p, a.mg};
     const long long ints[] = {nf, a.nbx, a.nby, a.nslots, a.ntab, a.fold, a.ntilt, N, (long long)fp64,
                               (long long)w.stage_off.size(), h->device};
     gkey.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));

@@ -168,12 +168,12 @@ struct FusedCtx {
 // are stored pre-masked, so only register slots r < ceil(nbx/G) can hold box
 // pixels.  A slot feeding an exit adds its (masked) input to the FP64 exit
 // accumulator on the way.
-template <typename C, int N, int NZ>
+template <typename C, int N, int NZ, int NT>
 __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int slot, int exitk, C* M,
                                              C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
+  constexpr int NTEAM = NT;
   const int nbx = a.nbx, nby = a.nby;
   const C* src = a.state + ((size_t)f * a.nslots + slot) * (size_t)(nby * nbx);
   double2* acc = exitk >= 0 ? a.exitacc + ((size_t)exitk * a.nfreq + f) * (size_t)(nby * nbx) : nullptr;
@@ -214,12 +214,12 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
 
 // Phase 2: per column kx, forward FFT along y, phasor, inverse FFT along y,
 // in place in M (only the nby box rows are read and written).
-template <typename C, int N, int NZ>
+template <typename C, int N, int NZ, int NT>
 __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, C* M, C* scr,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
+  constexpr int NTEAM = NT;
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
@@ -273,13 +273,13 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
 // Phase 3: inverse FFT along x of every box row, tilt/surface map, then the
 // epilogue: store the propagated field into obuf (first of two propagations)
 // or apply the boundary mix and write the new (masked) fields.
-template <typename C, int N, bool MIX, int NZ>
+template <typename C, int N, bool MIX, int NZ, int NT>
 __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, int region,
                                              bool prop_is_b, C* M, C* scr, C* obuf,
                                              const C (&tw)[Team<N>::RR], int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
+  constexpr int NTEAM = NT;
   const int nbx = a.nbx, nby = a.nby;
   const size_t plane = (size_t)nby * nbx;
   const int ti = a.tilt_idx[region];
@@ -337,24 +337,29 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
   }
 }
 
-// ---- joint step: both slots propagated, processed together ----------------
+// ---- joint step: both slots processed together ------------------------------
 // The rows of A and of B form one task list (2 nby rows), and so do their
 // columns (2 N), so the teams stay busy where a single field's nby rows leave
-// most of them idle in the last round; the propagated fields stay in shared
-// memory (MA, MB) and the boundary mix runs as one pass over the box.
+// most of them idle in the last round; the propagated fields stay in the row
+// tiles MA, MB and the boundary mix runs as one pass over the box.  A team
+// takes the tasks t0 + team, t0 + team + ts, ... (the fused kernel: t0 = 0,
+// ts = its teams; the split-phase kernels spread the tasks over CTAs); the
+// tasks of a slot that is not propagated (pa / pb false) are skipped.
 
 // Phase 1, joint: forward FFT along x of the box rows of A (tasks < nby) and B.
-template <typename C, int N, int NZ>
+template <typename C, int N, int NZ, int NT, bool SPLIT>
 __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
-                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
+                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts,
+                                             bool pa, bool pb) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
   const int rv = (nbx + G - 1) / G;
-  for (int base = 0; base < ntask; base += NTEAM) {
+  // the fused kernel's joint steps: all tasks of the CTA, both slots propagated
+  const int T0 = SPLIT ? t0 : 0, TS = SPLIT ? ts : NT;
+  for (int base = T0; base < ntask; base += TS) {
     const int t = base + team;
-    const bool act = t < ntask;
+    const bool act = t < ntask && (!SPLIT || (t >= nby ? pb : pa));
     if (!__any_sync(0xffffffffu, act)) continue;
     const bool isb = act && t >= nby;
     const int y = act ? (isb ? t - nby : t) : 0;
@@ -392,36 +397,38 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
 
 // Ask L2 for the phasor row of column task t (rows of 128-byte lines, one per
 // thread g of the team), so that it is there when the team reaches that task.
-template <typename C, int N>
+// QA / QB are null for a slot that is not propagated.
+template <typename C, int N, bool MAYBE_NULL>
 __device__ __forceinline__ void prefetch_qrow(const FusedArgs<C>& a, const C* QA, const C* QB, int t, int g) {
   if (t >= 2 * N) return;
   const int QW = a.fold ? N / 2 : N;
   const int kx = t < N ? t : t - N;
   const C* Q = t < N ? QA : QB;
+  if (MAYBE_NULL && !Q) return;
   const C* row = Q + (size_t)(a.fold ? (kx < N / 2 ? kx : N - 1 - kx) : kx) * QW;
   const int lines = (int)((sizeof(C) * QW + 127) / 128);
   if (g < lines) asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char*>(row) + 128 * g));
 }
 
 // Phase 2, joint: columns of A (tasks < N) and of B, each with its region's phasor.
-template <typename C, int N, int NZ>
+template <typename C, int N, int NZ, int NT, bool SPLIT>
 __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
-                                             const C (&tw)[Team<N>::RR], int team, int g) {
+                                             const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
-  for (int base = 0; base < 2 * N; base += NTEAM) {
+  const int T0 = SPLIT ? t0 : 0, TS = SPLIT ? ts : NT;
+  for (int base = T0; base < 2 * N; base += TS) {
     const int t = base + team;
-    const bool act = t < 2 * N;
+    const bool act = t < 2 * N && (!SPLIT || (t >= N ? QB : QA) != nullptr);
     if (!__any_sync(0xffffffffu, act)) continue;
     const bool isb = act && t >= N;
     const int kx = act ? (isb ? t - N : t) : 0;
     C* M = isb ? MB : MA;
     const C* Q = isb ? QB : QA;
-    prefetch_qrow<C, N>(a, QA, QB, t + NTEAM, g);
+    prefetch_qrow<C, N, SPLIT>(a, QA, QB, t + TS, g);
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -467,21 +474,22 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
 // Phase 3, joint: inverse FFT along x of the box rows of A and B, times the
 // region's tilt/surface map, written back in place into the row's first nbx
 // entries (the team's exchange has already consumed the row).
-template <typename C, int N, int NZ>
+template <typename C, int N, int NZ, int NT, bool SPLIT>
 __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
-                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
+                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts,
+                                             bool pa, bool pb) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
-  const int NTEAM = blockDim.x / G;
   const int nbx = a.nbx, nby = a.nby, ntask = 2 * nby;
   const size_t plane = (size_t)nby * nbx;
-  const int tiA = a.tilt_idx[sd.ra], tiB = a.tilt_idx[sd.rb];
+  const int tiA = (!SPLIT || pa) ? a.tilt_idx[sd.ra] : -1, tiB = (!SPLIT || pb) ? a.tilt_idx[sd.rb] : -1;
   const C* tA = tiA >= 0 ? a.tilt + ((size_t)f * a.ntilt + tiA) * plane : nullptr;
   const C* tB = tiB >= 0 ? a.tilt + ((size_t)f * a.ntilt + tiB) * plane : nullptr;
   const int rv = (nbx + G - 1) / G;
-  for (int base = 0; base < ntask; base += NTEAM) {
+  const int T0 = SPLIT ? t0 : 0, TS = SPLIT ? ts : NT;
+  for (int base = T0; base < ntask; base += TS) {
     const int t = base + team;
-    const bool act = t < ntask;
+    const bool act = t < ntask && (!SPLIT || (t >= nby ? pb : pa));
     if (!__any_sync(0xffffffffu, act)) continue;
     const bool isb = act && t >= nby;
     const int y = act ? (isb ? t - nby : t) : 0;
@@ -507,11 +515,12 @@ __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDe
   __syncthreads();
 }
 
-// Boundary mix of a joint step over the whole box: A' = cAA A~ + cAB B~ (+ add),
-// B' = cBA A~ + cBB B~, stored masked.
+// Boundary mix of a step over the box: A' = cAA A~ + cAB B~ (+ add),
+// B' = cBA A~ + cBB B~, stored masked; X~ is the propagated field (row tile)
+// of a propagated slot, else the slot's stored field.  Pixels i0, i0 + is, ...
 template <typename C, int N>
 __device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc& sd, int f, const C* MA,
-                                          const C* MB) {
+                                          const C* MB, bool pa, bool pb, int i0, int is) {
   constexpr int P = FusedCtx<C, N>::P;
   const int nbx = a.nbx, nby = a.nby;
   const size_t plane = (size_t)nby * nbx;
@@ -520,9 +529,10 @@ __device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc&
   const C* add = sd.addA >= 0 ? a.addbuf + (size_t)sd.addA * plane : nullptr;
   const double2* cf = a.coefs + 4 * sd.coef;
   const C cAA = from_d<C>(cf[0]), cAB = from_d<C>(cf[1]), cBA = from_d<C>(cf[2]), cBB = from_d<C>(cf[3]);
-  for (int i = threadIdx.x; i < (int)plane; i += blockDim.x) {
+  for (int i = i0; i < (int)plane; i += is) {
     const int y = i / nbx, x = i - y * nbx;
-    const C A = MA[y * P + x], B = MB[y * P + x];
+    const C A = pa ? MA[y * P + x] : (stA ? stA[i] : czero<C>());
+    const C B = pb ? MB[y * P + x] : (stB ? stB[i] : czero<C>());
     const bool in = a.mask[i] != 0;
     if (stA) {
       C o = cadd(cmul(cAA, A), cmul(cAB, B));
@@ -561,31 +571,107 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
   if (JOINT && pa && pb) {
     C* MB = M + nby * P;
-    prefetch_qrow<C, N>(a, qptr(sd.ra), qptr(sd.rb), team, g);
-    joint_phase1<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
-    joint_phase2<C, N, NZ>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g);
-    joint_phase3<C, N, NZ>(a, sd, f, M, MB, scr, tw, team, g);
-    joint_mix<C, N>(a, sd, f, M, MB);
+    constexpr int nteam = THREADS / G;
+    prefetch_qrow<C, N, false>(a, qptr(sd.ra), qptr(sd.rb), team, g);
+    joint_phase1<C, N, NZ, THREADS / G, false>(a, sd, f, M, MB, scr, tw, team, g, 0, nteam, true, true);
+    joint_phase2<C, N, NZ, THREADS / G, false>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g, 0, nteam);
+    joint_phase3<C, N, NZ, THREADS / G, false>(a, sd, f, M, MB, scr, tw, team, g, 0, nteam, true, true);
+    joint_mix<C, N>(a, sd, f, M, MB, true, true, threadIdx.x, blockDim.x);
   } else if (pa && pb) {
     // A~ is parked in the A slot itself until the boundary mix
     C* obuf = a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * a.nbx);
-    fused_phase1<C, N, NZ>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, false, NZ>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, false, NZ, THREADS / G>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
     __syncthreads();
-    fused_phase1<C, N, NZ>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
   } else if (pa) {
-    fused_phase1<C, N, NZ>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
   } else if (pb) {
-    fused_phase1<C, N, NZ>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
   }
 }
+
+// ---- split-phase stage: for stages with fewer steps x frequencies than SMs --
+// The four phases of a step (forward rows, columns, inverse rows, boundary
+// mix) run as four launches whose tasks are spread over blockIdx.z, so a
+// stage with a handful of steps (one frequency, a short stack) still spreads
+// its FFT work over many SMs.  The row tiles of step s, frequency f live in
+// global memory at a.mg + (s nfreq + f) 2 nby P (A, then B) and stay in L2.
+constexpr int kSplitThreads = 64;
+
+template <typename R, int N, int NZ>
+__global__ void __launch_bounds__(kSplitThreads) k_split_phase(FusedArgs<cplx_t<R>> a, int phase) {
+  using C = cplx_t<R>;
+  using X = FusedCtx<C, N>;
+  constexpr int G = X::G, RR = X::RR, P = X::P;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int tid = threadIdx.x, team = tid / G, g = tid % G, nteam = blockDim.x / G;
+  const StepDesc sd = a.steps[blockIdx.x];
+  const int f = blockIdx.y;
+  C* MA = a.mg + ((size_t)blockIdx.x * a.nfreq + f) * 2 * (size_t)a.nby * P;
+  C* MB = MA + (size_t)a.nby * P;
+  const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
+  if (phase == 3) {
+    joint_mix<C, N>(a, sd, f, MA, MB, pa, pb, blockIdx.z * blockDim.x + tid, gridDim.z * blockDim.x);
+    return;
+  }
+  C* scr = reinterpret_cast<C*>(smem_raw) + team * X::T::SCR;
+  C tw[RR];
+  team_twiddles<N>(tw, g);
+  const int t0 = blockIdx.z * nteam, ts = gridDim.z * nteam;
+  if (phase == 0) {
+    joint_phase1<C, N, NZ, kSplitThreads / G, true>(a, sd, f, MA, MB, scr, tw, team, g, t0, ts, pa, pb);
+  } else if (phase == 1) {
+    const int QW = a.fold ? N / 2 : N;
+    const C* QA = pa ? a.phasor + ((size_t)f * a.ntab + sd.ra) * (size_t)(QW * QW) : nullptr;
+    const C* QB = pb ? a.phasor + ((size_t)f * a.ntab + sd.rb) * (size_t)(QW * QW) : nullptr;
+    joint_phase2<C, N, NZ, kSplitThreads / G, true>(a, QA, QB, MA, MB, scr, tw, team, g, t0, ts);
+  } else {
+    joint_phase3<C, N, NZ, kSplitThreads / G, true>(a, sd, f, MA, MB, scr, tw, team, g, t0, ts, pa, pb);
+  }
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+  }
+  return n;
+}
+
+template <typename R, int N, int NZ>
+static int launch_split(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
+  using T = Team<N>;
+  const int nteam = kSplitThreads / T::G;
+  const size_t smem = sizeof(cplx_t<R>) * nteam * T::SCR;
+  const int zr = (2 * a.nby + nteam - 1) / nteam, zc = (2 * N + nteam - 1) / nteam;
+  const int zm = (a.nbx * a.nby + kSplitThreads - 1) / kSplitThreads;
+  const int z[4] = {zr, zc, zr, zm};
+  for (int ph = 0; ph < 4; ++ph) {
+    COUNT_LAUNCH();
+    k_split_phase<R, N, NZ><<<dim3(nsteps, a.nfreq, z[ph]), kSplitThreads, ph == 3 ? 0 : smem, st>>>(a, ph);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
+  return 0;
+}
+
+// Bytes of the split-phase row tiles for a stage of `nsteps` steps.
+size_t split_tile_bytes(int N, int nby, int nfreq, int nsteps, bool fp64) {
+  return (size_t)nsteps * nfreq * 2 * nby * (N + 2) * (fp64 ? 16 : 8);
+}
+
+// Whether a stage of `nsteps` steps x `nfreq` frequencies takes the split path.
+bool split_stage(int nsteps, int nfreq) { return (long long)nsteps * nfreq < sm_count(); }
 
 template <int N>
 static size_t fused_smem_for(int nby, size_t csz, int tiles = 1, int threads = kFusedThreads) {
@@ -647,6 +733,11 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
                      (size_t)ctas * (smem + kSmemReservedPerCta) <= kSmemPerSM;
   constexpr int G = Team<N>::G, RR = Team<N>::RR;
   const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
+  if (a.mg && split_stage(nsteps, a.nfreq) && N >= 64) {
+    if constexpr ((sizeof(R) == 4 && N >= 64) || (sizeof(R) == 8 && (N == 64 || N == 128)))
+      if (rv <= pruned_slots<N>()) return launch_split<R, N, pruned_slots<N>()>(a, nsteps, st);
+    return launch_split<R, N, RR>(a, nsteps, st);
+  }
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
   if constexpr (sizeof(R) == 4 && N == 256) {

@@ -43,6 +43,7 @@ struct FusedArgs {
   const C* addbuf;                // [add][nby][nbx] (frequency independent)
   const StepDesc* steps;          // this stage
   int* err;                       // set to 1 if a bounded wait gave up
+  C* mg;                          // row tiles of the split-phase path [step][f][2][nby][N+2], or null
 };
 
 // Launch the fused stage kernel (templated on the grid size N and the field
@@ -51,6 +52,10 @@ int launch_fused_stage_f(int N, const FusedArgs<float2>& a, int nsteps, cudaStre
 int launch_fused_stage_d(int N, const FusedArgs<double2>& a, int nsteps, cudaStream_t st);
 size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64);
 bool fused_supported(int N, int nbx, int nby, bool fp64);
+// Split-phase path (stages with fewer steps x frequencies than SMs): the row
+// tiles it needs for a stage of nsteps steps, and whether a stage takes it.
+size_t split_tile_bytes(int N, int nby, int nfreq, int nsteps, bool fp64);
+bool split_stage(int nsteps, int nfreq);
 
 // ---- split-TF32 tensor-core GEMM (bf_tcgemm.cu) --------------------------
 // planes[z][m][n] (FP32) = sum over the z-th of `splits` K slices of

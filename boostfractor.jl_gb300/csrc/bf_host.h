@@ -105,7 +105,7 @@ struct StageGraph {
 // Per-stack device workspace reused across solves (no allocation on the
 // steady-state path) and the cached bounce plan.
 struct Workspace {
-  DBuf freq, reg, phasor, tidx, tregs, tilt, init, state, add, coef, exitacc, steps, tmp, beta;
+  DBuf freq, reg, phasor, tidx, tregs, tilt, init, state, add, coef, exitacc, steps, tmp, beta, mg;
   DBuf exit_full[2], direct[2];
   std::string plan_key;  // solver/nmax/emission of the cached plan
   std::vector<size_t> stage_off, stage_len;
