@@ -191,6 +191,25 @@ def test_batch_equals_single(B):
     st.close()
 
 
+def test_fused_batch_equals_split_single(B):
+    """A batch large enough for the fused stage kernel (steps x frequencies >=
+    SMs) and the same frequencies solved one at a time (split-phase stages)
+    run the same per-pixel arithmetic: identical results."""
+    distance, eps, tx, ty, X, _ = _stack_case(128, 3, seed=17)
+    cb, co = coords_pair(B, X)
+    sbb, _ = bdry_pair(B, cb, co, distance, eps, tx, ty)
+    st = B.Stack(sbb, cb, 0.15)
+    freqs = np.linspace(19.5e9, 20.5e9, 160)
+    try:
+        for prec in ("mixed", "fp64"):
+            Rb, _, bb = st.cheerleader(freqs, nmax=12, precision=prec)
+            for k in (0, 77, 159):
+                R1, _, b1 = st.cheerleader(freqs[k:k + 1], nmax=12, precision=prec)
+                assert np.array_equal(R1[0], Rb[k]) and b1[0] == bb[k], (prec, k)
+    finally:
+        st.close()
+
+
 def test_stage_graph_replay(B):
     """Repeated solves with the same launch sequence are captured into a CUDA
     graph (second solve) and replayed (third on): bit-identical to the plain
