@@ -863,11 +863,19 @@ __global__ void k_line_dft(C* data, int nx, int ny, int axis, int inverse) {
   const size_t stride = axis == 0 ? 1 : nx;
   const size_t off = axis == 0 ? (size_t)line * nx : (size_t)line;
   const double sgn = inverse ? 2.0 : -2.0;
+  // power-of-two lengths up to 1024 take the unit roots from the constant
+  // table (FP64, exactly symmetric) instead of one FP64 sincospi per entry
+  const bool table = (n & (n - 1)) == 0 && n <= 1024;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     buf0[i] = data[base + off + i * stride];
-    double s, c;
-    sincospi(sgn * (double)i / (double)n, &s, &c);
-    tw[i] = from_d<C>(make_double2(c, s));
+    if (table) {
+      const double2 r = c_root1024_d[i * (1024 / n)];   // exp(-2 pi i k / n)
+      tw[i] = from_d<C>(make_double2(r.x, inverse ? -r.y : r.y));
+    } else {
+      double s, c;
+      sincospi(sgn * (double)i / (double)n, &s, &c);
+      tw[i] = from_d<C>(make_double2(c, s));
+    }
   }
   __syncthreads();
   if ((n & (n - 1)) == 0) {
