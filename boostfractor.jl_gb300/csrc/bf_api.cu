@@ -48,7 +48,9 @@ int bf_fail(bf_handle* h, int code, const std::string& msg) { return fail(h, cod
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \
     if (e_ != cudaSuccess)                                                               \
-      return fail(h, BF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+      return fail(h, BF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                  std::string(__FILE__).substr(std::string(__FILE__).find_last_of('/') + 1) + ":" +  \
+                  std::to_string(__LINE__) + ")");   \
   } while (0)
 #define CKL(call)                                                                        \
   do {                                                                                   \

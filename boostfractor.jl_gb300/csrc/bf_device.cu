@@ -712,10 +712,14 @@ bool fused_supported(int N, int nbx, int nby, bool fp64) {
 // Shared memory of one SM (bytes) and what the driver reserves per CTA.
 static const size_t kSmemPerSM = 228 * 1024, kSmemReservedPerCta = 1024;
 
+// The dynamic shared-memory limit of a kernel is raised to the per-block
+// maximum, the same value for every launch: launches of one kernel with
+// different sizes from several host threads (the serving engine's workers)
+// must not lower it under one another.
 template <typename R, int N, bool JOINT, int NZ, int THREADS = kFusedThreads>
 static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ, THREADS>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
   if (e != cudaSuccess) return (int)e;
   k_fused_stage<R, N, JOINT, NZ, THREADS><<<grid, THREADS, smem, st>>>(a);
   return (int)cudaGetLastError();
@@ -926,11 +930,11 @@ int launch_line_dft(bool fp64, void* data, int nb, int nx, int ny, int axis, int
   dim3 grid(nlines, nb);
   int thr = n >= 256 ? 256 : ((n + 31) / 32) * 32;
   if (fp64) {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
       COUNT_LAUNCH();
       k_line_dft<double2><<<grid, thr, smem, st>>>((double2*)data, nx, ny, axis, inverse);
   } else {
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_line_dft<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
       COUNT_LAUNCH();
       k_line_dft<float2><<<grid, thr, smem, st>>>((float2*)data, nx, ny, axis, inverse);
   }

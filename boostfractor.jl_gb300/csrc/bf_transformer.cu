@@ -61,7 +61,9 @@ int bf_general_prop(bf_handle* h, const bf_stack* s, int kind, bool fp64, void* 
   do {                                                                                       \
     cudaError_t e_ = (call);                                                                 \
     if (e_ != cudaSuccess)                                                                   \
-      return bf_fail(h, BF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));    \
+      return bf_fail(h, BF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_) + " (" + \
+                  std::string(__FILE__).substr(std::string(__FILE__).find_last_of('/') + 1) + ":" +  \
+                  std::to_string(__LINE__) + ")");    \
   } while (0)
 #define TCKS(call)              \
   do {                          \
@@ -1538,6 +1540,11 @@ struct TraceArgs {
   double* out;          // nf x (nd, 2, nm) complex, column-major per frequency
 };
 
+// Dynamic shared-memory limit set on the solve kernels: the per-block maximum,
+// the same for every launch, so that concurrent launches of one kernel with
+// different sizes (serving workers) cannot lower it under one another.
+constexpr int kMaxDynSmem = 227 * 1024;
+
 // PT: storage of the propagation matrices, their inverses and the chain:
 // double2 (FP64 path) or float2 (mixed path); the boundary solve is FP64.
 template <typename PT>
@@ -1627,7 +1634,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaGetLastError());
   } else {
     const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
-    TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     dim3 grid(nd - 1, nf);
     bf::note_launch();
     k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
@@ -1682,7 +1689,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   TCKS(ax.alloc(h, sizeof(double2) * (size_t)nf * nm));
   if constexpr (fp64) {
     const size_t smem = sizeof(D2) * 2 * nm * nm + sizeof(double2) * 2 * nm;
-    TCK(cudaFuncSetAttribute(k_chain<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TCK(cudaFuncSetAttribute(k_chain<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();
     k_chain<D2><<<nf, 256, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                        T21.as<D2>(), T22.as<D2>(), ax.as<double2>());
@@ -1697,7 +1704,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
       TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
       TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
     }
-    TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();
     // one thread per matrix entry up to 1024 (at 64 modes one CTA per frequency
     // owns the SM's shared memory, and 32 warps hide the serial TwoSum chains)
@@ -1717,7 +1724,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   TCKS(b2.alloc(h, sizeof(double) * nf));
   {
     const size_t smem = sizeof(double2) * nm * (nm + 2) + 256 * (sizeof(double) + sizeof(int));
-    TCK(cudaFuncSetAttribute(k_final_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TCK(cudaFuncSetAttribute(k_final_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();
     k_final_solve<double2><<<nf, 256, smem, st>>>(T21.as<double2>(), T22.as<double2>(), ax.as<double2>(),
                                              reflect ? d_refl.as<double2>() : nullptr, nm, boost.as<double2>(),
