@@ -689,7 +689,7 @@ __device__ __forceinline__ DFc dfc_add(DFc x, DFc y) {
 
 __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2* Pinv, const ChainRegion* cr,
                                                   int nd, int nm, const double2* emit, DFc* T21g, DFc* T22g,
-                                                  double2* axg, double2* T21out, double2* T22out) {
+                                                  double2* axg, double2* T21out, double2* T22out, int par_axion) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int n2 = nm * nm;
   DFc* U = reinterpret_cast<DFc*>(sm);
@@ -703,6 +703,10 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
   // the axion sum reads a row of T per step, one dependent load per entry
   DFc* T21 = T21g ? T21g + (size_t)f * n2 : em + nm;
   DFc* T22 = T21g ? T22g + (size_t)f * n2 : em + nm + n2;
+  // par_axion (T in shared memory and room for one more matrix): the axion
+  // terms of all (m, k) are formed in parallel into Wt, then each row is
+  // summed in k order as the serial form does (same values, shorter chain)
+  DFc* Wt = par_axion ? em + nm + 2 * n2 : nullptr;
   const DFc zero = {0.f, 0.f, 0.f, 0.f}, one = {1.f, 0.f, 0.f, 0.f};
   for (int e = tid; e < n2; e += nt) {
     T21[e] = zero;
@@ -716,11 +720,15 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
   for (int j = 1; j < nd; ++j) {
     const ChainRegion g = cr[j];
     // axion_beam += S (T21 + T22) emit   (T of the previous step)
-    for (int m = tid; m < nm; m += nt) {
-      DFc acc = zero;
-      for (int k = 0; k < nm; ++k) acc = dfc_add(acc, dfc_mul(dfc_add(T21[m * nm + k], T22[m * nm + k]), em[k]));
-      const double2 v = dfc_to_d(acc);
-      ax[m] = bf::cadd(ax[m], bf::cmul(g.S, v));
+    if (Wt) {
+      for (int e = tid; e < n2; e += nt) Wt[e] = dfc_mul(dfc_add(T21[e], T22[e]), em[e % nm]);
+    } else {
+      for (int m = tid; m < nm; m += nt) {
+        DFc acc = zero;
+        for (int k = 0; k < nm; ++k) acc = dfc_add(acc, dfc_mul(dfc_add(T21[m * nm + k], T22[m * nm + k]), em[k]));
+        const double2 v = dfc_to_d(acc);
+        ax[m] = bf::cadd(ax[m], bf::cmul(g.S, v));
+      }
     }
     // U = a T21 + b T22, V = b T21 + a T22; stage P_j and inverse(P_j)
     const DFc a = dfc_from(g.a), b = dfc_from(g.b), sc = dfc_from(g.inv2n);
@@ -736,6 +744,13 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
       Qs[e] = Qj[e];
     }
     __syncthreads();
+    if (Wt)   // reads only Wt: runs alongside the product below, which rewrites T
+      for (int m = tid; m < nm; m += nt) {
+        DFc acc = zero;
+        for (int k = 0; k < nm; ++k) acc = dfc_add(acc, Wt[m * nm + k]);
+        const double2 v = dfc_to_d(acc);
+        ax[m] = bf::cadd(ax[m], bf::cmul(g.S, v));
+      }
     // T21 = s U P, T22 = s V inverse(P)
     for (int e = tid; e < n2; e += nt) {
       const int r = e / nm, c = e % nm;
@@ -1703,8 +1718,9 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     DBuf T21df, T22df;
     size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
     const bool t_in_smem = smem + sizeof(DFc) * 2 * nm * nm <= 160 * 1024;
+    const bool par_axion = t_in_smem && smem + sizeof(DFc) * 3 * nm * nm <= 160 * 1024;
     if (t_in_smem) {
-      smem += sizeof(DFc) * 2 * nm * nm;
+      smem += sizeof(DFc) * (par_axion ? 3 : 2) * nm * nm;
     } else {
       TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
       TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
@@ -1717,7 +1733,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     k_chain_df<<<nf, nthr, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                       t_in_smem ? nullptr : T21df.as<DFc>(), t_in_smem ? nullptr : T22df.as<DFc>(),
                                       ax.as<double2>(), T21.as<double2>(),
-                                      T22.as<double2>());
+                                      T22.as<double2>(), par_axion ? 1 : 0);
     TCK(cudaGetLastError());
   }
   if (reflect) {
