@@ -618,6 +618,12 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_phase(FusedArgs<cplx_t<
   constexpr int G = X::G, RR = X::RR, P = X::P;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int tid = threadIdx.x, team = tid / G, g = tid % G, nteam = blockDim.x / G;
+  // programmatic dependent launch: let the next phase launch now, and wait for
+  // the previous phase (its writes visible) before reading anything it wrote
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  C tw[RR];
+  team_twiddles<N>(tw, g);
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const StepDesc sd = a.steps[blockIdx.x];
   const int f = blockIdx.y;
   C* MA = a.mg + ((size_t)blockIdx.x * a.nfreq + f) * 2 * (size_t)a.nby * P;
@@ -628,8 +634,6 @@ __global__ void __launch_bounds__(kSplitThreads) k_split_phase(FusedArgs<cplx_t<
     return;
   }
   C* scr = reinterpret_cast<C*>(smem_raw) + team * X::T::SCR;
-  C tw[RR];
-  team_twiddles<N>(tw, g);
   const int t0 = blockIdx.z * nteam, ts = gridDim.z * nteam;
   if (phase == 0) {
     joint_phase1<C, N, NZ, kSplitThreads / G, true>(a, sd, f, MA, MB, scr, tw, team, g, t0, ts, pa, pb);
@@ -661,10 +665,21 @@ static int launch_split(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t 
   const int zr = (2 * a.nby + nteam - 1) / nteam, zc = (2 * N + nteam - 1) / nteam;
   const int zm = (a.nbx * a.nby + kSplitThreads - 1) / kSplitThreads;
   const int z[4] = {zr, zc, zr, zm};
+  // each phase may launch while the previous one drains (programmatic
+  // dependent launch); the kernel waits for it before touching its data
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
   for (int ph = 0; ph < 4; ++ph) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nsteps, a.nfreq, z[ph]);
+    cfg.blockDim = dim3(kSplitThreads);
+    cfg.dynamicSmemBytes = ph == 3 ? 0 : smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
     COUNT_LAUNCH();
-    k_split_phase<R, N, NZ><<<dim3(nsteps, a.nfreq, z[ph]), kSplitThreads, ph == 3 ? 0 : smem, st>>>(a, ph);
-    const cudaError_t e = cudaGetLastError();
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_split_phase<R, N, NZ>, a, ph);
     if (e != cudaSuccess) return (int)e;
   }
   return 0;
