@@ -155,6 +155,20 @@ __global__ void k_build_v(C* V, const double2* pat, const int* supp, int Kd, int
   V[(size_t)mm * Kd + s] = dto<C>(make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x));
 }
 
+// Upper triangle of V as real rows: pair t = (m, m') with m <= m' gives
+// Vr[2t][s] = Re V[mm'][s] and Vr[2t+1][s] = Im V[mm'][s].  V is Hermitian in
+// the mode pair (V[m'm] = conj V[mm']), so these rows determine all of it.
+__global__ void k_build_vr(float* Vr, const double2* pat, const int* supp, const int2* tri, int Kd, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  if (s >= Kd) return;
+  const int2 mp = tri[t];
+  const int x = supp[s];
+  const double2 a = pat[(size_t)mp.x * npix + x], b = pat[(size_t)mp.y * npix + x];
+  Vr[(size_t)(2 * t) * Kd + s] = (float)(a.x * b.x + a.y * b.y);
+  Vr[(size_t)(2 * t + 1) * Kd + s] = (float)(a.x * b.y - a.y * b.x);
+}
+
 // kz[e][f][o] = sqrt(k0^2 - kx^2 - ky^2) at the orbit representative o, for the
 // distinct permittivities e of the k-space regions (FP64, once per solve)
 __global__ void k_build_kz(double2* KZ, const int2* rep, int K, const double* freqs, int nf, const double2* eps,
@@ -423,6 +437,32 @@ __global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const R
   }
 }
 
+// P[f][j] of the pixel class from the real-row GEMM output H[2T][f*ncols + col]
+// (rows of k_build_vr): with X = H[2t] and Y = H[2t+1],
+// P[m][m'] = X + iY and P[m'][m] = X - iY; disk regions get diag(DG) from the left.
+template <typename PT>
+__global__ void k_scatter_herm(PT* P, const double2* H, int nf, int ncols, const RegionT* regs,
+                               const int* cls_regions, int nd, int nm, const double2* DG, const int2* tri, int T) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int2 mp = tri[t];
+  const size_t N = (size_t)nf * ncols;
+  for (int c = blockIdx.y; c < nf * ncols; c += gridDim.y) {
+    const int f = c / ncols, q = c % ncols;
+    const int j = cls_regions[q];
+    const double2 X = H[(size_t)(2 * t) * N + c], Y = H[(size_t)(2 * t + 1) * N + c];
+    double2 p1 = make_double2(X.x - Y.y, X.y + Y.x);
+    double2 p2 = make_double2(X.x + Y.y, X.y - Y.x);
+    if (DG && regs[j].klass == 1) {
+      p1 = bf::cmul(DG[(size_t)c * nm + mp.x], p1);
+      p2 = bf::cmul(DG[(size_t)c * nm + mp.y], p2);
+    }
+    PT* Pj = P + ((size_t)f * nd + j) * nm * nm;
+    Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
+    if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
+  }
+}
+
 // field class: P[m][m'] = sum_x conj(Psi_m(x)) Q[m'][x]
 template <typename PT, typename C>
 __global__ void k_overlap(PT* P, const double2* pat, const C* Q, int nm, int npix) {
@@ -543,6 +583,143 @@ __global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int
   for (int e = threadIdx.x; e < nm * nm; e += blockDim.x) M[e] = P[off + e];
   __syncthreads();
   bf::cta_invert(M, W, nm, nullptr, red_v, red_i);
+}
+
+// ---- batched inversion of complex64 matrices, 16 < nm <= NB, in registers ----
+// Gauss-Jordan by Jordan exchanges with implicit partial pivoting.  The matrix,
+// padded to NB x NB with the identity, lives in registers, 4 x 4 entries per
+// thread.  Step c takes the unused row p with the largest |A[p][c]|^2 (lowest
+// row on ties), d = 1/A[p][c] and R[k] = -A[p][k] d, then
+//   A[r][k] += A[r][c] R[k] (r != p, k != c),   A[r][c] = A[r][c] d (r != p),
+//   A[p][k] = R[k] (k != c),                    A[p][c] = d.
+// After nm steps row p_c expresses x_c in the y_{p_k}: inv[c][p_k] = A[p_c][k].
+// Shared memory carries only the pivot column (double-buffered by step parity)
+// and the scaled pivot row, so each step is 16 complex FMAs per thread against
+// 8 shared loads.  Singular pivots give inf/NaN (the host checks).
+__device__ __forceinline__ float2 pick4(const float2 (&v)[4], int s) {
+  float2 r = v[0];
+  if (s == 1) r = v[1];
+  if (s == 2) r = v[2];
+  if (s == 3) r = v[3];
+  return r;
+}
+
+template <int NB>
+__global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2* P, float2* Pinv, int nd, int j0,
+                                                                  int nm) {
+  constexpr int NBB = NB / 4, NT = NBB * NBB, RPL = NB / 32;
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ float2 colv[2][NB], rowv[NB];
+  __shared__ int piv[NB], cof[NB];
+  __shared__ float2 dsh;
+  __shared__ int psh;
+  __shared__ float2 outs[NB * NB];
+  const int tid = threadIdx.x, br = tid / NBB, bc = tid % NBB, lane = tid & 31;
+  const int f = blockIdx.y, j = j0 + blockIdx.x;
+  const size_t off = (((size_t)f * nd + j) * nm) * nm;
+  float2 A[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = br * 4 + i, k = bc * 4 + q;
+      A[i][q] = (r < nm && k < nm) ? P[off + (size_t)r * nm + k] : make_float2(r == k ? 1.f : 0.f, 0.f);
+    }
+  bool used[RPL];
+#pragma unroll
+  for (int q = 0; q < RPL; ++q) used[q] = false;
+  for (int c = 0; c < nm; ++c) {
+    const int cb = c >> 2, cs = c & 3;
+    float2* cv = colv[c & 1];
+    if (bc == cb)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) cv[br * 4 + i] = pick4(A[i], cs);
+    __syncthreads();
+    if (tid < 32) {
+      float best = -1.f;
+      int bi = NB;
+#pragma unroll
+      for (int q = 0; q < RPL; ++q) {
+        const int r = lane + 32 * q;
+        if (r < nm && !used[q]) {
+          const float2 a = cv[r];
+          float v = a.x * a.x + a.y * a.y;
+          if (v != v) v = INFINITY;   // NaN orders as largest: the argmax stays a total order
+          if (v > best) { best = v; bi = r; }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float vo = __shfl_xor_sync(FULL, best, o);
+        const int io = __shfl_xor_sync(FULL, bi, o);
+        if (vo > best || (vo == best && io < bi)) { best = vo; bi = io; }
+      }
+      bi = min(bi, nm - 1);   // an unused row < nm always exists; keeps cv[] in bounds
+#pragma unroll
+      for (int q = 0; q < RPL; ++q)
+        if (lane + 32 * q == bi) used[q] = true;
+      if (lane == 0) {
+        const float2 a = cv[bi];
+        const float s2 = a.x * a.x + a.y * a.y;
+        dsh = make_float2(a.x / s2, -a.y / s2);
+        psh = bi;
+        piv[c] = bi;
+        cof[bi] = c;
+        cv[bi] = make_float2(0.f, 0.f);
+      }
+    }
+    __syncthreads();
+    const int p = psh;
+    const float2 d = dsh;
+    if (br == (p >> 2))
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        float2 a = A[0][q];
+        if ((p & 3) == 1) a = A[1][q];
+        if ((p & 3) == 2) a = A[2][q];
+        if ((p & 3) == 3) a = A[3][q];
+        const int k = bc * 4 + q;
+        rowv[k] = k == c ? make_float2(0.f, 0.f)
+                         : make_float2(-(a.x * d.x - a.y * d.y), -(a.x * d.y + a.y * d.x));
+      }
+    __syncthreads();
+    float2 F[4], R[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) F[i] = cv[br * 4 + i];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) R[q] = rowv[bc * 4 + q];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        A[i][q].x = fmaf(F[i].x, R[q].x, fmaf(-F[i].y, R[q].y, A[i][q].x));
+        A[i][q].y = fmaf(F[i].x, R[q].y, fmaf(F[i].y, R[q].x, A[i][q].y));
+      }
+    // column c: A[r][c] d (r != p) and d; row p: R (k != c)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = br * 4 + i;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = bc * 4 + q;
+        if (k == c) {
+          A[i][q] = r == p ? d : make_float2(F[i].x * d.x - F[i].y * d.y, F[i].x * d.y + F[i].y * d.x);
+        } else if (r == p) {
+          A[i][q] = R[q];
+        }
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = br * 4 + i, k = bc * 4 + q;
+      if (r < nm && k < nm) outs[cof[r] * nm + piv[k]] = A[i][q];
+    }
+  __syncthreads();
+  for (int e = tid; e < nm * nm; e += NT) Pinv[off + e] = outs[e];
 }
 
 // ---- the chain: one CTA per frequency ---------------------------------------
@@ -989,6 +1166,9 @@ struct TfCache {
   int mode = -1;   // operands built for: 0 FP64, 1 complex64 (SIMT GEMM), 2 TF32 pairs (tensor cores)
   int K = 0, msz = 0, Kd = 0, nm = 0;
   DBuf W, V, rep, supp, U, Phi, members;
+  // complex64 path: upper triangle of V as real rows (k_build_vr), pair table
+  DBuf Vr, tri;
+  int T = 0;
   // BF_PREC_TF32: A'' of both classes as TF32 hi/lo pairs (K padded to Kp, Kdp)
   DBuf Wt_hi, Wt_lo, Vt_hi, Vt_lo;
   int Kp = 0, Kdp = 0;
@@ -999,8 +1179,8 @@ static void tf_cache_delete(void* p) { delete static_cast<TfCache*>(p); }
 static size_t tf_cache_bytes(const void* p) {
   const TfCache* c = static_cast<const TfCache*>(p);
   size_t b = 0;
-  for (const DBuf* d : {&c->W, &c->V, &c->rep, &c->supp, &c->U, &c->Phi, &c->members, &c->Wt_hi, &c->Wt_lo,
-                        &c->Vt_hi, &c->Vt_lo})
+  for (const DBuf* d : {&c->W, &c->V, &c->Vr, &c->tri, &c->rep, &c->supp, &c->U, &c->Phi, &c->members,
+                        &c->Wt_hi, &c->Wt_lo, &c->Vt_hi, &c->Vt_lo})
     b += d->p ? d->n : 0;
   return b;
 }
@@ -1018,7 +1198,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   // which a stack changes after creation (bf_stack_set_distance moves the
   // disks), so gap updates of an optimiser reuse them.
   if (c.modes_id == md->id && c.mode == mode) return BF_OK;
-  for (DBuf* d : {&c.W, &c.V, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
+  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.tri, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -1126,8 +1306,15 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm,
                                                (int)npix);
     } else if (mode == 1) {
-      TCKS(c.V.alloc(h, csz * (size_t)nm * nm * c.Kd));
-      k_build_v<float2><<<grid, 256, 0, st>>>(c.V.as<float2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm, (int)npix);
+      std::vector<int2> tri;
+      for (int m = 0; m < nm; ++m)
+        for (int mp = m; mp < nm; ++mp) tri.push_back(make_int2(m, mp));
+      c.T = (int)tri.size();
+      TCKS(c.tri.alloc(h, sizeof(int2) * tri.size()));
+      TCK(cudaMemcpyAsync(c.tri.p, tri.data(), sizeof(int2) * tri.size(), cudaMemcpyHostToDevice, st));
+      TCKS(c.Vr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.Kd));
+      k_build_vr<<<dim3(blocks_for(c.Kd), c.T), 256, 0, st>>>(c.Vr.as<float>(), md->d_pat, c.supp.as<int>(),
+                                                               c.tri.as<int2>(), c.Kd, (int)npix);
     } else {
       const size_t n = (size_t)2 * nm * nm * 2 * c.Kdp;
       TCKS(c.Vt_hi.alloc(h, sizeof(float) * n));
@@ -1183,6 +1370,32 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
       bf::note_launch();
       bf::k_sum_planes<<<blocks_for(n), 256, 0, h->stream()>>>(Cm, part.as<double2>(), n, splits);
     }
+  }
+  TCK(cudaGetLastError());
+  return BF_OK;
+}
+
+// Real-row class GEMM H = A * B (A real FP32 [R][K], B complex64 [K][N],
+// H complex128 [R][N]) with the split-K rule of launch_gemm.
+static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* Hm, int R, int K, int N) {
+  g_tf_gemm_flops += 4.0 * (double)R * (double)K * (double)N;
+  dim3 grid((N + 31) / 32, (R + 127) / 128);
+  const long tiles = (long)grid.x * grid.y;
+  int splits = 1;
+  while (splits < 16 && tiles * splits < 2 * 152 && K / (splits * 2) >= 256) splits *= 2;
+  bf::note_launch();
+  if (splits == 1) {
+    bf::k_rcgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, Hm, R, K, N, K);
+  } else {
+    const int kchunk = ((K + splits - 1) / splits + 15) / 16 * 16;
+    DBuf part;
+    TCKS(part.alloc(h, sizeof(double2) * (size_t)splits * R * N));
+    grid.z = splits;
+    bf::k_rcgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, part.as<double2>(), R, K, N, kchunk);
+    TCK(cudaGetLastError());
+    const size_t n = (size_t)R * N;
+    bf::note_launch();
+    bf::k_sum_planes<<<blocks_for(n), 256, 0, h->stream()>>>(Hm, part.as<double2>(), n, splits);
   }
   TCK(cudaGetLastError());
   return BF_OK;
@@ -1300,7 +1513,8 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(lst.alloc(h, sizeof(int) * npx));
     TCK(cudaMemcpyAsync(lst.p, preg.data(), sizeof(int) * npx, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npx;
-    TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
+    const int grows = mode == 1 ? 2 * c.T : nm * nm;   // mode 1: real rows of the upper triangle
+    TCKS(G.alloc(h, sizeof(C) * (size_t)grows * ncol));
     DBuf K0, DG;
     TCKS(K0.alloc(h, sizeof(double2) * (size_t)ncol));
     TCKS(DG.alloc(h, sizeof(double2) * (size_t)ncol * nm));
@@ -1318,7 +1532,10 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
           E.as<S>(), c.supp.as<int>(), c.Kd, nf, dr, lst.as<int>(), npx, K0.as<double2>(), s->dX, s->dY, nx,
           s->d_surf, (int)npix);
       TCK(cudaGetLastError());
-      TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
+      if constexpr (std::is_same<S, float2>::value)
+        TCKS(launch_rgemm(h, c.Vr.as<float>(), E.as<float2>(), G.as<C>(), 2 * c.T, c.Kd, ncol));
+      else
+        TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
     } else {
       DBuf Bh, Bl;
       const size_t nb = (size_t)ncol * 2 * c.Kdp;
@@ -1332,9 +1549,16 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       TCKS(tc_class_gemm(h, c.Vt_hi.as<float>(), c.Vt_lo.as<float>(), nm * nm, c.Kdp, Bh.as<float>(),
                          Bl.as<float>(), ncol, G.as<C>(), tc_err));
     }
-    dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
-    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm, DG.as<double2>());
+    if (mode == 1) {
+      dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+      k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
+                                            DG.as<double2>(), c.tri.as<int2>(), c.T);
+    } else {
+      dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
+      k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
+                                         DG.as<double2>());
+    }
     TCK(cudaGetLastError());
   }
   // field class: propagate every mode (FP64), then overlap
@@ -1651,6 +1875,14 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     bf::note_launch();
     if (nm <= 8) k_invert_warp<D2, 8><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
     else k_invert_warp<D2, 16><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
+    TCK(cudaGetLastError());
+  } else if (std::is_same<D2, float2>::value && nm <= 64) {
+    dim3 grid(nd - 1, nf);
+    bf::note_launch();
+    if constexpr (std::is_same<D2, float2>::value) {
+      if (nm <= 32) k_invert_reg<32><<<grid, 64, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
+      else k_invert_reg<64><<<grid, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
+    }
     TCK(cudaGetLastError());
   } else {
     const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));

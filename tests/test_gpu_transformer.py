@@ -174,6 +174,28 @@ def test_transformer_batched_mixed_and_injected(B):
     assert rel(got, O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=freqs[2], propagation_matrices=pm)) < FP64_TOL
 
 
+@pytest.mark.parametrize("M,L,n", [(5, 2, 32), (8, 2, 64)])
+def test_transformer_mixed_mid_mode_counts(B, M, L, n):
+    """Mixed path at 25 and 40 modes: the register-resident complex64 inverses
+    (padded to 32 and 64; the 32-pixel case has propagation matrices of
+    condition ~100, so pivoting matters) and the real-row pixel-class GEMM.
+    beta^2 within 1e-4 of the oracle."""
+    distance, eps, tx, ty, X, s = _stack(2, n, seed=M, surf=True)
+    kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
+              relative_surfaces=s)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=M, Lmax=L, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=M, Lmax=L, diskR=0.15)
+    assert mb.nm == M * (2 * L + 1)
+    freqs = np.array([19.6e9, 20.3e9])
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    for k, f in enumerate(freqs):
+        ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
+        r2 = np.sum(np.abs(ref) ** 2)
+        assert abs(np.sum(np.abs(b32[k]) ** 2) - r2) / r2 < MIXED_BETA2_TOL
+        assert rel(b32[k], ref) < 1e-3
+
+
 def test_transformer_lg_pattern_input_vs_oracle(B):
     """Laguerre-Gauss modes through pattern_input/kT_arr (transformer.jl:46,
     :99-104) on a reduced stack with surface maps: FP64 boost within 1e-10,
