@@ -521,7 +521,9 @@ def run_transformer(args):
                              "executed_gemm_tflop_per_request": gemm_fl / args.steps / 1e12},
             "roofline": {"bound": "fp32-simt", "achieved": gemm_fl / (gemm_ms / 1000.0) / 1e12,
                          "peak": peak_fp32, "peak_source": fp32_src, "unit": "TFLOP/s",
-                         "frac": gemm_fl / (gemm_ms / 1000.0) / 1e12 / peak_fp32, "kernel": "k_cgemm_c64",
+                         "frac": gemm_fl / (gemm_ms / 1000.0) / 1e12 / peak_fp32,
+                         "kernel": "k_rcgemm_c64 (real rows of the Hermitian class overlaps; k_cgemm_c64 when "
+                                   "the modes extend beyond the disk mask)",
                          "phase_ms": gemm_ms / args.steps},
             "tensor_core_tf32": {
                 "value": nf / (ms_tc / 1000.0), "unit": UNIT, "ms_per_step": ms_tc,

@@ -155,6 +155,27 @@ __global__ void k_build_v(C* V, const double2* pat, const int* supp, int Kd, int
   V[(size_t)mm * Kd + s] = dto<C>(make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x));
 }
 
+// Upper triangle of W as real rows (valid when W is Hermitian in the mode
+// pair: Phi = U, every mode zero outside the mask): pair t = (m, m') gives
+// Wr[2t][o] = Re W[mm'][o], Wr[2t+1][o] = Im W[mm'][o], summed like k_build_w.
+__global__ void k_build_wr(float* Wr, const double2* U, const double2* Phi, const int* members, const int2* tri,
+                           int K, int msz, int npix, double scale) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  if (o >= K) return;
+  const int2 mp = tri[t];
+  double2 acc = make_double2(0.0, 0.0);
+  for (int q = 0; q < msz; ++q) {
+    const int k = members[(size_t)o * msz + q];
+    if (k < 0) break;
+    const double2 u = U[(size_t)mp.x * npix + k], p = Phi[(size_t)mp.y * npix + k];
+    acc.x += u.x * p.x + u.y * p.y;
+    acc.y += u.x * p.y - u.y * p.x;
+  }
+  Wr[(size_t)(2 * t) * K + o] = (float)(acc.x * scale);
+  Wr[(size_t)(2 * t + 1) * K + o] = (float)(acc.y * scale);
+}
+
 // Upper triangle of V as real rows: pair t = (m, m') with m <= m' gives
 // Vr[2t][s] = Re V[mm'][s] and Vr[2t+1][s] = Im V[mm'][s].  V is Hermitian in
 // the mode pair (V[m'm] = conj V[mm']), so these rows determine all of it.
@@ -1166,9 +1187,11 @@ struct TfCache {
   int mode = -1;   // operands built for: 0 FP64, 1 complex64 (SIMT GEMM), 2 TF32 pairs (tensor cores)
   int K = 0, msz = 0, Kd = 0, nm = 0;
   DBuf W, V, rep, supp, U, Phi, members;
-  // complex64 path: upper triangle of V as real rows (k_build_vr), pair table
-  DBuf Vr, tri;
+  // complex64 path: upper triangle of V as real rows (k_build_vr), pair table;
+  // W the same way (Wr, k_build_wr) when every mode vanishes outside the mask
+  DBuf Vr, Wr, tri;
   int T = 0;
+  bool herm_w = false;
   // BF_PREC_TF32: A'' of both classes as TF32 hi/lo pairs (K padded to Kp, Kdp)
   DBuf Wt_hi, Wt_lo, Vt_hi, Vt_lo;
   int Kp = 0, Kdp = 0;
@@ -1179,7 +1202,7 @@ static void tf_cache_delete(void* p) { delete static_cast<TfCache*>(p); }
 static size_t tf_cache_bytes(const void* p) {
   const TfCache* c = static_cast<const TfCache*>(p);
   size_t b = 0;
-  for (const DBuf* d : {&c->W, &c->V, &c->Vr, &c->tri, &c->rep, &c->supp, &c->U, &c->Phi, &c->members,
+  for (const DBuf* d : {&c->W, &c->V, &c->Vr, &c->Wr, &c->tri, &c->rep, &c->supp, &c->U, &c->Phi, &c->members,
                         &c->Wt_hi, &c->Wt_lo, &c->Vt_hi, &c->Vt_lo})
     b += d->p ? d->n : 0;
   return b;
@@ -1198,7 +1221,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   // which a stack changes after creation (bf_stack_set_distance moves the
   // disks), so gap updates of an optimiser reuse them.
   if (c.modes_id == md->id && c.mode == mode) return BF_OK;
-  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.tri, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
+  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.Wr, &c.tri, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -1271,9 +1294,32 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(),
                                                c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
     } else if (mode == 1) {
-      TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
-      k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(),
-                                              c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
+      // Phi = FFT(mask Psi) equals U = FFT(Psi) bit for bit when no mode has a
+      // non-zero pixel outside the (0/1) mask; W is then Hermitian in the mode
+      // pair, W[m'm] = conj W[mm'], and its upper triangle determines it.
+      c.herm_w = true;
+      for (int m = 0; m < nm && c.herm_w; ++m)
+        for (size_t x = 0; x < npix; ++x)
+          if (!s->mask_full[x] && md->pat[(size_t)m * npix + x] != cd(0.0, 0.0)) {
+            c.herm_w = false;
+            break;
+          }
+      std::vector<int2> tri;
+      for (int m = 0; m < nm; ++m)
+        for (int mp = m; mp < nm; ++mp) tri.push_back(make_int2(m, mp));
+      c.T = (int)tri.size();
+      TCKS(c.tri.alloc(h, sizeof(int2) * tri.size()));
+      TCK(cudaMemcpyAsync(c.tri.p, tri.data(), sizeof(int2) * tri.size(), cudaMemcpyHostToDevice, st));
+      if (c.herm_w) {
+        TCKS(c.Wr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.K));
+        k_build_wr<<<dim3(blocks_for(c.K), c.T), 256, 0, st>>>(c.Wr.as<float>(), c.U.as<double2>(),
+                                                                c.Phi.as<double2>(), c.members.as<int>(),
+                                                                c.tri.as<int2>(), c.K, c.msz, (int)npix, scale);
+      } else {
+        TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+        k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(),
+                                                c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
+      }
     } else {
       const size_t n = (size_t)2 * nm * nm * 2 * c.Kp;
       TCKS(c.Wt_hi.alloc(h, sizeof(float) * n));
@@ -1306,12 +1352,6 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       k_build_v<double2><<<grid, 256, 0, st>>>(c.V.as<double2>(), md->d_pat, c.supp.as<int>(), c.Kd, nm,
                                                (int)npix);
     } else if (mode == 1) {
-      std::vector<int2> tri;
-      for (int m = 0; m < nm; ++m)
-        for (int mp = m; mp < nm; ++mp) tri.push_back(make_int2(m, mp));
-      c.T = (int)tri.size();
-      TCKS(c.tri.alloc(h, sizeof(int2) * tri.size()));
-      TCK(cudaMemcpyAsync(c.tri.p, tri.data(), sizeof(int2) * tri.size(), cudaMemcpyHostToDevice, st));
       TCKS(c.Vr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.Kd));
       k_build_vr<<<dim3(blocks_for(c.Kd), c.T), 256, 0, st>>>(c.Vr.as<float>(), md->d_pat, c.supp.as<int>(),
                                                                c.tri.as<int2>(), c.Kd, (int)npix);
@@ -1476,7 +1516,8 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCKS(d_peps.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(d_peps.p, par_eps.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
     TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
-    TCKS(G.alloc(h, sizeof(C) * (size_t)nm * nm * ncol));
+    const bool herm = mode == 1 && c.herm_w;   // real rows of W's upper triangle
+    TCKS(G.alloc(h, sizeof(C) * (size_t)(herm ? 2 * c.T : nm * nm) * ncol));
     bf::note_launch();
     k_build_kz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
         KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
@@ -1487,7 +1528,12 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
           D.as<S>(), KZ.as<double2>(), c.K, nf, dr, lst.as<int>(), d_peps.as<int>(), npar);
       TCK(cudaGetLastError());
-      TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
+      if (herm) {
+        if constexpr (std::is_same<S, float2>::value)
+          TCKS(launch_rgemm(h, c.Wr.as<float>(), D.as<float2>(), G.as<C>(), 2 * c.T, c.K, ncol));
+      } else {
+        TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
+      }
     } else {
       DBuf Bh, Bl;
       const size_t nb = (size_t)ncol * 2 * c.Kp;
@@ -1501,9 +1547,15 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       TCKS(tc_class_gemm(h, c.Wt_hi.as<float>(), c.Wt_lo.as<float>(), nm * nm, c.Kp, Bh.as<float>(),
                          Bl.as<float>(), ncol, G.as<C>(), tc_err));
     }
-    dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
     bf::note_launch();
-    k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
+    if (herm) {
+      dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+      k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
+                                            c.tri.as<int2>(), c.T);
+    } else {
+      dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
+      k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
+    }
     TCK(cudaGetLastError());
   }
   // pixel class: one GEMM V * E

@@ -196,6 +196,31 @@ def test_transformer_mixed_mid_mode_counts(B, M, L, n):
         assert rel(b32[k], ref) < 1e-3
 
 
+@pytest.mark.parametrize("cut", [0.15, 0.3])
+def test_transformer_mixed_modes_inside_and_beyond_mask(B, cut):
+    """Laguerre-Gauss pattern_input cut at r <= 0.15 m (inside the 0.15 m disk
+    mask: the k-space overlaps are Hermitian in the mode pair and the mixed
+    path runs their upper triangle as real rows) and at r <= 0.3 m (non-zero
+    outside the mask: the full complex overlap GEMM).  Mixed beta^2 within
+    1e-4 of the oracle either way."""
+    from bfgb300 import workloads as W
+    distance, eps, tx, ty, _, _ = _stack(3, 64, seed=53, tilt_air=True)
+    X = W.symmetric_grid(64, width=0.4)
+    pats, kt = W.lg_modes(X, X, 20, 0.05, cut)
+    kw = dict(diskno=3, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=20, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=20, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    outside = (X[:, None] ** 2 + X[None, :] ** 2) >= 0.15 ** 2
+    assert np.any(np.abs(pats[:, 0, :, :, 0][:, outside]) > 0) == (cut > 0.15)
+    freqs = np.array([19.4e9, 20.7e9])
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    for k, f in enumerate(freqs):
+        ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
+        r2 = np.sum(np.abs(ref) ** 2)
+        assert abs(np.sum(np.abs(b32[k]) ** 2) - r2) / r2 < MIXED_BETA2_TOL
+
+
 def test_transformer_lg_pattern_input_vs_oracle(B):
     """Laguerre-Gauss modes through pattern_input/kT_arr (transformer.jl:46,
     :99-104) on a reduced stack with surface maps: FP64 boost within 1e-10,
