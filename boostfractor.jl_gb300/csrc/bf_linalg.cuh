@@ -165,12 +165,19 @@ __global__ void __launch_bounds__(256, 1) k_cgemm_c64(const float2* __restrict__
 // Real-by-complex GEMM Cout[r][c] = sum_k A[r][k] B[k][c]: A real (FP32),
 // B complex64, one FP32 product per term and accumulator, summed like
 // k_cgemm_c64 (FP32 over a 16-term K tile, TwoSum-folded into double-float).
-// Each thread owns 8 rows and 2 columns of a 128 x 32 tile.  blockIdx.z selects the K slice [z kchunk, (z+1) kchunk) and
-// the output plane Cout + z R Ncol.
-__global__ void __launch_bounds__(256, 1) k_rcgemm_c64(const float* __restrict__ A, const float2* __restrict__ B,
-                                                        double2* __restrict__ Cout, int R, int K, int Ncol,
-                                                        int kchunk) {
-  constexpr int TM = 128, TN = 32, TK = 16;
+// A CTA computes a 128 x 32 tile; each of its 16 * 128 / RPT threads owns RPT rows
+// and 2 columns.  RPT = 8 (256 threads, 203 registers, 8 warps per SM) is the
+// one launched: RPT = 4 (512 threads, 119 registers, 16 warps per SM) gave
+// the same transformer throughput on GB300 (4593 vs 4624 freq-points/s).
+// blockIdx.z selects the K slice [z kchunk, (z+1) kchunk) and the output plane
+// Cout + z R Ncol.
+template <int RPT>
+__global__ void __launch_bounds__(16 * 128 / RPT, 1) k_rcgemm_c64(const float* __restrict__ A,
+                                                                  const float2* __restrict__ B,
+                                                                  double2* __restrict__ Cout, int R, int K,
+                                                                  int Ncol, int kchunk) {
+  constexpr int TM = 128, TN = 32, TK = 16, NT = 16 * TM / RPT;
+  constexpr int QA = TM * TK / NT, QB = TK * TN / NT;   // staged elements per thread
   __shared__ __align__(16) float As[TK][TM + 4];
   __shared__ __align__(16) float2 Bs[TK][TN];
   const int tid = threadIdx.x;
@@ -178,24 +185,23 @@ __global__ void __launch_bounds__(256, 1) k_rcgemm_c64(const float* __restrict__
   const int r0 = blockIdx.y * TM, c0 = blockIdx.x * TN;
   const int kbeg = blockIdx.z * kchunk, kend = min(K, kbeg + kchunk);
   Cout += (size_t)blockIdx.z * R * Ncol;
-  float hr[8][2], lr[8][2], hi[8][2], li[8][2], ar[8][2], ai[8][2];
+  float hr[RPT][2], lr[RPT][2], hi[RPT][2], li[RPT][2], ar[RPT][2], ai[RPT][2];
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < RPT; ++i)
 #pragma unroll
     for (int j = 0; j < 2; ++j) hr[i][j] = lr[i][j] = hi[i][j] = li[i][j] = ar[i][j] = ai[i][j] = 0.0f;
-  // each thread stages 8 A and 2 B elements per tile
-  float pa[8];
-  float2 pb[2];
+  float pa[QA];
+  float2 pb[QB];
   auto fetch = [&](int k0) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int e = tid + 256 * q;
+    for (int q = 0; q < QA; ++q) {
+      const int e = tid + NT * q;
       const int gr = r0 + e / TK, gk = k0 + e % TK;
       pa[q] = (gr < R && gk < kend) ? A[(size_t)gr * K + gk] : 0.0f;
     }
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int e = tid + 256 * q;
+    for (int q = 0; q < QB; ++q) {
+      const int e = tid + NT * q;
       const int gk = k0 + e / TN, gc = c0 + e % TN;
       pb[q] = (gk < kend && gc < Ncol) ? B[(size_t)gk * Ncol + gc] : make_float2(0.f, 0.f);
     }
@@ -203,25 +209,31 @@ __global__ void __launch_bounds__(256, 1) k_rcgemm_c64(const float* __restrict__
   fetch(kbeg);
   for (int k0 = kbeg; k0 < kend; k0 += TK) {
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int e = tid + 256 * q;
+    for (int q = 0; q < QA; ++q) {
+      const int e = tid + NT * q;
       As[e % TK][e / TK] = pa[q];
     }
 #pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      const int e = tid + 256 * q;
+    for (int q = 0; q < QB; ++q) {
+      const int e = tid + NT * q;
       Bs[e / TN][e % TN] = pb[q];
     }
     __syncthreads();
     if (k0 + TK < kend) fetch(k0 + TK);
 #pragma unroll
     for (int kk = 0; kk < TK; ++kk) {
-      const float4 a0 = *reinterpret_cast<const float4*>(&As[kk][tr * 8]);
-      const float4 a1 = *reinterpret_cast<const float4*>(&As[kk][tr * 8 + 4]);
-      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      float a[RPT];
+#pragma unroll
+      for (int v = 0; v < RPT / 4; ++v) {
+        const float4 a4 = *reinterpret_cast<const float4*>(&As[kk][tr * RPT + 4 * v]);
+        a[4 * v] = a4.x;
+        a[4 * v + 1] = a4.y;
+        a[4 * v + 2] = a4.z;
+        a[4 * v + 3] = a4.w;
+      }
       const float2 b[2] = {Bs[kk][tc], Bs[kk][tc + 16]};
 #pragma unroll
-      for (int i = 0; i < 8; ++i)
+      for (int i = 0; i < RPT; ++i)
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
           ar[i][j] = fmaf(a[i], b[j].x, ar[i][j]);
@@ -229,7 +241,7 @@ __global__ void __launch_bounds__(256, 1) k_rcgemm_c64(const float* __restrict__
         }
     }
 #pragma unroll
-    for (int i = 0; i < 8; ++i)
+    for (int i = 0; i < RPT; ++i)
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         two_sum_acc(hr[i][j], lr[i][j], ar[i][j]);
@@ -239,10 +251,10 @@ __global__ void __launch_bounds__(256, 1) k_rcgemm_c64(const float* __restrict__
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 8; ++i)
+  for (int i = 0; i < RPT; ++i)
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
-      const int gr = r0 + tr * 8 + i, gc = c0 + tc + 16 * j;
+      const int gr = r0 + tr * RPT + i, gc = c0 + tc + 16 * j;
       if (gr < R && gc < Ncol)
         Cout[(size_t)gr * Ncol + gc] =
             make_double2((double)hr[i][j] + (double)lr[i][j], (double)hi[i][j] + (double)li[i][j]);

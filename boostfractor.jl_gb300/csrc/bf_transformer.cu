@@ -1425,13 +1425,13 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
   while (splits < 16 && tiles * splits < 2 * 152 && K / (splits * 2) >= 256) splits *= 2;
   bf::note_launch();
   if (splits == 1) {
-    bf::k_rcgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, Hm, R, K, N, K);
+    bf::k_rcgemm_c64<8><<<grid, 256, 0, h->stream()>>>(A, B, Hm, R, K, N, K);
   } else {
     const int kchunk = ((K + splits - 1) / splits + 15) / 16 * 16;
     DBuf part;
     TCKS(part.alloc(h, sizeof(double2) * (size_t)splits * R * N));
     grid.z = splits;
-    bf::k_rcgemm_c64<<<grid, 256, 0, h->stream()>>>(A, B, part.as<double2>(), R, K, N, kchunk);
+    bf::k_rcgemm_c64<8><<<grid, 256, 0, h->stream()>>>(A, B, part.as<double2>(), R, K, N, kchunk);
     TCK(cudaGetLastError());
     const size_t n = (size_t)R * N;
     bf::note_launch();
