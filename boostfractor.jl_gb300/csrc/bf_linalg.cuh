@@ -294,9 +294,9 @@ __device__ __forceinline__ C crecip(C v) {
 // |W[p][c]|^2, lowest row on ties) is a warp-shuffle argmax, then one over
 // the warps; its reciprocal is computed once and broadcast.  Magnitudes and
 // the reciprocal use the matrix's own precision: a warp-wide FP64 instruction
-// costs the same with one lane active, at 1/64 of the FP32 rate.  Singular
-// pivots give inf/NaN like LAPACK's inv would report an error (the host
-// checks).
+// costs the same with one lane active, at 1/64 of the FP32 rate.  A zero
+// pivot gives inf/NaN, which propagates to the solver's outputs (where Julia's
+// inv raises SingularException).
 template <typename C>
 __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* red_i) {
   using R = decltype(C().x);

@@ -616,7 +616,8 @@ __global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int
 // After nm steps row p_c expresses x_c in the y_{p_k}: inv[c][p_k] = A[p_c][k].
 // Shared memory carries only the pivot column (double-buffered by step parity)
 // and the scaled pivot row, so each step is 16 complex FMAs per thread against
-// 8 shared loads.  Singular pivots give inf/NaN (the host checks).
+// 8 shared loads.  A zero pivot gives inf/NaN, which propagates to the
+// solver's outputs (where Julia's inv raises SingularException).
 __device__ __forceinline__ float2 pick4(const float2 (&v)[4], int s) {
   float2 r = v[0];
   if (s == 1) r = v[1];
