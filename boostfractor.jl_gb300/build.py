@@ -82,24 +82,5 @@ def build(force=False, verbose=False):
     return LIB
 
 
-PEAKS_SRC = os.path.join(HERE, "peaks", "bf_peaks.cu")
-PEAKS_LIB = os.path.join(LIBDIR, "libbfpeaks.so")
-
-
-def build_peaks(force=False):
-    """libbfpeaks.so: the arithmetic-throughput probes bench.py uses for its
-    SIMT roofline denominators (not part of the solver library)."""
-    os.makedirs(LIBDIR, exist_ok=True)
-    if not force and not _newer(PEAKS_LIB, [PEAKS_SRC, os.path.abspath(__file__)]):
-        return PEAKS_LIB
-    tmp = PEAKS_LIB + ".tmp"
-    cmd = [nvcc()] + ARCH + ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", PEAKS_SRC, "-o", tmp]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
-    os.replace(tmp, PEAKS_LIB)
-    return PEAKS_LIB
-
-
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))

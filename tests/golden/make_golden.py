@@ -1,16 +1,15 @@
-"""Regenerate the committed fixtures under tests/golden/.
+"""Regenerate tests/golden/analytical1d.npz from the reference's own 1D model.
 
 Run in a container that has the reference checkout (its src/Analytical1D.py
 is plain numpy and runs as-is):
 
     python tests/golden/make_golden.py /path/to/BoostFractor.jl
 
-Writes
-  * analytical1d.npz -- |ax|^2 of the reference's 1D model
-    (src/Analytical1D.py:79-131, ``disk_system``) for seeded lossless stacks,
-    the independent cross-check of the transformer/cheerleader 1D limit;
-  * rfp_small.npz / transformer_small.npz -- oracle outputs on small seeded
-    cases, the fixtures the GPU parity tests compare against.
+Writes analytical1d.npz: |ax|^2 of the reference's 1D model
+(src/Analytical1D.py:79-131, ``disk_system``) for seeded lossless stacks, the
+independent cross-check of the transformer/cheerleader 1D limit.  The
+full-size oracle fixtures are written by make_c2_fixture.py (cheerleader) and
+make_c3_fixture.py (transformer).
 """
 import math
 import os
@@ -48,10 +47,9 @@ def analytical1d(ref_root):
 
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else None
-    if ref_root:
-        analytical1d(ref_root)
-    from tests.golden import fixtures
-    fixtures.write_all(HERE)
+    if not ref_root:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/BoostFractor.jl")
+    analytical1d(ref_root)
 
 
 if __name__ == "__main__":
