@@ -21,11 +21,16 @@
 //   * nx, ny <= BF_NOALLOC_MAX_N (256): the scratch below is sized for a
 //     256 x 256 grid (about 2.1 MiB of static device memory per device).
 //     Larger grids are rejected with BF_ERR_INVALID.
-//   * The first call on a device performs the set-up: it resolves the
-//     scratch's device address with cudaGetSymbolAddress (which also loads
-//     this module's device globals if the runtime deferred that) and launches
-//     each kernel of the path for the first time.  Make that first call before
-//     any stream capture begins.
+//   * The first call on a device performs the set-up: with that device
+//     current it resolves the scratch's device address with
+//     cudaGetSymbolAddress (which also loads this module's device globals if
+//     the runtime deferred that) and caches it for the device.  Make that
+//     first call before any stream capture begins.
+//   * The host arrays X, Y, kX, kY (and the surface map of the 3D kind) are
+//     copied into the scratch with cudaMemcpyAsync on the handle's stream.
+//     From pageable memory the runtime stages them before the call returns;
+//     from pinned memory the copy is asynchronous, so pinned arrays must stay
+//     valid and unchanged until the stream has reached this call's work.
 //   * There is ONE scratch per device, shared by every handle and thread of the
 //     process.  Calls that overlap in time on the same device (different
 //     streams, different host threads) race on it and give wrong results;
@@ -33,7 +38,8 @@
 //   * What must start at zero: nothing.  Every scratch byte a call reads is
 //     written earlier in the same call (coordinates, frequency, mask, surface
 //     map, the momentum-space roll buffer), so no clearing is needed between
-//     calls; the surface map is skipped entirely when the caller passes none.
+//     calls; the surface map is read only by the 3D kind, and only when the
+//     caller passes a non-zero one.
 #include <math.h>
 
 #include <cmath>
@@ -81,6 +87,9 @@ __global__ void k_noalloc_mask(unsigned char* mask, const double* X, const doubl
   const double s = __dadd_rn(__dmul_rn(X[x], X[x]), __dmul_rn(Y[y], Y[y]));
   mask[i] = fabs(s) < R2 ? 1 : 0;
 }
+
+// The frequency into the scratch, passed by value (no host buffer to keep alive).
+__global__ void k_noalloc_set_freq(double* dst, double freq) { *dst = freq; }
 
 // Device address of the scratch for `device`, resolved once per device.
 static int scratch_of(bf_handle* h, int device, unsigned char** out) {
@@ -147,16 +156,19 @@ extern "C" int bf_propagate_noalloc(bf_handle* h, int prop_kind, double* E_dev, 
   double2* dtmp = reinterpret_cast<double2*>(sc + kOffTmp);
   unsigned char* dmask = sc + kOffMask;
 
-  // Pageable-source copies are staged by the runtime before the call returns,
-  // so the caller's host arrays (and `freq` on this stack) may go away after it.
+  // Pageable sources are staged by the runtime before cudaMemcpyAsync returns;
+  // pinned ones are read when the stream gets there (see the rules above).
   const double freq = 299792458.0 / lambda;
   NK(cudaMemcpyAsync(dX, X, sizeof(double) * nx, cudaMemcpyHostToDevice, st));
   NK(cudaMemcpyAsync(dY, Y, sizeof(double) * ny, cudaMemcpyHostToDevice, st));
   NK(cudaMemcpyAsync(dkX, kX, sizeof(double) * nx, cudaMemcpyHostToDevice, st));
   NK(cudaMemcpyAsync(dkY, kY, sizeof(double) * ny, cudaMemcpyHostToDevice, st));
-  NK(cudaMemcpyAsync(dfreq, &freq, sizeof(double), cudaMemcpyHostToDevice, st));
+  bf::note_launch();
+  k_noalloc_set_freq<<<1, 1, 0, st>>>(dfreq, freq);
+  NK(cudaGetLastError());
+  // only the 3D propagator applies a surface map
   bool surf_nonzero = false;
-  if (surface)
+  if (surface && prop_kind == BF_PROP_3D)
     for (size_t i = 0; i < 2 * npix && !surf_nonzero; ++i) surf_nonzero = surface[i] != 0.0;
   if (surf_nonzero) NK(cudaMemcpyAsync(dsurf, surface, sizeof(double2) * npix, cudaMemcpyHostToDevice, st));
   if (prop_kind != BF_PROP_1D) {
