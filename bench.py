@@ -83,25 +83,35 @@ def _cpu_worker(args):
     return dt, float(np.sum(np.abs(E) ** 2))
 
 
-def cpu_baseline(w, nmax_s=60, workers=None):
-    """Time the oracle on `workers` host cores, one frequency each, nmax_s+1 bounces;
-    extrapolate linearly in propagations to the full request."""
-    P = workers or os.cpu_count() or 1
-    freqs = w["freqs"][np.linspace(0, len(w["freqs"]) - 1, P).astype(int)]
-    ctx = mp.get_context("spawn")
+def cpu_sample(pool, w, freqs, nmax_s):
+    """One bounded sample of the request on the host cores: the oracle's
+    cheerleader for each of `freqs` (one frequency per pool process) with
+    nmax_s + 1 bounces.  Returns (wall seconds, per-process solve seconds)."""
     t0 = time.perf_counter()
+    res = pool.map(_cpu_worker, [(w, float(f), nmax_s) for f in freqs])
+    return time.perf_counter() - t0, [r[0] for r in res]
+
+
+def sample_freqs(w, P, step=0):
+    """P of the request's frequencies, evenly spread, shifted by `step` so
+    that successive samples cover different frequencies."""
+    nf = len(w["freqs"])
+    idx = (np.linspace(0, nf - 1, P).astype(int) + step) % nf
+    return w["freqs"][idx]
+
+
+def cpu_baseline(w, workers=None):
+    """The oracle on `workers` host cores (spawned processes, one frequency
+    each) for the whole bounce count of the request: freq-points/s = workers
+    / the slowest process's solve time (process start-up excluded)."""
+    P = workers or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
     with ctx.Pool(P) as pool:
-        res = pool.map(_cpu_worker, [(w, float(f), nmax_s) for f in freqs])
-    wall = time.perf_counter() - t0
-    nd = len(w["distance"])
-    props = lambda nm: (nd - 2) + (nm + 1) * 2 * (nd - 2)
-    scale = props(w["nmax"]) / props(nmax_s)
-    per_point = max(r[0] for r in res) * scale
-    value = P / per_point
-    return dict(value=value, unit=UNIT, cores=P, kind="port",
-                sample=f"FP64 numpy oracle, {P} frequencies x {nmax_s + 1} of {w['nmax'] + 1} bounces "
-                       f"({P} spawned processes, one per core), extrapolated x{scale:.2f} in propagations; "
-                       f"pool wall {wall:.1f}s")
+        pool.map(_cpu_worker, [(w, float(w["freqs"][0]), 0)] * P)   # start-up and imports
+        wall, per = cpu_sample(pool, w, sample_freqs(w, P), w["nmax"])
+    return dict(value=P / max(per), unit=UNIT, cores=P, kind="port",
+                sample=f"FP64 numpy oracle cheerleader, {P} of the {len(w['freqs'])} frequencies at the full "
+                       f"{w['nmax'] + 1} bounces ({P} spawned processes, one per core); sample wall {wall:.1f}s")
 
 
 def _cpu_tf_worker(fi):
@@ -203,8 +213,8 @@ def measured_peaks():
 
 
 def simt_peaks():
-    """FP32 / FP64 / TF32 rates measured on this machine's GB300 by
-    `bench.py --workload peaks` (profiles/simt_peaks.json), or None."""
+    """FP32 / FP64 / TF32 rates measured on this machine's GB300 with hand-written
+    FFMA/DFMA probes and a cuBLAS TF32 GEMM (profiles/simt_peaks.json), or None."""
     p = os.path.join(REPO, "profiles", "simt_peaks.json")
     if os.path.exists(p):
         try:
@@ -219,7 +229,7 @@ def measured_tf32_peak():
     measured bf16 GEMM rate (burst)."""
     sp = simt_peaks()
     if sp and sp.get("tf32_cublas_tflops"):
-        return float(sp["tf32_cublas_tflops"]), "measured (cuBLAS TF32 GEMM, bench.py --workload peaks)"
+        return float(sp["tf32_cublas_tflops"]), "measured (cuBLAS TF32 GEMM, profiles/simt_peaks.json)"
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
@@ -289,6 +299,17 @@ def run_ours(args):
     errs = np.abs(b_mixed - b_fp64) / np.abs(b_fp64)
     rel_err = float(np.max(errs))
     rel_err_med = float(np.median(errs))
+    # the same batch's beta^2 against the oracle at the fixture's frequencies
+    # (tests/golden/make_c2_fixture.py: the oracle's cheerleader at full size)
+    vs_oracle = None
+    fxp = os.path.join(REPO, "tests", "golden", "c2_cheerleader_oracle.npz")
+    if os.path.exists(fxp) and nf == 256 and nmax == 400 and rank == 0:
+        fx = np.load(fxp)
+        if np.array_equal(w["freqs"][fx["freq_index"]], fx["freqs"]):
+            bm = out_beta2.cpu().numpy()[fx["freq_index"]]
+            e = np.abs(bm - fx["beta2"]) / np.abs(fx["beta2"])
+            vs_oracle = {"max": float(np.max(e)), "freq_index": [int(i) for i in fx["freq_index"]],
+                         "per_freq": [float(x) for x in e]}
     # the plain FP64 single-stack path (one frequency per solve)
     t0 = time.perf_counter()
     st.cheerleader(w["freqs"][:1], nmax=nmax, precision="fp64")
@@ -378,13 +399,11 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64 (fields, FFTs), f64 (phase kz*dz, exit accumulation)",
         "data": "synthetic (seeded geometry, no dataset)",
-        "config": {"workload": w["name"] + f"-{nf}f-{nmax + 1}bounces", "grid": N,
-                   "disks": (len(w["distance"]) - 2) // 2, "freqs": nf, "bounces": nmax + 1,
-                   "precision": "mixed", "per_gpu_request": "one 256-frequency request per GPU",
-                   "l2": "no flush: per-step working set (phasor tables + fields) > L2"},
+        "config": c2_config(w),
         "beta2_rel_err_vs_fp64": rel_err,
         "beta2_rel_err_vs_fp64_median": rel_err_med,
         "beta2_checked_freqs": int(len(sub)),
+        "beta2_rel_err_vs_oracle": vs_oracle,
         "plain_fp64_single_freqpts_per_s": fp64_single,
         "gpu_launches": launches,
         "roofline": roof,
@@ -393,7 +412,7 @@ def run_ours(args):
         "clocks": clk,
     }
     if ws == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(w, nmax_s=args.cpu_nmax)
+        line["cpu_baseline"] = cpu_baseline(w)
     assert np.all(np.isfinite(b2_e2e))
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -491,12 +510,13 @@ def run_transformer(args):
     h.set_profiling(False)
     ms_tc = e0.elapsed_time(e1) / args.steps
     tf32_peak, tf32_src = measured_tf32_peak()
-    # three MMAs (hi*hi, hi*lo, lo*hi) per product of the real-form GEMM
-    tc_tensor = 3.0 * tc_fl / (tc_ms / 1000.0) / 1e12
+    # the executed MMA work: three MMAs (hi*hi, hi*lo, lo*hi) per product of
+    # the real-row GEMMs, counted by the library
+    tc_tensor = tc_fl / (tc_ms / 1000.0) / 1e12
     N = len(w["X"])
     sp = simt_peaks()
     if sp and sp.get("fp32_ffma_tflops"):
-        peak_fp32, fp32_src = float(sp["fp32_ffma_tflops"]), "measured (FFMA probe, bench.py --workload peaks)"
+        peak_fp32, fp32_src = float(sp["fp32_ffma_tflops"]), "measured (FFMA probe, profiles/simt_peaks.json)"
     else:
         peak_fp32, fp32_src = 152 * 128 * 2 * 2.07e9 / 1e12, "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)"
     line = {"metric": f"beta2 freq-points/s (transformer, 20 disks + surface maps, {nm} LG modes, {N}x{N}, {nf} freqs)",
@@ -529,7 +549,7 @@ def run_transformer(args):
                 "value": nf / (ms_tc / 1000.0), "unit": UNIT, "ms_per_step": ms_tc,
                 "beta2_rel_err_vs_fp64": float(np.max(errs_tc)),
                 "beta2_rel_err_vs_fp64_median": float(np.median(errs_tc)),
-                "note": "BF_PREC_TF32: overlap GEMMs on tcgen05 (split TF32); outside the 1e-4 bar",
+                "note": "BF_PREC_TF32: real-row class GEMMs on tcgen05 (split TF32, accumulator drained every 32 K)",
                 "roofline": {"bound": "tensor", "achieved": tc_tensor, "peak": tf32_peak, "unit": "TFLOP/s",
                              "frac": tc_tensor / tf32_peak, "peak_source": tf32_src,
                              "kernel": "k_tc_gemm_tf32x3 (whole propagation-matrix phase)",
@@ -630,14 +650,67 @@ def run_uneven(args):
          "clocks": clocks})
 
 
+def _size_class(r):
+    """Latency class of a request: solver, disk count band, grid, frequency band."""
+    nd = r["ndisk"]
+    band = "5-20" if nd <= 20 else ("21-40" if nd <= 40 else "41-80")
+    nfb = "64-256" if len(r["freqs"]) <= 256 else "257-1024"
+    return f"{r['solver']} {band} disks {r['n']}^2 {nfb} f"
+
+
+def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0):
+    """Open-loop arrivals: a Poisson process of `rate` requests/s for
+    `seconds`, each arrival assigned to a uniformly drawn client; the
+    dispatcher submits at the scheduled time whatever the state of earlier
+    requests (a client's requests queue behind each other on its stack).  A
+    request's latency runs from its scheduled arrival to its completion: the
+    server's submit-to-completion time plus the dispatcher's lag.  Completions
+    are collected after the window (no polling thread competes with the
+    dispatcher); requests still pending `drain_s` after the window are
+    counted as unfinished.  Returns (records, wall seconds from the first
+    arrival to the last completion, arrivals, unfinished, failed)."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.poisson(rate * seconds))
+    t_arr = np.sort(rng.uniform(0.0, seconds, n))
+    who = rng.integers(0, nclients, n)
+    sent = []
+    t0 = time.perf_counter()
+    for i in range(n):
+        dt = t0 + t_arr[i] - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        lag = time.perf_counter() - (t0 + t_arr[i])
+        rid, cls = submit_one(int(who[i]))
+        sent.append((rid, {"client": int(who[i]), "cls": cls, "lag_s": lag}))
+    deadline = time.perf_counter() + drain_s
+    recs, unfinished, failed = [], 0, 0
+    first, last = None, None
+    for rid, meta in sent:
+        try:
+            res = srv.wait(rid, timeout_ms=int(max(0.0, deadline - time.perf_counter()) * 1000))
+        except TimeoutError:
+            unfinished += 1
+            continue
+        except Exception:
+            failed += 1
+            continue
+        t_first = res["t_submit"] - meta["lag_s"]
+        first = t_first if first is None else min(first, t_first)
+        last = res["t_done"] if last is None else max(last, res["t_done"])
+        recs.append(dict(meta, latency_ms=1e3 * (res["t_done"] - res["t_submit"] + meta["lag_s"])))
+    wall = (last - first) if recs else seconds
+    return recs, wall, n, unfinished, failed
+
+
 def run_serve(args, optimiser_class=False):
-    """Serving loop: 32 disk-position optimiser clients, each with its own
-    resident stack; every step moves the gaps by N(0, 10 um) (bf_request.distance),
-    submits, waits for beta^2 and thinks for an exponential time of mean
-    32/2000 s (2000 requests/s offered when the service is instant).  Stacks
-    follow the uneven-batch distribution, or, with optimiser_class, are all
+    """Serving loop, open loop: boost-factor solves arrive as a Poisson
+    process of mean rate --rate (2000 requests/s) for --serve-seconds; each
+    arrival is a step of one of 32 disk-position optimiser clients (drawn
+    uniformly), which moves that client's gaps by N(0, 10 um) and submits a
+    solve of its resident stack (bf_request.distance).  Stacks follow the
+    uneven-batch size distribution, or, with optimiser_class, are all
     20-disk, 256-frequency transformer requests (8 Laguerre-Gauss modes,
-    128x128 over 1 m)."""
+    128x128 over 1 m).  Latency percentiles are reported per request class."""
     import torch
     torch.cuda.set_device(0)
     import build as _b
@@ -660,35 +733,23 @@ def run_serve(args, optimiser_class=False):
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
     # one warm-up step per client (builds the resident overlaps / plans), untimed
     for (st, m), r in zip(stacks, reqs):
-        srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision="mixed"))
+        srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision=args.serve_precision))
     srv.close()
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
-    deadline = time.perf_counter() + args.serve_seconds
-    errors = []
+    rngs = [np.random.default_rng(1000 + k) for k in range(nclients)]
+    dist = [np.array(r["distance"]) for r in reqs]
+    classes = [_size_class(r) for r in reqs]
 
-    def client(k):
-        rng = np.random.default_rng(1000 + k)
+    def submit_one(k):
+        dist[k] = W.optimiser_step(dist[k], rngs[k])
         st, m = stacks[k]
         r = reqs[k]
-        d = np.array(r["distance"])
-        try:
-            while time.perf_counter() < deadline:
-                d = W.optimiser_step(d, rng)
-                srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, distance=d, nmax=r["nmax"],
-                                    precision="mixed"))
-                time.sleep(rng.exponential(nclients / 2000.0))
-        except Exception as e:  # reported in the JSON line
-            errors.append(repr(e))
+        return srv.submit(st, r["freqs"], r["solver"], modes=m, distance=dist[k], nmax=r["nmax"],
+                          precision=args.serve_precision), classes[k]
 
     clock = ClockSampler(0)
     clock.start()
-    t0 = time.perf_counter()
-    threads = [threading.Thread(target=client, args=(k,)) for k in range(nclients)]
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    wall = time.perf_counter() - t0
+    recs, wall, n_arr, unfinished, failed = _open_loop(srv, nclients, args.rate, args.serve_seconds, submit_one)
     clocks = clock.stop()
     st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
     srv.close()
@@ -697,18 +758,30 @@ def run_serve(args, optimiser_class=False):
             m.close()
         st.close()
     h.close()
+    lat = np.array([r["latency_ms"] for r in recs]) if recs else np.zeros(1)
+    per_class = {}
+    for cl in sorted(set(r["cls"] for r in recs)):
+        v = np.array([r["latency_ms"] for r in recs if r["cls"] == cl])
+        per_class[cl] = {"requests": int(len(v)), "p50_ms": float(np.percentile(v, 50)),
+                         "p99_ms": float(np.percentile(v, 99)), "max_ms": float(v.max())}
+    fpts = float(sum(len(reqs[r["client"]]["freqs"]) for r in recs))
     name = ("20-disk 256-frequency transformer requests (8 LG modes, 128x128)" if optimiser_class
             else "stacks of the uneven-batch distribution")
     _server_line(
-        f"beta2 freq-points/s and p50/p99 latency, 32 optimiser clients, {name}",
-        st_all["freq_points"] / wall, st_all["completed"], wall,
+        f"beta2 freq-points/s and p50/p99 latency, Poisson arrivals at {args.rate:g}/s from 32 optimiser clients, "
+        f"{name}",
+        fpts / wall, len(recs), wall,
         {"config": {"workload": "serve-optimiser-class" if optimiser_class else "serve-uneven-mix",
-                    "clients": nclients, "think_mean_ms": 1000.0 * nclients / 2000.0, "seconds": args.serve_seconds,
-                    "workers": args.workers, "hbm_budget_gb": 180, "gap_step_um": 10},
-         "latency_ms": {"p50": st_all["p50_ms"], "p99": st_all["p99_ms"], "mean": st_all["mean_ms"],
-                        "max": st_all["max_ms"]},
-         "requests_per_s": st_all["completed"] / wall, "per_solver": {"dancer": st_d, "transformer": st_t},
-         "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
+                    "arrivals": "poisson", "rate_per_s": args.rate, "clients": nclients,
+                    "seconds": args.serve_seconds, "workers": args.workers, "hbm_budget_gb": 180,
+                    "gap_step_um": 10, "precision": args.serve_precision},
+         "offered": n_arr, "completed": len(recs), "unfinished_after_drain": unfinished, "failed": failed,
+         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                        "mean": float(lat.mean()), "max": float(lat.max())},
+         "latency_by_class": per_class,
+         "requests_per_s": len(recs) / wall, "per_solver": {"dancer": st_d, "transformer": st_t},
+         "dispatch_lag_ms_p99": float(np.percentile([1e3 * r["lag_s"] for r in recs], 99)) if recs else None,
+         "evictions": st_all["evictions"], "batched": st_all.get("batched"), "clocks": clocks})
 
 
 def run_serve_pgrid(args):
@@ -904,49 +977,17 @@ def run_c1(args):
 
 
 def run_peaks(args):
-    """Measured arithmetic peaks of this GPU, the denominators of the SIMT and
-    TF32 rooflines: FP32 FFMA, packed FP32x2 FFMA and FP64 DFMA from the
-    probes in boostfractor.jl_gb300/peaks/bf_peaks.cu (8 independent chains per
-    thread, 8 CTAs of 256 threads per SM, best of 5 launches), and the TF32
-    tensor-core rate of a cuBLAS 8192^3 FP32 GEMM with TF32 allowed."""
-    import ctypes
-    import torch
-    torch.cuda.set_device(0)
-    import build as _b
-    path = _b.build_peaks()
-    L = ctypes.CDLL(path)
-    L.bf_peak_probe.restype = ctypes.c_int
-    L.bf_peak_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-    clock = ClockSampler(0)
-    clock.start()
-    out = {}
-    for name, kind, iters in (("fp32_ffma_tflops", 0, 20000), ("fp32x2_ffma2_tflops", 1, 10000), ("fp64_dfma_tflops", 2, 400)):
-        v = ctypes.c_double(0.0)
-        if L.bf_peak_probe(kind, iters, 5, 8, ctypes.byref(v)) != 0:
-            raise RuntimeError(f"peak probe {name} failed")
-        out[name] = v.value
-    torch.backends.cuda.matmul.allow_tf32 = True
-    n = 8192
-    a = torch.randn(n, n, device="cuda")
-    b = torch.randn(n, n, device="cuda")
-    for _ in range(3):
-        a @ b
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    best = 0.0
-    for _ in range(5):
-        e0.record()
-        for _ in range(10):
-            a @ b
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, 10 * 2.0 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
-    out["tf32_cublas_tflops"] = best
-    out["clocks"] = clock.stop()
-    out["method"] = ("FFMA/FFMA2/DFMA: hand-written probes, 8 chains per thread, SMs x 8 CTAs x 256 threads, "
-                     "best of 5; TF32: torch.matmul 8192^3 FP32 with allow_tf32, best of 5 x 10")
-    print(json.dumps({"metric": "measured arithmetic peaks", "value": out["fp32_ffma_tflops"], "unit": "TFLOP/s",
-                      "peaks": out}), flush=True)
+    """The measured arithmetic peaks that are the denominators of the SIMT and
+    TF32 rooflines (FP32 FFMA, packed FP32x2 FFMA, FP64 DFMA and a cuBLAS
+    8192^3 TF32 GEMM on this machine's GB300), as recorded in
+    profiles/simt_peaks.json with the method that measured them."""
+    sp = simt_peaks()
+    if not sp:
+        print(json.dumps({"metric": "measured arithmetic peaks", "unavailable": "profiles/simt_peaks.json missing"}),
+              flush=True)
+        return
+    print(json.dumps({"metric": "measured arithmetic peaks", "value": sp["fp32_ffma_tflops"], "unit": "TFLOP/s",
+                      "source": "profiles/simt_peaks.json (recorded measurement)", "peaks": sp}), flush=True)
 
 
 def run_1d(args):
@@ -1023,7 +1064,7 @@ def run_1d(args):
     nregions = len(eps) - 1
     flops = 52.0 * nregions * nconf * nf
     sp = simt_peaks()
-    fp64_peak, fp64_src = ((float(sp["fp64_dfma_tflops"]), "measured (DFMA probe, bench.py --workload peaks)")
+    fp64_peak, fp64_src = ((float(sp["fp64_dfma_tflops"]), "measured (DFMA probe, profiles/simt_peaks.json)")
                            if sp and sp.get("fp64_dfma_tflops") else (1.25, "nominal"))
     line = {"metric": "beta2 freq-points/s (batched 1D model, 20-disk booster, spacing configurations x frequencies)",
             "value": nconf * nf / (kms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
@@ -1044,7 +1085,24 @@ def run_1d(args):
     print(json.dumps(line), flush=True)
 
 
+def c2_config(w):
+    """The `config` of the cheerleader workload, the same on both arms."""
+    nf, nmax = len(w["freqs"]), w["nmax"]
+    return {"workload": w["name"] + f"-{nf}f-{nmax + 1}bounces", "grid": len(w["X"]),
+            "disks": (len(w["distance"]) - 2) // 2, "freqs": nf, "bounces": nmax + 1,
+            "precision": "mixed", "per_gpu_request": f"one {nf}-frequency request per GPU",
+            "l2": "no flush: per-step working set (phasor tables + fields) > L2"}
+
+
 def run_reference(args):
+    """The reference's algorithm on the host cores.  The reference is Julia
+    (FFTW/LAPACK), which this machine does not have, so its FP64 numpy
+    restatement (the oracle, pinned to the reference's golden vectors) runs
+    instead, on every host core.  A step is a bounded sample of the request:
+    as many of its frequencies as there are cores, each solved at the full
+    bounce count by one process; freq-points/s = sample size / step wall.
+    The warm-up steps start the process pool and run a one-bounce solve per
+    process (imports, FFT set-up); a CPU solve has no other state to warm."""
     ws, rank, local = dist_env()
     if rank != 0:
         return
@@ -1054,25 +1112,34 @@ def run_reference(args):
     if args.nmax is not None:
         over["nmax"] = args.nmax
     w = workload(0, **over)
-    for _ in range(max(args.warmup, 0)):
-        cpu_baseline(w, nmax_s=2)
-    vals = []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        cb = cpu_baseline(w, nmax_s=args.cpu_nmax)
-        vals.append(cb["value"])
-    wall = time.perf_counter() - t0
-    value = statistics.median(vals)
-    cb["value"] = value
+    P = os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    walls, per_proc = [], []
+    with ctx.Pool(P) as pool:
+        for k in range(max(args.warmup, 0)):
+            cpu_sample(pool, w, sample_freqs(w, P, k), 0)
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            wall, per = cpu_sample(pool, w, sample_freqs(w, P, k), w["nmax"])
+            walls.append(wall)
+            per_proc.append(max(per))
+        timed = time.perf_counter() - t0
+    ms_step = 1000.0 * timed / max(args.steps, 1)
+    value = P / (ms_step / 1000.0)
+    cb = dict(value=value, unit=UNIT, cores=P, kind="port",
+              sample=f"per step {P} of the {len(w['freqs'])} frequencies (shifted by one index per step), "
+                     f"each at the full {w['nmax'] + 1} bounces in one of {P} spawned processes; "
+                     f"FP64 numpy oracle cheerleader")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * len(w["freqs"]) / value,
+            "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (FP64 oracle)",
             "data": "synthetic (seeded geometry, no dataset)",
-            "config": {"workload": w["name"] + f"-{len(w['freqs'])}f-{w['nmax'] + 1}bounces"},
+            "config": c2_config(w),
             "impl": "reference", "cpu_baseline": cb,
-            "reference_note": "the reference is Julia (not installed); its algorithm runs as the FP64 numpy "
-                              "restatement pinned to the reference's golden vectors",
-            "wall_s": wall,
+            "reference_note": "the reference is Julia (not installed here or on the GPU box); its algorithm runs "
+                              "as the FP64 numpy restatement pinned to the reference's golden vectors",
+            "step_wall_s": {"median": statistics.median(walls), "max": max(walls)} if walls else None,
+            "slowest_process_s_median": statistics.median(per_proc) if per_proc else None,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1085,14 +1152,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nf", type=int, default=0, help="override frequency count (testing only)")
     ap.add_argument("--nmax", type=int, default=None, help="override nmax (testing only)")
-    ap.add_argument("--cpu-nmax", type=int, default=60, help="bounces-1 of the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="cheerleader",
                     choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d", "peaks",
                              "c1", "pgrid"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
-    ap.add_argument("--serve-seconds", type=float, default=30.0)
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--rate", type=float, default=2000.0, help="serving: mean Poisson arrival rate, requests/s")
+    ap.add_argument("--serve-precision", default="mixed", help="serving: precision of the transformer requests")
     args = ap.parse_args()
     if args.workload == "transformer" and args.impl == "ours":
         run_transformer(args)

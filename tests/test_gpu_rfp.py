@@ -314,3 +314,28 @@ def test_invalid_arguments_raise(B):
         B.cheerleader(0, 5, sb, c, f=20e9, handle=h)
     assert e.value.code == 2
     h.close()
+
+
+def test_cheerleader_full_size_vs_oracle_fixture(B):
+    """The full 20-disk cheerleader workload (128x128, per-disk tilts, 401
+    bounces) at four of its 256 frequencies, one of them the spectrum's
+    maximum, against the oracle's exit fields stored by
+    tests/golden/make_c2_fixture.py: FP64 exit field within 1e-10, mixed
+    beta^2 within 1e-4 (src/boost_fractor_recurprop.jl:226-363)."""
+    import os
+    from bfgb300 import workloads as W
+    fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "c2_cheerleader_oracle.npz"))
+    w = W.config2_cheerleader()
+    assert np.array_equal(w["freqs"][fx["freq_index"]], fx["freqs"])
+    c = B.SeedCoordinateSystem(X=w["X"], Y=w["Y"])
+    sb = B.SeedSetupBoundaries(c, diskno=(len(w["distance"]) - 2) // 2, distance=w["distance"],
+                               epsilon=w["eps"], relative_tilt_x=w["relative_tilt_x"],
+                               relative_tilt_y=w["relative_tilt_y"])
+    st = B.Stack(sb, c, w["diskR"])
+    R64, _, b64 = st.cheerleader(fx["freqs"], nmax=w["nmax"], precision="fp64")
+    _, _, b32 = st.cheerleader(fx["freqs"], nmax=w["nmax"], precision="mixed")
+    st.close()
+    for k in range(len(fx["freqs"])):
+        assert rel(R64[k], fx["exit_field"][k]) < FP64_TOL
+        assert abs(b64[k] - fx["beta2"][k]) / fx["beta2"][k] < FP64_TOL
+        assert abs(b32[k] - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
