@@ -22,12 +22,12 @@ import threading
 import numpy as np
 
 from . import _lib
-from ._lib import BFError
+from ._lib import BFError, SingularError
 
 __all__ = [
     "CoordinateSystem", "SeedCoordinateSystem", "SetupBoundaries", "SeedSetupBoundaries",
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
-    "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError",
+    "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError", "SingularError",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
     "gauss_profile", "unnormalized_match", "transformer_coupled", "transformer_1d_batch",
@@ -64,7 +64,8 @@ class Handle:
     def check(self, rc):
         if rc != _lib.BF_OK:
             msg = _lib.lib().bf_last_error(self._h)
-            raise BFError(rc, msg.decode() if msg else "")
+            cls = SingularError if rc == _lib.BF_ERR_SINGULAR else BFError
+            raise cls(rc, msg.decode() if msg else "")
 
     def device_bytes(self):
         return int(_lib.lib().bf_device_bytes(self._h))

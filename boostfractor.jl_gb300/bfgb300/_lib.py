@@ -16,6 +16,7 @@ BF_ERR_NOMEM = 2
 BF_ERR_CUDA = 3
 BF_ERR_TIMEOUT = 4
 BF_ERR_UNSUPPORTED = 5
+BF_ERR_SINGULAR = 6
 
 BF_PROP_3D = 0
 BF_PROP_NOTILTS = 1
@@ -114,6 +115,7 @@ _SIGS = {
     "bf_calc_propagation_matrices": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl]),
     "bf_transformer": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                 _p_dbl, _p_dbl, _p_dbl]),
+    "bf_test_tc_withhold_loads": (_c_int, [_c_int]),
 }
 
 _lib = None
@@ -144,6 +146,12 @@ class BFError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"bf error {code}: {msg}")
         self.code = code
+
+
+class SingularError(BFError):
+    """An exactly singular propagation matrix or boundary system: where the
+    reference's inv / \\ raise SingularException
+    (src/boost_fractor_transformer.jl:247,346,356)."""
 
 
 def ptr(a):

@@ -58,12 +58,16 @@ size_t split_tile_bytes(int N, int nby, int nfreq, int nsteps, bool fp64);
 bool split_stage(int nsteps, int nfreq);
 
 // ---- split-TF32 tensor-core GEMM (bf_tcgemm.cu) --------------------------
-// planes[z][m][n] (FP32) = sum over the z-th of `splits` K slices of
+// out[z][n][m] (FP32) = sum over the z-th of `splits` K slices of
 // (Ahi Bhi + Ahi Blo + Alo Bhi)[m][n]; A [M][Kp], B [N][Kp] row-major FP32
-// holding TF32-rounded hi/lo parts, Kp a multiple of 32, bases 16-byte
-// aligned.  *d_err becomes non-zero if a bounded wait in the kernel expired.
+// holding TF32-rounded hi/lo parts, M a multiple of 128, Kp of 32, bases
+// 16-byte aligned.  The tensor-memory accumulator is drained into FP32
+// registers every 32 K-elements.  *d_err becomes non-zero if a bounded wait in
+// the kernel expired.
 int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
-                   int splits, float* planes, int* d_err, cudaStream_t st);
+                   int splits, float* out, int* d_err, cudaStream_t st);
+// K slices for an M x N x Kp product: enough work units to keep every SM busy.
+int tc_gemm_splits(int M, int N, int Kp);
 bool tc_gemm_available();
 
 // ---- phasor / tilt tables (FP64 phase arguments) -----------------------

@@ -294,11 +294,12 @@ __device__ __forceinline__ C crecip(C v) {
 // |W[p][c]|^2, lowest row on ties) is a warp-shuffle argmax, then one over
 // the warps; its reciprocal is computed once and broadcast.  Magnitudes and
 // the reciprocal use the matrix's own precision: a warp-wide FP64 instruction
-// costs the same with one lane active, at 1/64 of the FP32 rate.  A zero
-// pivot gives inf/NaN, which propagates to the solver's outputs (where Julia's
-// inv raises SingularException).
+// costs the same with one lane active, at 1/64 of the FP32 rate.  An exactly
+// zero pivot (LAPACK getrf's info > 0, where Julia's inv raises
+// SingularException) records `tag` in *sing (atomicMin); the inverse is then
+// inf/NaN.
 template <typename C>
-__device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* red_i) {
+__device__ void cta_invert(C* M, C* W, int n, int* sing, int tag, double* red_v, int* red_i) {
   using R = decltype(C().x);
   constexpr unsigned FULL = 0xffffffffu;
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = (nt + 31) >> 5;
@@ -351,6 +352,7 @@ __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* re
     __syncthreads();
     if (tid == 0) {
       const C w = W[c * w2 + c];
+      if (w.x == (R)0 && w.y == (R)0) atomicMin(sing, tag);
       const R d = w.x * w.x + w.y * w.y;
       *inv_s = mk(w.x / d, -w.y / d);
     }
@@ -372,7 +374,6 @@ __device__ void cta_invert(C* M, C* W, int n, int* piv_s, double* red_v, int* re
   }
   for (int e = tid; e < n * n; e += nt) M[e] = W[(e / n) * w2 + n + (e % n)];
   __syncthreads();
-  (void)piv_s;
 }
 
 }  // namespace bf

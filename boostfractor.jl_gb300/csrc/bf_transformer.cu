@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <complex>
 #include <map>
@@ -224,76 +225,224 @@ __device__ __forceinline__ void tf32_split_d(double x, float& hi, float& lo) {
 }
 
 // ---- operands of the tensor-core class GEMMs (BF_PREC_TF32) -------------------
-// The complex product G = A B becomes the real product [Gr; Gi] = A'' B'' with
-// A'' = [[Ar, -Ai], [Ai, Ar]] (2R x 2Kp) and B'' = [Br; Bi] (2Kp x N), both
-// stored K-major (B'' transposed, [N][2Kp]) as TF32 hi/lo pairs.  Columns
-// [0, K) hold real parts, [Kp, Kp + K) imaginary parts, the rest are zero.
-__device__ __forceinline__ void put_a2(float* Ahi, float* Alo, int R, int Kp, int row, int k, double re, double im) {
-  const size_t w = 2 * (size_t)Kp;
-  float h, l;
-  tf32_split_d(re, h, l);
-  Ahi[(size_t)row * w + k] = h;
-  Alo[(size_t)row * w + k] = l;
-  Ahi[(size_t)(R + row) * w + Kp + k] = h;
-  Alo[(size_t)(R + row) * w + Kp + k] = l;
-  tf32_split_d(im, h, l);
-  Ahi[(size_t)(R + row) * w + k] = h;
-  Alo[(size_t)(R + row) * w + k] = l;
-  Ahi[(size_t)row * w + Kp + k] = -h;
-  Alo[(size_t)row * w + Kp + k] = -l;
-}
-__device__ __forceinline__ void put_bt(float* Bhi, float* Blo, int Kp, int c, int k, float re, float im) {
-  const size_t w = 2 * (size_t)Kp;
-  float h, l;
-  tf32_split(re, h, l);
-  Bhi[(size_t)c * w + k] = h;
-  Blo[(size_t)c * w + k] = l;
-  tf32_split(im, h, l);
-  Bhi[(size_t)c * w + Kp + k] = h;
-  Blo[(size_t)c * w + Kp + k] = l;
+// Both classes are Hermitian in the mode pair, so the tensor cores see the
+// real-row form of the mixed path: A = the real rows of the upper triangle
+// (Re and Im of W[mm'] or V[mm'] for m <= m', rows 2t and 2t + 1, padded with
+// zero rows to a multiple of 128) and B^T = the complex operand column c as
+// two real rows 2c (Re) and 2c + 1 (Im), all K-major TF32 hi/lo pairs with K
+// padded to a multiple of 32.  The GEMM runs on B - c(column) instead of B,
+// where the constant c is the operand's value at the centre of its domain
+// (k-space: exp(-i k0 dz), the transverse-momentum-zero phasor; pixels: 1,
+// an untilted flat disk); P adds c times the FP64 row sums of A back.  The
+// summed terms are then ~|B - c| instead of ~1, which scales down every
+// rounding error of the products and of the sums.
+
+// exp(re + i im) - 1 as complex64, accurate relative to its own (often small)
+// magnitude: the phase is reduced to [-pi, pi] in FP64, then
+// cos t - 1 = -2 sin^2(t/2) and expm1 avoid the cancellation of exp - 1.
+__device__ __forceinline__ float2 cexpm1_f(double re, double im) {
+  const double r = im - 6.283185307179586 * rint(im * 0.15915494309189535);
+  const float t = (float)r;
+  const float h = sinf(0.5f * t), sn = sinf(t);
+  const float cm1 = -2.0f * h * h;
+  const float em = expm1f((float)re);
+  return make_float2(fmaf(em, 1.0f + cm1, cm1), (em + 1.0f) * sn);
 }
 
-// A'' of the k-space class from the FP64 orbit sums (rows mm = m nm + m')
-__global__ void k_build_w_t(float* Ahi, float* Alo, const double2* U, const double2* Phi, const int* members, int K,
-                            int Kp, int msz, int nm, int npix, double scale) {
+__device__ __forceinline__ void put_tf32(float* hi, float* lo, size_t i, float v) {
+  float h, l;
+  tf32_split(v, h, l);
+  hi[i] = h;
+  lo[i] = l;
+}
+__device__ __forceinline__ void put_tf32_d(float* hi, float* lo, size_t i, double v) {
+  float h, l;
+  tf32_split_d(v, h, l);
+  hi[i] = h;
+  lo[i] = l;
+}
+
+// A of the k-space class: the real rows of k_build_wr as TF32 pairs [Mp][Kp]
+// (zero for o >= K; rows >= 2T are zeroed beforehand), and the same rows in
+// FP64 (Ad [2T][K]) for the row sums.
+__global__ void k_build_wr_tc(float* Ah, float* Al, double* Ad, const double2* U, const double2* Phi,
+                              const int* members, const int2* tri, int K, int Kp, int msz, int npix, double scale) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  const int mm = blockIdx.y;
-  if (o >= K) return;
-  const int m = mm / nm, mp = mm % nm;
-  double2 acc = make_double2(0.0, 0.0);
-  for (int q = 0; q < msz; ++q) {
-    const int k = members[(size_t)o * msz + q];
-    if (k < 0) break;
-    const double2 u = U[(size_t)m * npix + k], p = Phi[(size_t)mp * npix + k];
-    acc.x += u.x * p.x + u.y * p.y;
-    acc.y += u.x * p.y - u.y * p.x;
-  }
-  put_a2(Ahi, Alo, nm * nm, Kp, mm, o, acc.x * scale, acc.y * scale);
-}
-
-// A'' of the pixel class: conj(Psi_m(x_s)) Psi_m'(x_s)
-__global__ void k_build_v_t(float* Ahi, float* Alo, const double2* pat, const int* supp, int Kd, int Kdp, int nm,
-                            int npix) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int mm = blockIdx.y;
-  if (s >= Kd) return;
-  const int m = mm / nm, mp = mm % nm;
-  const int x = supp[s];
-  const double2 a = pat[(size_t)m * npix + x], b = pat[(size_t)mp * npix + x];
-  put_a2(Ahi, Alo, nm * nm, Kdp, mm, s, a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
-
-// G[r][n] = (sum_z planes[z][r][n], sum_z planes[z][R + r][n]), planes in order
-__global__ void k_planes_to_g(double2* G, const float* planes, int R, int N, int splits) {
-  const size_t n_out = (size_t)R * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n_out; i += (size_t)gridDim.x * blockDim.x) {
-    double re = 0.0, im = 0.0;
-    for (int z = 0; z < splits; ++z) {
-      const float* pz = planes + (size_t)z * 2 * n_out;
-      re += (double)pz[i];
-      im += (double)pz[n_out + i];
+  const int t = blockIdx.y;
+  if (o >= Kp) return;
+  double re = 0.0, im = 0.0;
+  if (o < K) {
+    const int2 mp = tri[t];
+    double2 acc = make_double2(0.0, 0.0);
+    for (int q = 0; q < msz; ++q) {
+      const int k = members[(size_t)o * msz + q];
+      if (k < 0) break;
+      const double2 u = U[(size_t)mp.x * npix + k], p = Phi[(size_t)mp.y * npix + k];
+      acc.x += u.x * p.x + u.y * p.y;
+      acc.y += u.x * p.y - u.y * p.x;
     }
-    G[i] = make_double2(re, im);
+    re = acc.x * scale;
+    im = acc.y * scale;
+    Ad[(size_t)(2 * t) * K + o] = re;
+    Ad[(size_t)(2 * t + 1) * K + o] = im;
+  }
+  put_tf32_d(Ah, Al, (size_t)(2 * t) * Kp + o, re);
+  put_tf32_d(Ah, Al, (size_t)(2 * t + 1) * Kp + o, im);
+}
+
+// A of the pixel class: the real rows of k_build_vr as TF32 pairs [Mp][Kdp]
+// and in FP64 (Ad [2T][Kd]).
+__global__ void k_build_vr_tc(float* Ah, float* Al, double* Ad, const double2* pat, const int* supp,
+                              const int2* tri, int Kd, int Kdp, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.y;
+  if (s >= Kdp) return;
+  double re = 0.0, im = 0.0;
+  if (s < Kd) {
+    const int2 mp = tri[t];
+    const int x = supp[s];
+    const double2 a = pat[(size_t)mp.x * npix + x], b = pat[(size_t)mp.y * npix + x];
+    re = a.x * b.x + a.y * b.y;
+    im = a.x * b.y - a.y * b.x;
+    Ad[(size_t)(2 * t) * Kd + s] = re;
+    Ad[(size_t)(2 * t + 1) * Kd + s] = im;
+  }
+  put_tf32_d(Ah, Al, (size_t)(2 * t) * Kdp + s, re);
+  put_tf32_d(Ah, Al, (size_t)(2 * t + 1) * Kdp + s, im);
+}
+
+// g[r] = sum_k Ad[r][k] in FP64, one CTA of 256 threads per row (fixed order)
+__global__ void k_rowsum(double* g, const double* Ad, int K) {
+  __shared__ double red[256];
+  const int r = blockIdx.x;
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) acc += Ad[(size_t)r * K + k];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) g[r] = red[0];
+}
+
+// Per column c = f * npar + p of the k-space class: kz0 = sqrt(k0^2) (the
+// phasor's transverse-momentum-zero wavenumber) and c0 = exp(-i kz0 dz), FP64.
+__global__ void k_build_c0(double2* KZ0, double2* C0, const double* freqs, int nf, const double2* eps,
+                           const RegionT* regs, const int* par_regions, const int* par_eps, int npar) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nf * npar) return;
+  const int f = c / npar, p = c % npar;
+  const double2 e = eps[par_eps[p]];
+  const double2 k0 = k0_c(kC / freqs[f], e.x, e.y);
+  const double2 kz0 = dsqrt_c(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+  const double dz = regs[par_regions[p]].dz;
+  KZ0[c] = kz0;
+  C0[c] = dexp_c(kz0.y * dz, -kz0.x * dz);
+}
+
+// B^T of the k-space class: rows 2c, 2c + 1 = Re, Im of D[o][c] - c0[c] =
+// c0 (exp(-i (kz - kz0) dz) - 1) as TF32 pairs [2 ncol][Kp], zero for o >= K
+__global__ void k_build_d_tc(float* Bh, float* Bl, const double2* KZ, const double2* KZ0, const double2* C0, int K,
+                             int Kp, int nf, const RegionT* regs, const int* par_regions, const int* par_eps,
+                             int npar) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= Kp) return;
+  const int ncol = nf * npar;
+  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+    float2 v = make_float2(0.f, 0.f);
+    if (o < K) {
+      const int f = c / npar, p = c % npar;
+      const double dz = regs[par_regions[p]].dz;
+      const double2 kz = KZ[((size_t)par_eps[p] * nf + f) * K + o];
+      const double2 kz0 = KZ0[c];
+      const float2 m1 = cexpm1_f((kz.y - kz0.y) * dz, -(kz.x - kz0.x) * dz);
+      const float2 c0 = make_float2((float)C0[c].x, (float)C0[c].y);
+      v = make_float2(c0.x * m1.x - c0.y * m1.y, c0.x * m1.y + c0.y * m1.x);
+    }
+    put_tf32(Bh, Bl, (size_t)(2 * c) * Kp + o, v.x);
+    put_tf32(Bh, Bl, (size_t)(2 * c + 1) * Kp + o, v.y);
+  }
+}
+
+// B^T of the pixel class: rows 2c, 2c + 1 = Re, Im of E[s][c] - 1 (the
+// tilt/surface phase of k_build_e less its untilted, flat value) as TF32
+// pairs [2 ncol][Kdp], zero for s >= Kd
+__global__ void k_build_e_tc(float* Bh, float* Bl, const int* supp, int Kd, int Kdp, int nf, const RegionT* regs,
+                             const int* pix_regions, int npx, const double2* K0, const double* X, const double* Y,
+                             int nx, const double2* surf, int npix) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= Kdp) return;
+  const int ncol = nf * npx;
+  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+    float2 v = make_float2(0.f, 0.f);
+    if (s < Kd) {
+      const int reg = pix_regions[c % npx];
+      const RegionT g = regs[reg];
+      const double2 k0 = K0[c];
+      double re, im;
+      if (g.klass == 2) {
+        re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
+        im = -k0.x * g.dz;
+      } else {
+        const int x = supp[s] % nx, y = supp[s] / nx;
+        const double t = g.tx * X[x] + g.ty * Y[y];
+        re = k0.y * t;
+        im = -k0.x * t;
+        if (surf) {
+          const double2 sv = surf[(size_t)reg * npix + supp[s]];
+          re += k0.x * sv.y + k0.y * sv.x;
+          im -= k0.x * sv.x - k0.y * sv.y;
+        }
+      }
+      v = cexpm1_f(re, im);
+    }
+    put_tf32(Bh, Bl, (size_t)(2 * c) * Kdp + s, v.x);
+    put_tf32(Bh, Bl, (size_t)(2 * c + 1) * Kdp + s, v.y);
+  }
+}
+
+// P from the tensor-core GEMM's output out[z][n][m] (FP32, n = 2c + {Re, Im}
+// of column c, m = real row) with the subtracted constant added back:
+// H[r][c] = sum_z out[z][2c..2c+1][r] + cc[c] g[r] (cc = null: 1), then
+// P[m][m'] = X + iY and P[m'][m] = X - iY with X = H[2t], Y = H[2t+1], as
+// k_scatter_herm; disk regions get diag(DG) from the left.
+template <typename PT>
+__global__ void k_scatter_herm_tc(PT* P, const float* out, int Mp, int splits, const double2* cc, const double* g,
+                                  int nf, int ncols, const RegionT* regs, const int* cls_regions, int nd, int nm,
+                                  const double2* DG, const int2* tri, int T) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  const int2 mp = tri[t];
+  const int ncol = nf * ncols;
+  const size_t plane = (size_t)2 * ncol * Mp;
+  const double g0 = g[2 * t], g1 = g[2 * t + 1];
+  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+    const int f = c / ncols, q = c % ncols;
+    const int j = cls_regions[q];
+    double xr = 0.0, xi = 0.0, yr = 0.0, yi = 0.0;
+    for (int z = 0; z < splits; ++z) {
+      const float2 re = *reinterpret_cast<const float2*>(out + z * plane + (size_t)(2 * c) * Mp + 2 * t);
+      const float2 im = *reinterpret_cast<const float2*>(out + z * plane + (size_t)(2 * c + 1) * Mp + 2 * t);
+      xr += (double)re.x;
+      yr += (double)re.y;
+      xi += (double)im.x;
+      yi += (double)im.y;
+    }
+    const double2 k = cc ? cc[c] : make_double2(1.0, 0.0);
+    xr += k.x * g0;
+    xi += k.y * g0;
+    yr += k.x * g1;
+    yi += k.y * g1;
+    double2 p1 = make_double2(xr - yi, xi + yr);
+    double2 p2 = make_double2(xr + yi, xi - yr);
+    if (DG && regs[j].klass == 1) {
+      p1 = bf::cmul(DG[(size_t)c * nm + mp.x], p1);
+      p2 = bf::cmul(DG[(size_t)c * nm + mp.y], p2);
+    }
+    PT* Pj = P + ((size_t)f * nd + j) * nm * nm;
+    Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
+    if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
   }
 }
 
@@ -310,24 +459,6 @@ __global__ void k_build_d(C* D, const double2* KZ, int K, int nf, const RegionT*
   for (int o = blockIdx.y; o < K; o += gridDim.y) {
     const double2 kz = kzp[o];
     D[(size_t)o * ncol + c] = cexp_as<C>(kz.y * dz, -kz.x * dz);
-  }
-}
-
-// B''^T of the k-space class: row c = f * npar + p, column o (orbit)
-__global__ void k_build_d_t(float* Bhi, float* Blo, const double2* KZ, int K, int Kp, int nf, const RegionT* regs,
-                            const int* par_regions, const int* par_eps, int npar) {
-  const int o = blockIdx.x * blockDim.x + threadIdx.x;
-  if (o >= Kp) return;
-  const int ncol = nf * npar;
-  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
-    float2 v = make_float2(0.f, 0.f);
-    if (o < K) {
-      const int f = c / npar, p = c % npar;
-      const double dz = regs[par_regions[p]].dz;
-      const double2 kz = KZ[((size_t)par_eps[p] * nf + f) * K + o];
-      v = cexp_as<float2>(kz.y * dz, -kz.x * dz);
-    }
-    put_bt(Bhi, Blo, Kp, c, o, v.x, v.y);
   }
 }
 
@@ -386,40 +517,6 @@ __global__ void k_build_e(C* E, const int* supp, int Kd, int nf, const RegionT* 
       }
       E[(size_t)s * ncol + c] = v;
     }
-  }
-}
-
-// B''^T of the pixel class: row c = f * npx + q, column s (support pixel)
-__global__ void k_build_e_t(float* Bhi, float* Blo, const int* supp, int Kd, int Kdp, int nf, const RegionT* regs,
-                            const int* pix_regions, int npx, const double2* K0, const double* X, const double* Y,
-                            int nx, const double2* surf, int npix) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= Kdp) return;
-  const int ncol = nf * npx;
-  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
-    float2 v = make_float2(0.f, 0.f);
-    if (s < Kd) {
-      const int reg = pix_regions[c % npx];
-      const RegionT g = regs[reg];
-      const double2 k0 = K0[c];
-      double re, im;
-      if (g.klass == 2) {
-        re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
-        im = -k0.x * g.dz;
-      } else {
-        const int x = supp[s] % nx, y = supp[s] / nx;
-        const double t = g.tx * X[x] + g.ty * Y[y];
-        re = k0.y * t;
-        im = -k0.x * t;
-        if (surf) {
-          const double2 sv = surf[(size_t)reg * npix + supp[s]];
-          re += k0.x * sv.y + k0.y * sv.x;
-          im -= k0.x * sv.x - k0.y * sv.y;
-        }
-      }
-      v = cexp_as<float2>(re, im);
-    }
-    put_bt(Bhi, Blo, Kdp, c, s, v.x, v.y);
   }
 }
 
@@ -525,7 +622,8 @@ __global__ void k_copy_modes(C* out, const double2* pat, int nm, int npix, int r
 // own precision: FP32 for complex64 (a warp-wide FP64 instruction costs the
 // same with one lane active, at 1/64 of the FP32 rate), FP64 for complex128.
 template <typename C, int NM>
-__global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd, int j0, int nm, int nmat) {
+__global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd, int j0, int nm, int nmat,
+                                                     int* sing) {
   using R = decltype(C().x);
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -563,6 +661,7 @@ __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd
       b[k].y = __shfl_sync(FULL, b[k].y, src);
     }
     if (lane == c) {
+      if (a[c].x == R(0) && a[c].y == R(0)) atomicMin(sing, f);   // exactly singular (LAPACK info > 0)
       const R d = a[c].x * a[c].x + a[c].y * a[c].y;
       const C inv = bf::mk(a[c].x / d, -a[c].y / d);
 #pragma unroll
@@ -593,7 +692,7 @@ __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd
 
 // ---- batched inversion: Pinv[f][j] = inv(P[f][j]), j in [j0, nd) -----------
 template <typename C>
-__global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int j0, int nm) {
+__global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int j0, int nm, int* sing) {
   extern __shared__ __align__(16) unsigned char sm[];
   C* W = reinterpret_cast<C*>(sm);
   double* red_v = reinterpret_cast<double*>(W + 2 * nm * nm);
@@ -603,7 +702,7 @@ __global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int
   C* M = Pinv + off;
   for (int e = threadIdx.x; e < nm * nm; e += blockDim.x) M[e] = P[off + e];
   __syncthreads();
-  bf::cta_invert(M, W, nm, nullptr, red_v, red_i);
+  bf::cta_invert(M, W, nm, sing, f, red_v, red_i);
 }
 
 // ---- batched inversion of complex64 matrices, 16 < nm <= NB, in registers ----
@@ -616,8 +715,10 @@ __global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int
 // After nm steps row p_c expresses x_c in the y_{p_k}: inv[c][p_k] = A[p_c][k].
 // Shared memory carries only the pivot column (double-buffered by step parity)
 // and the scaled pivot row, so each step is 16 complex FMAs per thread against
-// 8 shared loads.  A zero pivot gives inf/NaN, which propagates to the
-// solver's outputs (where Julia's inv raises SingularException).
+// 8 shared loads.  An exactly zero pivot (the remaining column is zero, the
+// case where LAPACK's getrf reports info > 0 and Julia's inv raises
+// SingularException) records the frequency in *sing (atomicMin); the inverse
+// is then inf/NaN.
 __device__ __forceinline__ float2 pick4(const float2 (&v)[4], int s) {
   float2 r = v[0];
   if (s == 1) r = v[1];
@@ -628,7 +729,7 @@ __device__ __forceinline__ float2 pick4(const float2 (&v)[4], int s) {
 
 template <int NB>
 __global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2* P, float2* Pinv, int nd, int j0,
-                                                                  int nm) {
+                                                                  int nm, int* sing) {
   constexpr int NBB = NB / 4, NT = NBB * NBB, RPL = NB / 32;
   constexpr unsigned FULL = 0xffffffffu;
   __shared__ float2 colv[2][NB], rowv[NB];
@@ -682,6 +783,7 @@ __global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2
         if (lane + 32 * q == bi) used[q] = true;
       if (lane == 0) {
         const float2 a = cv[bi];
+        if (a.x == 0.f && a.y == 0.f) atomicMin(sing, f);   // exactly singular (LAPACK info > 0)
         const float s2 = a.x * a.x + a.y * a.y;
         dsh = make_float2(a.x / s2, -a.y / s2);
         psh = bi;
@@ -1047,10 +1149,12 @@ __global__ void __launch_bounds__(256) k_trace_back(const PT* P, const PT* Pinv,
 }
 
 // ---- FP64 boundary solve: boost = -T22 \ ax, refl = -T22 \ (T21 reflect) ----
+// An exactly zero pivot (Julia's `\` raises SingularException there,
+// transformer.jl:346,356) records the frequency in *sing (atomicMin).
 template <typename C>
 __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22g, const double2* axg,
                                                      const double2* reflect, int nm, double2* boost,
-                                                     double2* refl, double* beta2) {
+                                                     double2* refl, double* beta2, int* sing) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int f = blockIdx.x, tid = threadIdx.x, nt = blockDim.x;
   const int w = nm + 2;
@@ -1095,6 +1199,7 @@ __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22
       }
     __syncthreads();
     const double2 piv = A[c * w + c];
+    if (tid == 0 && piv.x == 0.0 && piv.y == 0.0) atomicMin(sing, f);   // T22 exactly singular
     for (int e = tid; e < (nm - c - 1) * (w - c); e += nt) {
       const int r = c + 1 + e / (w - c), k = c + e % (w - c);
       if (k == c) continue;
@@ -1193,9 +1298,11 @@ struct TfCache {
   DBuf Vr, Wr, tri;
   int T = 0;
   bool herm_w = false;
-  // BF_PREC_TF32: A'' of both classes as TF32 hi/lo pairs (K padded to Kp, Kdp)
-  DBuf Wt_hi, Wt_lo, Vt_hi, Vt_lo;
-  int Kp = 0, Kdp = 0;
+  // BF_PREC_TF32: the real rows of both classes as TF32 hi/lo pairs [Mp][Kp],
+  // [Mp][Kdp] (rows padded to a multiple of 128, K to a multiple of 32) and
+  // their FP64 row sums (gW, gV)
+  DBuf Wh, Wl, Vh, Vl, gW, gV;
+  int Kp = 0, Kdp = 0, Mp = 0;
   std::vector<int2> rep_h;
 };
 
@@ -1204,7 +1311,7 @@ static size_t tf_cache_bytes(const void* p) {
   const TfCache* c = static_cast<const TfCache*>(p);
   size_t b = 0;
   for (const DBuf* d : {&c->W, &c->V, &c->Vr, &c->Wr, &c->tri, &c->rep, &c->supp, &c->U, &c->Phi, &c->members,
-                        &c->Wt_hi, &c->Wt_lo, &c->Vt_hi, &c->Vt_lo})
+                        &c->Wh, &c->Wl, &c->Vh, &c->Vl, &c->gW, &c->gV})
     b += d->p ? d->n : 0;
   return b;
 }
@@ -1222,7 +1329,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   // which a stack changes after creation (bf_stack_set_distance moves the
   // disks), so gap updates of an optimiser reuse them.
   if (c.modes_id == md->id && c.mode == mode) return BF_OK;
-  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.Wr, &c.tri, &c.Wt_hi, &c.Wt_lo, &c.Vt_hi, &c.Vt_lo}) d->release();
+  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.Wr, &c.tri, &c.Wh, &c.Wl, &c.Vh, &c.Vl, &c.gW, &c.gV}) d->release();
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -1285,7 +1392,27 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 0, 0, st);
   if (!e) e = bf::launch_line_dft(true, c.Phi.p, nm, nx, ny, 1, 0, st);
   if (e) return bf_fail(h, BF_ERR_CUDA, "mode FFTs failed");
-  c.Kp = (c.K + 15) / 16 * 16;
+  c.Kp = (c.K + 31) / 32 * 32;
+  if (!fp64) {
+    // Phi = FFT(mask Psi) equals U = FFT(Psi) bit for bit when no mode has a
+    // non-zero pixel outside the (0/1) mask; W is then Hermitian in the mode
+    // pair, W[m'm] = conj W[mm'], and its upper triangle determines it.
+    c.herm_w = true;
+    for (int m = 0; m < nm && c.herm_w; ++m)
+      for (size_t x = 0; x < npix; ++x)
+        if (!s->mask_full[x] && md->pat[(size_t)m * npix + x] != cd(0.0, 0.0)) {
+          c.herm_w = false;
+          break;
+        }
+    std::vector<int2> tri;
+    for (int m = 0; m < nm; ++m)
+      for (int mp = m; mp < nm; ++mp) tri.push_back(make_int2(m, mp));
+    c.T = (int)tri.size();
+    c.Mp = (2 * c.T + 127) / 128 * 128;
+    TCKS(c.tri.alloc(h, sizeof(int2) * tri.size()));
+    TCK(cudaMemcpyAsync(c.tri.p, tri.data(), sizeof(int2) * tri.size(), cudaMemcpyHostToDevice, st));
+  }
+  DBuf Ad;   // FP64 real rows of the tensor-core path, for the row sums
   {
     dim3 grid(blocks_for(c.K), nm * nm);
     const double scale = 1.0 / ((double)nx * (double)ny);
@@ -1294,42 +1421,32 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
       k_build_w<double2><<<grid, 256, 0, st>>>(c.W.as<double2>(), c.U.as<double2>(), c.Phi.as<double2>(),
                                                c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
-    } else if (mode == 1) {
-      // Phi = FFT(mask Psi) equals U = FFT(Psi) bit for bit when no mode has a
-      // non-zero pixel outside the (0/1) mask; W is then Hermitian in the mode
-      // pair, W[m'm] = conj W[mm'], and its upper triangle determines it.
-      c.herm_w = true;
-      for (int m = 0; m < nm && c.herm_w; ++m)
-        for (size_t x = 0; x < npix; ++x)
-          if (!s->mask_full[x] && md->pat[(size_t)m * npix + x] != cd(0.0, 0.0)) {
-            c.herm_w = false;
-            break;
-          }
-      std::vector<int2> tri;
-      for (int m = 0; m < nm; ++m)
-        for (int mp = m; mp < nm; ++mp) tri.push_back(make_int2(m, mp));
-      c.T = (int)tri.size();
-      TCKS(c.tri.alloc(h, sizeof(int2) * tri.size()));
-      TCK(cudaMemcpyAsync(c.tri.p, tri.data(), sizeof(int2) * tri.size(), cudaMemcpyHostToDevice, st));
-      if (c.herm_w) {
-        TCKS(c.Wr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.K));
-        k_build_wr<<<dim3(blocks_for(c.K), c.T), 256, 0, st>>>(c.Wr.as<float>(), c.U.as<double2>(),
-                                                                c.Phi.as<double2>(), c.members.as<int>(),
-                                                                c.tri.as<int2>(), c.K, c.msz, (int)npix, scale);
-      } else {
-        TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
-        k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(),
-                                                c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
-      }
+    } else if (mode == 2 && c.herm_w) {
+      const size_t n = (size_t)c.Mp * c.Kp;
+      TCKS(c.Wh.alloc(h, sizeof(float) * n));
+      TCKS(c.Wl.alloc(h, sizeof(float) * n));
+      TCK(cudaMemsetAsync(c.Wh.p, 0, sizeof(float) * n, st));
+      TCK(cudaMemsetAsync(c.Wl.p, 0, sizeof(float) * n, st));
+      TCKS(Ad.alloc(h, sizeof(double) * 2 * (size_t)c.T * c.K));
+      k_build_wr_tc<<<dim3(blocks_for(c.Kp), c.T), 256, 0, st>>>(
+          c.Wh.as<float>(), c.Wl.as<float>(), Ad.as<double>(), c.U.as<double2>(), c.Phi.as<double2>(),
+          c.members.as<int>(), c.tri.as<int2>(), c.K, c.Kp, c.msz, (int)npix, scale);
+      TCK(cudaGetLastError());
+      TCKS(c.gW.alloc(h, sizeof(double) * c.Mp));
+      TCK(cudaMemsetAsync(c.gW.p, 0, sizeof(double) * c.Mp, st));
+      bf::note_launch();
+      k_rowsum<<<2 * c.T, 256, 0, st>>>(c.gW.as<double>(), Ad.as<double>(), c.K);
+    } else if (c.herm_w) {
+      TCKS(c.Wr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.K));
+      k_build_wr<<<dim3(blocks_for(c.K), c.T), 256, 0, st>>>(c.Wr.as<float>(), c.U.as<double2>(),
+                                                              c.Phi.as<double2>(), c.members.as<int>(),
+                                                              c.tri.as<int2>(), c.K, c.msz, (int)npix, scale);
     } else {
-      const size_t n = (size_t)2 * nm * nm * 2 * c.Kp;
-      TCKS(c.Wt_hi.alloc(h, sizeof(float) * n));
-      TCKS(c.Wt_lo.alloc(h, sizeof(float) * n));
-      TCK(cudaMemsetAsync(c.Wt_hi.p, 0, sizeof(float) * n, st));
-      TCK(cudaMemsetAsync(c.Wt_lo.p, 0, sizeof(float) * n, st));
-      k_build_w_t<<<grid, 256, 0, st>>>(c.Wt_hi.as<float>(), c.Wt_lo.as<float>(), c.U.as<double2>(),
-                                        c.Phi.as<double2>(), c.members.as<int>(), c.K, c.Kp, c.msz, nm, (int)npix,
-                                        scale);
+      // modes reaching beyond the mask (W not Hermitian): complex64 W for the
+      // SIMT GEMM (also on the tensor-core path)
+      TCKS(c.W.alloc(h, csz * (size_t)nm * nm * c.K));
+      k_build_w<float2><<<grid, 256, 0, st>>>(c.W.as<float2>(), c.U.as<double2>(), c.Phi.as<double2>(),
+                                              c.members.as<int>(), c.K, c.msz, nm, (int)npix, scale);
     }
     TCK(cudaGetLastError());
   }
@@ -1344,7 +1461,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   c.Kd = (int)supp.size();
   TCKS(c.supp.alloc(h, sizeof(int) * supp.size()));
   TCK(cudaMemcpyAsync(c.supp.p, supp.data(), sizeof(int) * supp.size(), cudaMemcpyHostToDevice, st));
-  c.Kdp = (c.Kd + 15) / 16 * 16;
+  c.Kdp = (c.Kd + 31) / 32 * 32;
   {
     dim3 grid(blocks_for(c.Kd), nm * nm);
     bf::note_launch();
@@ -1357,13 +1474,21 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       k_build_vr<<<dim3(blocks_for(c.Kd), c.T), 256, 0, st>>>(c.Vr.as<float>(), md->d_pat, c.supp.as<int>(),
                                                                c.tri.as<int2>(), c.Kd, (int)npix);
     } else {
-      const size_t n = (size_t)2 * nm * nm * 2 * c.Kdp;
-      TCKS(c.Vt_hi.alloc(h, sizeof(float) * n));
-      TCKS(c.Vt_lo.alloc(h, sizeof(float) * n));
-      TCK(cudaMemsetAsync(c.Vt_hi.p, 0, sizeof(float) * n, st));
-      TCK(cudaMemsetAsync(c.Vt_lo.p, 0, sizeof(float) * n, st));
-      k_build_v_t<<<grid, 256, 0, st>>>(c.Vt_hi.as<float>(), c.Vt_lo.as<float>(), md->d_pat, c.supp.as<int>(), c.Kd,
-                                        c.Kdp, nm, (int)npix);
+      const size_t n = (size_t)c.Mp * c.Kdp;
+      TCKS(c.Vh.alloc(h, sizeof(float) * n));
+      TCKS(c.Vl.alloc(h, sizeof(float) * n));
+      TCK(cudaMemsetAsync(c.Vh.p, 0, sizeof(float) * n, st));
+      TCK(cudaMemsetAsync(c.Vl.p, 0, sizeof(float) * n, st));
+      DBuf Vd;
+      TCKS(Vd.alloc(h, sizeof(double) * 2 * (size_t)c.T * c.Kd));
+      k_build_vr_tc<<<dim3(blocks_for(c.Kdp), c.T), 256, 0, st>>>(c.Vh.as<float>(), c.Vl.as<float>(), Vd.as<double>(),
+                                                                  md->d_pat, c.supp.as<int>(), c.tri.as<int2>(),
+                                                                  c.Kd, c.Kdp, (int)npix);
+      TCK(cudaGetLastError());
+      TCKS(c.gV.alloc(h, sizeof(double) * c.Mp));
+      TCK(cudaMemsetAsync(c.gV.p, 0, sizeof(double) * c.Mp, st));
+      bf::note_launch();
+      k_rowsum<<<2 * c.T, 256, 0, st>>>(c.gV.as<double>(), Vd.as<double>(), c.Kd);
     }
     TCK(cudaGetLastError());
   }
@@ -1442,26 +1567,18 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
   return BF_OK;
 }
 
-// Class GEMM of the TF32 path on the tensor cores: G[R][N] (complex128) from
-// A'' [2R][2Kp] and B''^T [N][2Kp] (TF32 hi/lo).  K is cut into slices of at
-// most 2048 real terms (FP32 accumulation in tensor memory per slice) and into
-// enough slices to fill the SMs; the slices are summed in FP64.
-static int tc_class_gemm(bf_handle* h, const float* Ahi, const float* Alo, int R, int Kp, const float* Bhi,
-                         const float* Blo, int N, double2* G, int* d_err) {
+// Class GEMM of the TF32 path on the tensor cores: out[splits][2 ncol][Mp]
+// (FP32) = A [Mp][Kp] times the 2 ncol real rows of B^T [2 ncol][Kp] (TF32
+// hi/lo pairs), K cut into slices only when the output tiles alone would
+// leave SMs idle; k_scatter_herm_tc sums the slices in FP64.
+static int tc_class_gemm(bf_handle* h, const float* Ah, const float* Al, int Mp, int Kp, const float* Bh,
+                         const float* Bl, int nrows_b, DBuf& out, int* splits, int* d_err) {
   cudaStream_t st = h->stream();
-  const int M2 = 2 * R, K2 = 2 * Kp;
-  g_tf_gemm_flops += 8.0 * (double)R * (double)Kp * (double)N;
-  const long tiles = (long)((N + 127) / 128) * ((M2 + 127) / 128);
-  const int ktiles = K2 / 32;
-  int splits = std::max((K2 + 2047) / 2048, (int)((2 * 152 + tiles - 1) / tiles));
-  splits = std::max(1, std::min({splits, ktiles, 64}));
-  DBuf planes;
-  TCKS(planes.alloc(h, sizeof(float) * (size_t)splits * M2 * N));
-  const int e = bf::tc_gemm_tf32x3(Ahi, Alo, Bhi, Blo, M2, N, K2, splits, planes.as<float>(), d_err, st);
+  g_tf_gemm_flops += 3.0 * 2.0 * (double)Mp * (double)Kp * (double)nrows_b;   // executed TF32 MMA work
+  *splits = bf::tc_gemm_splits(Mp, nrows_b, Kp);
+  TCKS(out.alloc(h, sizeof(float) * (size_t)*splits * nrows_b * Mp));
+  const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, *splits, out.as<float>(), d_err, st);
   if (e) return bf_fail(h, BF_ERR_CUDA, std::string("tensor-core GEMM: ") + cudaGetErrorString((cudaError_t)e));
-  bf::note_launch();
-  k_planes_to_g<<<blocks_for((size_t)R * N), 256, 0, st>>>(G, planes.as<float>(), R, N, splits);
-  TCK(cudaGetLastError());
   return BF_OK;
 }
 
@@ -1518,12 +1635,13 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCK(cudaMemcpyAsync(d_peps.p, par_eps.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
     TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
     const bool herm = mode == 1 && c.herm_w;   // real rows of W's upper triangle
-    TCKS(G.alloc(h, sizeof(C) * (size_t)(herm ? 2 * c.T : nm * nm) * ncol));
+    const bool tc = mode == 2 && c.herm_w;     // the same rows on the tensor cores
+    if (!tc) TCKS(G.alloc(h, sizeof(C) * (size_t)(herm ? 2 * c.T : nm * nm) * ncol));
     bf::note_launch();
     k_build_kz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
         KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
     TCK(cudaGetLastError());
-    if (mode != 2) {
+    if (!tc) {
       TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
       bf::note_launch();
       k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
@@ -1536,28 +1654,43 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
         TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
       }
     } else {
-      DBuf Bh, Bl;
-      const size_t nb = (size_t)ncol * 2 * c.Kp;
+      DBuf KZ0, C0, Bh, Bl, out;
+      TCKS(KZ0.alloc(h, sizeof(double2) * ncol));
+      TCKS(C0.alloc(h, sizeof(double2) * ncol));
+      bf::note_launch();
+      k_build_c0<<<blocks_for(ncol), 256, 0, st>>>(KZ0.as<double2>(), C0.as<double2>(), d_freq.as<double>(), nf,
+                                                   d_eps.as<double2>(), dr, lst.as<int>(), d_peps.as<int>(), npar);
+      TCK(cudaGetLastError());
+      const size_t nb = (size_t)2 * ncol * c.Kp;
       TCKS(Bh.alloc(h, sizeof(float) * nb));
       TCKS(Bl.alloc(h, sizeof(float) * nb));
       bf::note_launch();
-      k_build_d_t<<<dim3(blocks_for(c.Kp), std::min(ncol, 65535)), 256, 0, st>>>(
-          Bh.as<float>(), Bl.as<float>(), KZ.as<double2>(), c.K, c.Kp, nf, dr, lst.as<int>(), d_peps.as<int>(),
-          npar);
+      k_build_d_tc<<<dim3(blocks_for(c.Kp), std::min(ncol, 65535)), 256, 0, st>>>(
+          Bh.as<float>(), Bl.as<float>(), KZ.as<double2>(), KZ0.as<double2>(), C0.as<double2>(), c.K, c.Kp, nf, dr,
+          lst.as<int>(), d_peps.as<int>(), npar);
       TCK(cudaGetLastError());
-      TCKS(tc_class_gemm(h, c.Wt_hi.as<float>(), c.Wt_lo.as<float>(), nm * nm, c.Kp, Bh.as<float>(),
-                         Bl.as<float>(), ncol, G.as<C>(), tc_err));
-    }
-    bf::note_launch();
-    if (herm) {
+      int splits = 1;
+      TCKS(tc_class_gemm(h, c.Wh.as<float>(), c.Wl.as<float>(), c.Mp, c.Kp, Bh.as<float>(), Bl.as<float>(),
+                         2 * ncol, out, &splits, tc_err));
+      bf::note_launch();
       dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
-      k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
-                                            c.tri.as<int2>(), c.T);
-    } else {
-      dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
-      k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
+      k_scatter_herm_tc<S><<<gs, 256, 0, st>>>(P.as<S>(), out.as<float>(), c.Mp, splits, C0.as<double2>(),
+                                               c.gW.as<double>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
+                                               c.tri.as<int2>(), c.T);
+      TCK(cudaGetLastError());
     }
-    TCK(cudaGetLastError());
+    if (!tc) {
+      bf::note_launch();
+      if (herm) {
+        dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+        k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
+                                              c.tri.as<int2>(), c.T);
+      } else {
+        dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
+        k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
+      }
+      TCK(cudaGetLastError());
+    }
   }
   // pixel class: one GEMM V * E
   if (!preg.empty()) {
@@ -1567,7 +1700,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCK(cudaMemcpyAsync(lst.p, preg.data(), sizeof(int) * npx, cudaMemcpyHostToDevice, st));
     const int ncol = nf * npx;
     const int grows = mode == 1 ? 2 * c.T : nm * nm;   // mode 1: real rows of the upper triangle
-    TCKS(G.alloc(h, sizeof(C) * (size_t)grows * ncol));
+    if (mode != 2) TCKS(G.alloc(h, sizeof(C) * (size_t)grows * ncol));
     DBuf K0, DG;
     TCKS(K0.alloc(h, sizeof(double2) * (size_t)ncol));
     TCKS(DG.alloc(h, sizeof(double2) * (size_t)ncol * nm));
@@ -1590,29 +1723,38 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       else
         TCKS(launch_gemm<S>(h, c.V.as<S>(), E.as<S>(), G.as<C>(), nm * nm, c.Kd, ncol));
     } else {
-      DBuf Bh, Bl;
-      const size_t nb = (size_t)ncol * 2 * c.Kdp;
+      DBuf Bh, Bl, out;
+      const size_t nb = (size_t)2 * ncol * c.Kdp;
       TCKS(Bh.alloc(h, sizeof(float) * nb));
       TCKS(Bl.alloc(h, sizeof(float) * nb));
       bf::note_launch();
-      k_build_e_t<<<dim3(blocks_for(c.Kdp), std::min(ncol, 65535)), 256, 0, st>>>(
+      k_build_e_tc<<<dim3(blocks_for(c.Kdp), std::min(ncol, 65535)), 256, 0, st>>>(
           Bh.as<float>(), Bl.as<float>(), c.supp.as<int>(), c.Kd, c.Kdp, nf, dr, lst.as<int>(), npx,
           K0.as<double2>(), s->dX, s->dY, nx, s->d_surf, (int)npix);
       TCK(cudaGetLastError());
-      TCKS(tc_class_gemm(h, c.Vt_hi.as<float>(), c.Vt_lo.as<float>(), nm * nm, c.Kdp, Bh.as<float>(),
-                         Bl.as<float>(), ncol, G.as<C>(), tc_err));
-    }
-    bf::note_launch();
-    if (mode == 1) {
+      int splits = 1;
+      TCKS(tc_class_gemm(h, c.Vh.as<float>(), c.Vl.as<float>(), c.Mp, c.Kdp, Bh.as<float>(), Bl.as<float>(),
+                         2 * ncol, out, &splits, tc_err));
+      bf::note_launch();
       dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
-      k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
-                                            DG.as<double2>(), c.tri.as<int2>(), c.T);
-    } else {
-      dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
-      k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
-                                         DG.as<double2>());
+      k_scatter_herm_tc<S><<<gs, 256, 0, st>>>(P.as<S>(), out.as<float>(), c.Mp, splits, nullptr, c.gV.as<double>(),
+                                               nf, npx, dr, lst.as<int>(), nd, nm, DG.as<double2>(),
+                                               c.tri.as<int2>(), c.T);
+      TCK(cudaGetLastError());
     }
-    TCK(cudaGetLastError());
+    if (mode != 2) {
+      bf::note_launch();
+      if (mode == 1) {
+        dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+        k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
+                                              DG.as<double2>(), c.tri.as<int2>(), c.T);
+      } else {
+        dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
+        k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
+                                           DG.as<double2>());
+      }
+      TCK(cudaGetLastError());
+    }
   }
   // field class: propagate every mode (FP64), then overlap
   if (!freg.empty()) {
@@ -1842,6 +1984,26 @@ struct TraceArgs {
 // different sizes (serving workers) cannot lower it under one another.
 constexpr int kMaxDynSmem = 227 * 1024;
 
+// BF_ERR_SINGULAR when a solve met an exactly zero pivot, as Julia's inv
+// (transformer.jl:247) and `\` (:346,356) raise SingularException; the
+// outputs were still written (inf/NaN where the pivot was zero).
+static int singular_status(bf_handle* h, const int* sing, int nf, const double* freqs) {
+  char msg[192];
+  if (sing[0] >= 0 && sing[0] < nf) {
+    std::snprintf(msg, sizeof msg,
+                  "SingularException: a propagation matrix is exactly singular (first at frequency index %d, %.9g Hz)",
+                  sing[0], freqs[sing[0]]);
+    return bf_fail(h, BF_ERR_SINGULAR, msg);
+  }
+  if (sing[1] >= 0 && sing[1] < nf) {
+    std::snprintf(msg, sizeof msg,
+                  "SingularException: the boundary system T22 is exactly singular (first at frequency index %d, %.9g Hz)",
+                  sing[1], freqs[sing[1]]);
+    return bf_fail(h, BF_ERR_SINGULAR, msg);
+  }
+  return BF_OK;
+}
+
 // PT: storage of the propagation matrices, their inverses and the chain:
 // double2 (FP64 path) or float2 (mixed path); the boundary solve is FP64.
 template <typename PT>
@@ -1923,18 +2085,24 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   using D2 = PT;
   const D2* Pd = P_dev ? P_dev : P.as<D2>();
   TCKS(Pinv.alloc(h, sizeof(D2) * (size_t)nf * nd * nm * nm));
+  // d_sing[0]: lowest frequency index with an exactly singular propagation
+  // matrix, d_sing[1]: with an exactly singular T22 (0x7f7f7f7f = none); read
+  // back with the solve's outputs
+  int* d_sing = reinterpret_cast<int*>(h->d_scalar + 3);
+  TCK(cudaMemsetAsync(d_sing, 0x7f, 2 * sizeof(int), st));
+  int h_sing[2] = {0x7f7f7f7f, 0x7f7f7f7f};
   if (nm <= 16) {
     const int nmat = (nd - 1) * nf;
     bf::note_launch();
-    if (nm <= 8) k_invert_warp<D2, 8><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
-    else k_invert_warp<D2, 16><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat);
+    if (nm <= 8) k_invert_warp<D2, 8><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing);
+    else k_invert_warp<D2, 16><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing);
     TCK(cudaGetLastError());
   } else if (std::is_same<D2, float2>::value && nm <= 64) {
     dim3 grid(nd - 1, nf);
     bf::note_launch();
     if constexpr (std::is_same<D2, float2>::value) {
-      if (nm <= 32) k_invert_reg<32><<<grid, 64, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
-      else k_invert_reg<64><<<grid, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
+      if (nm <= 32) k_invert_reg<32><<<grid, 64, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
+      else k_invert_reg<64><<<grid, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
     }
     TCK(cudaGetLastError());
   } else {
@@ -1942,7 +2110,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     dim3 grid(nd - 1, nf);
     bf::note_launch();
-    k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm);
+    k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
     TCK(cudaGetLastError());
   }
   // chain coefficients: step j uses n_left = sqrt(eps[j]), n_right = sqrt(eps[j-1])
@@ -1984,9 +2152,10 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
         tb->per_freq ? nm : 0, d_em.as<double2>(), tb->axion, d_out.as<double2>());
     TCK(cudaGetLastError());
     TCK(cudaMemcpyAsync(tb->out, d_out.p, sizeof(cd) * nout, cudaMemcpyDeviceToHost, st));
+    TCK(cudaMemcpyAsync(h_sing, d_sing, sizeof(h_sing), cudaMemcpyDeviceToHost, st));
     TCK(cudaStreamSynchronize(st));
     if (mode == 2 && !pm && !P_dev) TCKS(tc_status(h));
-    return BF_OK;
+    return singular_status(h, h_sing, nf, freqs);
   }
   // T21 / T22 for the boundary solve, FP64
   TCKS(T21.alloc(h, sizeof(double2) * (size_t)nf * nm * nm));
@@ -2034,7 +2203,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     bf::note_launch();
     k_final_solve<double2><<<nf, 256, smem, st>>>(T21.as<double2>(), T22.as<double2>(), ax.as<double2>(),
                                              reflect ? d_refl.as<double2>() : nullptr, nm, boost.as<double2>(),
-                                             reflect ? refl.as<double2>() : nullptr, b2.as<double>());
+                                             reflect ? refl.as<double2>() : nullptr, b2.as<double>(), d_sing + 1);
     TCK(cudaGetLastError());
   }
   DBuf d_ant, d_cpl;
@@ -2067,9 +2236,10 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   if (out_refl && reflect) TCK(cudaMemcpyAsync(out_refl, refl.p, sizeof(cd) * nf * nm, cudaMemcpyDeviceToHost, st));
   if (out_beta2) TCK(cudaMemcpyAsync(out_beta2, b2.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
   if (cp) TCK(cudaMemcpyAsync(cp->out, d_cpl.p, sizeof(double) * nf, cudaMemcpyDeviceToHost, st));
+  TCK(cudaMemcpyAsync(h_sing, d_sing, sizeof(h_sing), cudaMemcpyDeviceToHost, st));
   TCK(cudaStreamSynchronize(st));
   if (mode == 2 && !pm && !P_dev) TCKS(tc_status(h));
-  return BF_OK;
+  return singular_status(h, h_sing, nf, freqs);
 }
 
 // precision: BF_PREC_FP64 (mode 0), BF_PREC_MIXED (mode 1) or BF_PREC_TF32 (mode 2)

@@ -10,6 +10,7 @@ module BoostFractorGB300
 
 using BoostFractor: SetupBoundaries, CoordinateSystem, Modes,
                     propagator, propagatorNoTilts, propagatorMomentumSpace, propagator1D
+using LinearAlgebra: SingularException
 
 const lib = get(ENV, "BFGB300_LIB", joinpath(@__DIR__, "..", "lib", "libbfgb300.so"))
 
@@ -25,6 +26,7 @@ function check(h::Handle, rc::Cint)
     rc == 0 && return nothing
     msg = unsafe_string(ccall((:bf_last_error, lib), Cstring, (Ptr{Cvoid},), h.ptr))
     rc == 1 && throw(ArgumentError(msg))
+    rc == 6 && throw(SingularException(0))   # inv / \ of an exactly singular matrix (transformer.jl:247,346,356)
     error("libbfgb300 error $rc: $msg")
 end
 

@@ -38,6 +38,10 @@ extern "C" {
 #define BF_ERR_CUDA        3  /* a CUDA runtime call failed */
 #define BF_ERR_TIMEOUT     4  /* a bounded wait expired */
 #define BF_ERR_UNSUPPORTED 5  /* valid request outside what this build implements */
+#define BF_ERR_SINGULAR    6  /* an exactly singular propagation matrix or boundary system T22
+                                 (an exactly zero pivot); the outputs are still written, with
+                                 inf/NaN where the pivot was zero (reference: SingularException
+                                 from inv and \, src/boost_fractor_transformer.jl:247,346,356) */
 
 /* ---- propagator plug-ins: the reference's `prop=` keyword ---------------- */
 #define BF_PROP_3D       0  /* propagator              src/boost_fractor.jl:137-149 */
@@ -141,10 +145,12 @@ int bf_propagate(bf_handle* h, int prop_kind, int precision,
  * with cudaFree's implicit synchronisation.
  *   - nx, ny <= BF_NOALLOC_MAX_N; larger grids return BF_ERR_INVALID.
  *   - The first call on a device does the set-up (cudaGetSymbolAddress of the
- *     scratch, first launch of each kernel); make it before any stream capture.
+ *     scratch with that device current); make it before any stream capture.
  *   - One scratch per device for the whole process: overlapping calls (other
  *     streams, other threads) race on it; serialise them.
- * X, Y, kX, kY, surface are host arrays as in bf_propagate. */
+ * X, Y, kX, kY, surface are host arrays as in bf_propagate, copied on the
+ * handle's stream: pageable ones are staged before the call returns, pinned
+ * ones must stay valid and unchanged until the stream has run the call. */
 #define BF_NOALLOC_MAX_N 256
 int bf_propagate_noalloc(bf_handle* h, int prop_kind, double* E_dev, int nx, int ny,
                          const double* X, const double* Y, const double* kX, const double* kY,
@@ -408,6 +414,13 @@ int bf_wait(bf_server* s, unsigned long long id, int timeout_ms, int* status, do
  * another's batch, stack workspaces released for admission. */
 int bf_server_stats(bf_server* s, int solver, double* out);
 const char* bf_server_last_error(const bf_server* s);
+
+/* ---- test hooks ------------------------------------------------------------ */
+/* No counterpart in the reference.  While `on` is non-zero, the tensor-core
+ * overlap GEMM (BF_PREC_TF32) issues no operand copies, so its MMA warp's
+ * bounded wait runs out after ~2 s and the solve returns BF_ERR_TIMEOUT with
+ * the CUDA context intact: the test of the kernel's bounded waits. */
+int bf_test_tc_withhold_loads(int on);
 
 #ifdef __cplusplus
 }

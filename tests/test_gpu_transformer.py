@@ -301,9 +301,9 @@ def test_tf32_propagation_matrices_vs_fp64(B):
 
 
 def test_tf32_transformer_full_size_vs_oracle_fixture(B):
-    """BF_PREC_TF32 on the full transformer workload: beta^2 within the stated
-    2e-2 of the oracle (the tensor cores' truncating FP32 accumulation keeps it
-    outside the 1e-4 bar of the mixed path)."""
+    """BF_PREC_TF32 on the full transformer workload: the overlap GEMMs on the
+    tensor cores (accumulator drained every 32 K-elements, operands less their
+    centre value) keep beta^2 within the 1e-4 bar of the oracle."""
     import os
     from bfgb300 import workloads as W
     fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "c3_lg_oracle.npz"))
@@ -316,7 +316,30 @@ def test_tf32_transformer_full_size_vs_oracle_fixture(B):
                     pattern_input=w["pattern_input"], kT_arr=w["kT_arr"])
     b = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"], precision="tf32")
     for k in range(len(fx["freqs"])):
-        assert abs(np.sum(np.abs(b[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < 2e-2
+        assert abs(np.sum(np.abs(b[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
+
+
+def test_tf32_bounded_wait_times_out(B):
+    """The tensor-core GEMM's mbarrier waits are bounded: with the operand
+    copies withheld (a test hook; nothing is read or written that a normal
+    launch would not touch), the MMA warp's wait runs out after ~2 s, the
+    solve returns BF_ERR_TIMEOUT, and the next solve on the same handle is
+    correct again."""
+    from bfgb300 import _lib
+    cb, mb, kw = _lg_reduced(B)
+    freqs = np.array([19.7e9])
+    ok = B.calc_propagation_matrices(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="tf32")
+    L = _lib.lib()
+    L.bf_test_tc_withhold_loads(1)
+    try:
+        with pytest.raises(B.BFError) as e:
+            B.calc_propagation_matrices(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="tf32")
+    finally:
+        L.bf_test_tc_withhold_loads(0)
+    assert e.value.code == _lib.BF_ERR_TIMEOUT
+    again = B.calc_propagation_matrices(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="tf32")
+    for j in range(1, len(kw["distance"])):
+        assert np.array_equal(again[0][j], ok[0][j])
 
 
 def test_tf32_rejected_by_bounce_solvers(B):
@@ -414,3 +437,37 @@ def test_transformer_1d_vs_analytical1d(B):
         sb = B.SeedSetupBoundaries(c1, diskno=nd, distance=np.array(dist), epsilon=np.array(eps, dtype=complex))
         got = np.abs(B.transformer(sb, c1, m1, f=freqs, prop=B.propagator1D)[:, 0]) ** 2
         assert np.allclose(got, gold, rtol=1e-6), k
+
+
+@pytest.mark.parametrize("M,precision", [(6, "fp64"), (6, "mixed"), (20, "fp64"), (20, "mixed")])
+def test_singular_propagation_matrix_raises(B, M, precision):
+    """An injected propagation matrix with a zero row is exactly singular: the
+    reference's inv raises SingularException (transformer.jl:247); here the
+    call returns BF_ERR_SINGULAR (SingularError) naming the frequency.  M = 6
+    runs the warp inverses, M = 20 the CTA (FP64) and register (complex64)
+    inverses.  A following regular solve on the same handle is unaffected."""
+    distance, eps, tx, ty, X, s = _stack(2, 32, seed=3, surf=False)
+    kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=M, Lmax=0, diskR=0.15)
+    mo = O.seed_modes(co, ThreeDim=True, Mmax=M, Lmax=0, diskR=0.15)
+    f = 20.1e9
+    sbo = O.seed_setup_boundaries(co, **kw)
+    sbo.eps[0] = 1e30
+    pm = O.calc_propagation_matrices(sbo, co, mo, f=f)
+    bad = [p.copy() for p in pm]
+    bad[3][1, :] = 0.0
+    with pytest.raises(B.SingularError, match="SingularException"):
+        B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=f, propagation_matrices=bad,
+                      precision=precision)
+    # the flag does not outlive the call: the regular matrices solve without an error
+    got = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=f, propagation_matrices=pm, precision=precision)
+    if M == 6:
+        # (20 Bessel modes on 32 x 32 pixels make an ill-conditioned chain, whose
+        # values mean nothing: only the error path is checked there)
+        ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f, propagation_matrices=pm)
+        if precision == "fp64":
+            assert rel(got, ref) < FP64_TOL
+        else:
+            r2 = np.sum(np.abs(ref) ** 2)
+            assert abs(np.sum(np.abs(got) ** 2) - r2) / r2 < MIXED_BETA2_TOL
