@@ -478,41 +478,44 @@ def run_transformer(args):
     h.set_profiling(True)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    gemm_ms, gemm_fl, launches = 0.0, 0.0, 0
+    gemm_ms, gemm_fl, launches, kern_ms, kern_n = 0.0, 0.0, 0, 0.0, 0
     e0.record(stream)
     for _ in range(args.steps):
         solve(w["freqs"], "mixed", boost, beta2)
         p = h.last_profile()
-        gemm_ms += p["stages_ms"]
-        gemm_fl += p["propagations"]
+        gemm_ms += p["stages_ms"]           # the propagation-matrix phase
+        kern_ms += p["exits_ms"]            # slot 3: the class-GEMM kernels alone
+        kern_n += int(p["stage_launches"])  # slot 4: class-GEMM launches
+        gemm_fl += p["propagations"]        # slot 6: their executed flops
         launches += int(p["launches"])
     e1.record(stream)
     torch.cuda.synchronize()
     h.set_profiling(False)
     ms = e0.elapsed_time(e1) / args.steps
-    # the same request with the overlap GEMMs on the tensor cores (BF_PREC_TF32,
-    # outside the 1e-4 bar): its first call builds the TF32 operands of W and V
-    b2_tc = np.empty(nf)
+    # the same request with the overlap GEMMs on the FP32 SIMT pipes
+    # (BF_PREC_MIXED_SIMT): its first call builds the FP32 real rows of W and V
+    b2_simt = np.empty(nf)
     for _ in range(max(args.warmup, 1)):
-        solve(w["freqs"], "tf32", boost, b2_tc)
-    errs_tc = np.abs(b2_tc[sub] - b2_64) / np.abs(b2_64)
+        solve(w["freqs"], "mixed-simt", boost, b2_simt)
+    errs_simt = np.abs(b2_simt[sub] - b2_64) / np.abs(b2_64)
     h.set_profiling(True)
     torch.cuda.synchronize()
-    tc_ms, tc_fl = 0.0, 0.0
+    simt_ms, simt_fl = 0.0, 0.0
     e0.record(stream)
     for _ in range(args.steps):
-        solve(w["freqs"], "tf32", boost, b2_tc)
+        solve(w["freqs"], "mixed-simt", boost, b2_simt)
         p = h.last_profile()
-        tc_ms += p["stages_ms"]
-        tc_fl += p["propagations"]
+        simt_ms += p["stages_ms"]
+        simt_fl += p["propagations"]
     e1.record(stream)
     torch.cuda.synchronize()
     h.set_profiling(False)
-    ms_tc = e0.elapsed_time(e1) / args.steps
+    ms_simt = e0.elapsed_time(e1) / args.steps
     tf32_peak, tf32_src = measured_tf32_peak()
-    # the executed MMA work: three MMAs (hi*hi, hi*lo, lo*hi) per product of
-    # the real-row GEMMs, counted by the library
-    tc_tensor = tc_fl / (tc_ms / 1000.0) / 1e12
+    # executed MMA work of the tensor-core class GEMMs (three MMAs, hi*hi,
+    # hi*lo, lo*hi, per product of the real-row GEMMs, counted by the library)
+    # over the GEMM kernels' own CUDA-event time
+    tc_tensor = gemm_fl / (kern_ms / 1000.0) / 1e12
     N = len(w["X"])
     sp = simt_peaks()
     if sp and sp.get("fp32_ffma_tflops"):
@@ -522,8 +525,8 @@ def run_transformer(args):
     line = {"metric": f"beta2 freq-points/s (transformer, 20 disks + surface maps, {nm} LG modes, {N}x{N}, {nf} freqs)",
             "value": nf / (ms / 1000.0), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c64 overlap operands (FP32 products, double-float accumulation), c64 propagation matrices "
-                     "and inverses, double-float chain, f64 phases and boundary solve",
+            "dtype": "split-TF32 overlap GEMMs on tcgen05 (FP32 register sums of 32-deep tensor-core blocks), "
+                     "c64 propagation matrices and inverses, double-float chain, f64 phases and boundary solve",
             "data": "synthetic (seeded geometry and surface maps)",
             "config": {"workload": w["name"] + f"-{nf}f", "grid": N, "modes": nm, "freqs": nf},
             "beta2_rel_err_vs_fp64": float(np.max(errs)), "beta2_rel_err_vs_fp64_median": float(np.median(errs)),
@@ -538,22 +541,23 @@ def run_transformer(args):
             "alg_roofline": {"gflop_per_freq_point": 104.0, "peak_tflops": tf32_peak / 3.0,
                              "freqpts_per_s": tf32_peak / 3.0 * 1e3 / 104.0,
                              "frac": (nf / (ms / 1000.0)) / (tf32_peak / 3.0 * 1e3 / 104.0),
-                             "executed_gemm_tflop_per_request": gemm_fl / args.steps / 1e12},
-            "roofline": {"bound": "fp32-simt", "achieved": gemm_fl / (gemm_ms / 1000.0) / 1e12,
-                         "peak": peak_fp32, "peak_source": fp32_src, "unit": "TFLOP/s",
-                         "frac": gemm_fl / (gemm_ms / 1000.0) / 1e12 / peak_fp32,
-                         "kernel": "k_rcgemm_c64 (real rows of the Hermitian class overlaps; k_cgemm_c64 when "
-                                   "the modes extend beyond the disk mask)",
-                         "phase_ms": gemm_ms / args.steps},
-            "tensor_core_tf32": {
-                "value": nf / (ms_tc / 1000.0), "unit": UNIT, "ms_per_step": ms_tc,
-                "beta2_rel_err_vs_fp64": float(np.max(errs_tc)),
-                "beta2_rel_err_vs_fp64_median": float(np.median(errs_tc)),
-                "note": "BF_PREC_TF32: real-row class GEMMs on tcgen05 (split TF32, accumulator drained every 32 K)",
-                "roofline": {"bound": "tensor", "achieved": tc_tensor, "peak": tf32_peak, "unit": "TFLOP/s",
-                             "frac": tc_tensor / tf32_peak, "peak_source": tf32_src,
-                             "kernel": "k_tc_gemm_tf32x3 (whole propagation-matrix phase)",
-                             "phase_ms": tc_ms / args.steps}}}
+                             "executed_mma_tflop_per_request": gemm_fl / args.steps / 1e12},
+            "roofline": {"bound": "tensor", "achieved": tc_tensor, "peak": tf32_peak, "unit": "TFLOP/s",
+                         "frac": tc_tensor / tf32_peak, "peak_source": tf32_src, "traffic": None,
+                         "kernel": "k_tc_gemm_tf32x3 (executed MMA flops / the kernel's CUDA-event time)",
+                         "launch_avg_ms": kern_ms / max(kern_n, 1), "launches_per_step": kern_n / args.steps,
+                         "phase_ms": gemm_ms / args.steps,
+                         "phase_tflops": gemm_fl / (gemm_ms / 1000.0) / 1e12},
+            "simt_gemm": {
+                "value": nf / (ms_simt / 1000.0), "unit": UNIT, "ms_per_step": ms_simt,
+                "beta2_rel_err_vs_fp64": float(np.max(errs_simt)),
+                "beta2_rel_err_vs_fp64_median": float(np.median(errs_simt)),
+                "note": "BF_PREC_MIXED_SIMT: the same solve with the class GEMMs on the FP32 SIMT pipes",
+                "roofline": {"bound": "fp32-simt", "achieved": simt_fl / (simt_ms / 1000.0) / 1e12,
+                             "peak": peak_fp32, "peak_source": fp32_src, "unit": "TFLOP/s",
+                             "frac": simt_fl / (simt_ms / 1000.0) / 1e12 / peak_fp32,
+                             "kernel": "k_rcgemm_c64 (whole propagation-matrix phase)",
+                             "phase_ms": simt_ms / args.steps}}}
     print(json.dumps(line), flush=True)
     st.close()
     modes.close()

@@ -27,7 +27,7 @@ from ._lib import BFError, SingularError
 __all__ = [
     "CoordinateSystem", "SeedCoordinateSystem", "SetupBoundaries", "SeedSetupBoundaries",
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
-    "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError", "SingularError",
+    "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError", "SingularError", "transformer_group",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
     "gauss_profile", "unnormalized_match", "transformer_coupled", "transformer_1d_batch",
@@ -192,7 +192,8 @@ def SeedSetupBoundaries(coords, diskno=3, distance=None, epsilon=None, relative_
 # --------------------------------------------------------------------------
 # propagators: the prop= plug-ins (src/boost_fractor.jl:137-227)
 # --------------------------------------------------------------------------
-_PREC = {"fp64": _lib.BF_PREC_FP64, "mixed": _lib.BF_PREC_MIXED, "tf32": _lib.BF_PREC_TF32}
+_PREC = {"fp64": _lib.BF_PREC_FP64, "mixed": _lib.BF_PREC_MIXED, "tf32": _lib.BF_PREC_TF32,
+         "mixed-simt": _lib.BF_PREC_MIXED_SIMT}
 
 
 def _prec(p):
@@ -502,6 +503,24 @@ def modes2field(mode_coeffs, coords, modes):
     modes.h.check(_lib.lib().bf_modes2field(modes.h.ptr, modes._m, _lib.ptr(c.view(np.float64)),
                                             _lib.ptr(out.view(np.float64))))
     return out.T[:, :, None]
+
+
+def transformer_group(stacks, modes, freqs, prop=propagator, precision="mixed", want_boost=False):
+    """transformer (default emission) for several resident stacks at once that
+    differ only in their untilted air-gap distances (bf_transformer_group):
+    one solve for all (stack, frequency) pairs.  Returns beta2 [nreq, nf]
+    (and boost [nreq, nf, nm] with want_boost)."""
+    freqs = np.ascontiguousarray(np.atleast_1d(freqs), dtype=np.float64)
+    nreq, nf, nm = len(stacks), len(freqs), modes.nm
+    arr = (_lib._vp * nreq)(*[st._s for st in stacks])
+    beta2 = np.empty((nreq, nf))
+    boost = np.empty((nreq, nf, nm), dtype=np.complex128) if want_boost else None
+    h = stacks[0].h
+    h.check(_lib.lib().bf_transformer_group(h.ptr, nreq, arr, modes._m, nf, _lib.ptr(freqs), _prop_kind(prop),
+                                            _prec(precision),
+                                            _lib.ptr(None if boost is None else boost.view(np.float64)),
+                                            _lib.ptr(beta2)))
+    return (beta2, boost) if want_boost else beta2
 
 
 def calc_propagation_matrices(bdry, coords, modes, f=10.0e9, prop=propagator, diskR=0.15, precision="fp64"):

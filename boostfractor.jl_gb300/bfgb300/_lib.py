@@ -27,6 +27,7 @@ BF_NOALLOC_MAX_N = 256
 BF_PREC_FP64 = 0
 BF_PREC_MIXED = 1
 BF_PREC_TF32 = 2
+BF_PREC_MIXED_SIMT = 3
 
 BF_OUT_DEVICE = 1
 BF_IN_DEVICE = 2
@@ -116,6 +117,8 @@ _SIGS = {
     "bf_transformer": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                 _p_dbl, _p_dbl, _p_dbl]),
     "bf_test_tc_withhold_loads": (_c_int, [_c_int]),
+    "bf_transformer_group": (_c_int, [_vp, _c_int, ctypes.POINTER(_vp), _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl,
+                                      _p_dbl]),
 }
 
 _lib = None

@@ -1486,7 +1486,8 @@ static int check_solver_args(bf_handle* h, bf_stack* s, int nf, const double* fr
   for (int i = 0; i < nf; ++i)
     if (!(freqs[i] > 0)) return fail(h, BF_ERR_INVALID, "frequency must be positive");
   if (prop_kind < 0 || prop_kind > 3) return fail(h, BF_ERR_INVALID, "unknown propagator kind");
-  if (precision == BF_PREC_TF32) return fail(h, BF_ERR_INVALID, "BF_PREC_TF32 applies to the transformer only");
+  if (precision == BF_PREC_TF32 || precision == BF_PREC_MIXED_SIMT)
+    return fail(h, BF_ERR_INVALID, "BF_PREC_TF32 / BF_PREC_MIXED_SIMT apply to the transformer only");
   if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED) return fail(h, BF_ERR_INVALID, "unknown precision");
   if (!std::isfinite(amin)) return fail(h, BF_ERR_INVALID, "non-finite amin");
   return BF_OK;

@@ -18,6 +18,9 @@
 //   * order and batching: one request per stack at a time, in submission order;
 //     queued requests on the same stack with the same solver settings and no
 //     geometry change join the first one's frequency batch (one solve);
+//     transformer requests on different stacks that differ only in their air
+//     gaps (the steps of several disk-position optimisers) join one group
+//     solve (bf_transformer_group), up to kMaxGroup requests;
 //   * completion: beta^2 (and the transformer boost) are copied to the caller's
 //     buffers, then the status becomes final; bf_poll / bf_wait report it.
 #include <algorithm>
@@ -40,6 +43,7 @@ namespace {
 using Clock = std::chrono::steady_clock;
 constexpr int kMaxPassOver = 8;
 constexpr int kMaxBatchFreqs = 4096;
+constexpr int kMaxGroup = 16;
 
 struct Req {
   unsigned long long id = 0;
@@ -63,6 +67,7 @@ struct StackInfo {
 struct Batch {
   std::vector<Req*> reqs;
   size_t need = 0;
+  bool group = false;   // reqs on different stacks, one group solve
 };
 
 }  // namespace
@@ -121,6 +126,27 @@ bool make_room(bf_server* S, size_t need, const bf_stack* keep) {
   return true;
 }
 
+// Transformer requests whose stacks may share one group solve: same modes,
+// frequencies and settings, and stacks that differ at most in distances (the
+// library checks that only untilted air gaps differ and refuses otherwise).
+bool groupable(const bf_server* S, const Req* a, const Req* b) {
+  if (a->r.solver != BF_SOLVER_TRANSFORMER || b->r.solver != BF_SOLVER_TRANSFORMER) return false;
+  if (a->r.modes != b->r.modes || a->r.prop_kind != b->r.prop_kind || a->r.precision != b->r.precision ||
+      a->freqs != b->freqs)
+    return false;
+  if (S->dry()) return true;
+  const bf_stack* x = a->r.stack;
+  const bf_stack* y = b->r.stack;
+  if (x->nd != y->nd || x->nx != y->nx || x->ny != y->ny || x->diskR != y->diskR || !x->surf.empty() ||
+      !y->surf.empty() || x->X != y->X || x->Y != y->Y || x->tilt_x != y->tilt_x || x->tilt_y != y->tilt_y)
+    return false;
+  for (int j = 0; j < x->nd; ++j) {
+    const cd e = x->eps[j], f = y->eps[j];
+    if (!(e == f || (std::isnan(e.real()) && std::isnan(f.real()) && e.imag() == f.imag()))) return false;
+  }
+  return true;
+}
+
 bool mergeable(const Req* a, const Req* b) {
   return b->distance.empty() && a->r.solver == b->r.solver && a->r.modes == b->r.modes &&
          a->r.nmax == b->r.nmax && a->r.prop_kind == b->r.prop_kind && a->r.precision == b->r.precision &&
@@ -156,9 +182,40 @@ Batch pick(bf_server* S, int w) {
       Q->in_batch = 1;
       taken.push_back(qj);
     }
+    // a lone transformer request gathers the queued steps of other stacks
+    // that can share its solve
+    if (b.reqs.size() == 1 && R->r.solver == BF_SOLVER_TRANSFORMER) {
+      for (size_t qj = qi + 1; qj < S->queue.size() && (int)b.reqs.size() < kMaxGroup; ++qj) {
+        Req* Q = S->queue[qj];
+        if (!groupable(S, R, Q)) continue;
+        bool dup = false;
+        for (Req* G : b.reqs) dup |= G->r.stack == Q->r.stack;
+        if (dup) continue;
+        StackInfo& qs = S->stacks[Q->r.stack];
+        if (qs.busy || (qs.home >= 0 && qs.home != w)) continue;
+        // an earlier queued request on Q's stack keeps its turn
+        bool earlier = false;
+        for (size_t qk = 0; qk < qj && !earlier; ++qk)
+          earlier = S->queue[qk] != R && S->queue[qk]->r.stack == Q->r.stack;
+        if (earlier) continue;
+        const size_t qneed = Q->est > qs.resident ? Q->est - qs.resident : 0;
+        if (S->resident + S->inflight + b.need + qneed > S->budget) break;
+        b.reqs.push_back(Q);
+        b.need += qneed;
+        Q->in_batch = 1;
+        taken.push_back(qj);
+      }
+      if (b.reqs.size() > 1) {
+        b.group = true;
+        std::sort(taken.begin(), taken.end());
+      }
+    }
     for (auto it = taken.rbegin(); it != taken.rend(); ++it) S->queue.erase(S->queue.begin() + (long)*it);
-    si.busy = true;
-    si.home = w;
+    for (Req* G : b.reqs) {
+      StackInfo& gi = S->stacks[G->r.stack];
+      gi.busy = true;
+      gi.home = w;
+    }
     S->inflight += b.need;
     return b;
   }
@@ -196,6 +253,37 @@ int run_batch(bf_server* S, int w, Batch& b, std::string& err) {
     rc = bf_pgrid_transformer(h, q.pgrid, R0->distance.data(), nullptr, q.out_boost ? boost.data() : nullptr,
                               b2.data());
     if (rc == BF_OK && q.out_boost) std::memcpy(q.out_boost, boost.data(), sizeof(double) * boost.size());
+  } else if (b.group) {
+    // steps of several stacks in one group solve (each request's distances first)
+    const int n = (int)b.reqs.size(), nfr = R0->r.nf, nm = R0->nm;
+    std::vector<bf_stack*> sts(n);
+    for (int r = 0; r < n && rc == BF_OK; ++r) {
+      Req* R = b.reqs[r];
+      sts[r] = R->r.stack;
+      if (r > 0 && !R->distance.empty()) rc = bf_stack_set_distance(h, sts[r], R->distance.data());
+    }
+    if (rc != BF_OK) { err = h->err; return rc; }
+    bool want = false;
+    for (Req* R : b.reqs) want |= R->r.out_boost != nullptr;
+    std::vector<double> gb2((size_t)n * nfr), gbo(want ? (size_t)n * nfr * nm * 2 : 0);
+    rc = bf_transformer_group(h, n, sts.data(), q.modes, nfr, R0->freqs.data(), q.prop_kind, q.precision,
+                              want ? gbo.data() : nullptr, gb2.data());
+    if (rc == BF_ERR_INVALID) {
+      // the stacks differ in more than their air gaps: solve them one by one
+      rc = BF_OK;
+      for (int r = 0; r < n && rc == BF_OK; ++r)
+        rc = bf_transformer(h, sts[r], q.modes, nfr, R0->freqs.data(), q.prop_kind, q.precision, nullptr, nullptr,
+                            nullptr, 0, want ? gbo.data() + (size_t)r * nfr * nm * 2 : nullptr, nullptr,
+                            gb2.data() + (size_t)r * nfr);
+    }
+    if (rc != BF_OK) { err = h->err; return rc; }
+    for (int r = 0; r < n; ++r) {
+      Req* R = b.reqs[r];
+      std::copy(gb2.begin() + (long)r * nfr, gb2.begin() + (long)(r + 1) * nfr, R->r.out_beta2);
+      if (R->r.out_boost)
+        std::memcpy(R->r.out_boost, gbo.data() + (size_t)r * nfr * nm * 2, sizeof(double) * nfr * nm * 2);
+    }
+    return BF_OK;
   } else if (q.solver == BF_SOLVER_TRANSFORMER) {
     bool want = false;
     for (Req* R : b.reqs) want |= R->r.out_boost != nullptr;
@@ -244,18 +332,25 @@ void worker(bf_server* S, int w) {
     lock.unlock();
     std::string err;
     const int rc = run_batch(S, w, b, err);
-    bf_stack* st = b.reqs[0]->r.stack;
-    const size_t res = S->dry() ? (size_t)std::max<unsigned long long>(b.reqs[0]->r.footprint_bytes, 1)
-                                : bf_stack_device_bytes(st);
+    std::vector<bf_stack*> sts;
+    std::vector<size_t> res;
+    for (Req* R : b.reqs) {
+      if (std::find(sts.begin(), sts.end(), R->r.stack) != sts.end()) continue;
+      sts.push_back(R->r.stack);
+      res.push_back(S->dry() ? (size_t)std::max<unsigned long long>(R->r.footprint_bytes, 1)
+                             : bf_stack_device_bytes(R->r.stack));
+    }
     lock.lock();
     const double t_done = S->now();
-    StackInfo& si = S->stacks[st];
     S->inflight -= b.need;
-    S->resident -= si.resident;
-    si.resident = res;
-    S->resident += res;
-    si.busy = false;
-    si.last_used = t_done;
+    for (size_t k = 0; k < sts.size(); ++k) {
+      StackInfo& si = S->stacks[sts[k]];
+      S->resident -= si.resident;
+      si.resident = res[k];
+      S->resident += res[k];
+      si.busy = false;
+      si.last_used = t_done;
+    }
     if (rc != BF_OK) S->err = err;
     for (Req* R : b.reqs) {
       R->t_done = t_done;
@@ -382,8 +477,10 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
   if (q->solver < BF_SOLVER_TRANSFORMER && q->nmax < 0) return server_fail(S, BF_ERR_INVALID, "nmax < 0");
   if (q->solver == BF_SOLVER_PGRID && (!q->pgrid || !q->distance))
     return server_fail(S, BF_ERR_INVALID, "a grid request needs the grid and the per-disk shifts (distance)");
-  if (q->precision != BF_PREC_FP64 && q->precision != BF_PREC_MIXED)
-    return server_fail(S, BF_ERR_INVALID, "unknown precision");
+  const bool tf_only = q->precision == BF_PREC_TF32 || q->precision == BF_PREC_MIXED_SIMT;
+  if (!(q->precision == BF_PREC_FP64 || q->precision == BF_PREC_MIXED ||
+        (tf_only && q->solver == BF_SOLVER_TRANSFORMER)))
+    return server_fail(S, BF_ERR_INVALID, "unknown precision for this solver");
   if (S->dry() && !q->footprint_bytes)
     return server_fail(S, BF_ERR_INVALID, "a dry-run request needs footprint_bytes");
   Req* R = new Req();

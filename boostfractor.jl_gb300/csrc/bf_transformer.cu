@@ -26,8 +26,10 @@
 #include <complex>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <type_traits>
+#include <utility>
 #include <vector>
 
 #include "../../include/boostfractor_gb300.h"
@@ -51,6 +53,12 @@ struct bf_modes {
   std::vector<cd> kt;    // [nm]
   double2* d_pat = nullptr;
   unsigned long long id = 0;
+  // the transformer's default emission, axion_induced_modes(coords, modes;
+  // diskR) (transformer.jl:285), for the last diskR asked for; it depends on
+  // the modes and diskR only, so solves do not recompute it
+  std::mutex emit_mu;
+  double emit_diskR = -1.0;
+  std::vector<cd> emit;
 };
 
 // engine-wide helpers from bf_api.cu
@@ -224,7 +232,7 @@ __device__ __forceinline__ void tf32_split_d(double x, float& hi, float& lo) {
   lo = __uint_as_float(l);
 }
 
-// ---- operands of the tensor-core class GEMMs (BF_PREC_TF32) -------------------
+// ---- operands of the tensor-core class GEMMs (BF_PREC_MIXED / BF_PREC_TF32) ----
 // Both classes are Hermitian in the mode pair, so the tensor cores see the
 // real-row form of the mixed path: A = the real rows of the upper triangle
 // (Re and Im of W[mm'] or V[mm'] for m <= m', rows 2t and 2t + 1, padded with
@@ -326,39 +334,77 @@ __global__ void k_rowsum(double* g, const double* Ad, int K) {
   if (threadIdx.x == 0) g[r] = red[0];
 }
 
-// Per column c = f * npar + p of the k-space class: kz0 = sqrt(k0^2) (the
-// phasor's transverse-momentum-zero wavenumber) and c0 = exp(-i kz0 dz), FP64.
-__global__ void k_build_c0(double2* KZ0, double2* C0, const double* freqs, int nf, const double2* eps,
-                           const RegionT* regs, const int* par_regions, const int* par_eps, int npar) {
+// Per column c = (r nf + f) npar + p of the k-space class (r: the request of
+// a group solve, whose regions are regs[r nd ..]), for the tensor-core
+// operand builder: c0 = exp(-i kz0 dz) with kz0 = sqrt(k0^2) (the phasor's
+// transverse-momentum-zero wavenumber) in FP64 (C0, also added back by the
+// scatter), and complex64 copies of c0, kz0, k0^2 and dz (col).
+struct ColTC {
+  float2 c0, kz0, k0sq;
+  float dz, pad;
+};
+__global__ void k_build_c0(double2* C0, ColTC* col, const double* freqs, int nf, int ncol, int nd,
+                           const double2* eps, const RegionT* regs, const int* par_regions, const int* par_eps,
+                           int npar) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= nf * npar) return;
-  const int f = c / npar, p = c % npar;
+  if (c >= ncol) return;
+  const int F = c / npar, p = c % npar, f = F % nf, r = F / nf;
   const double2 e = eps[par_eps[p]];
   const double2 k0 = k0_c(kC / freqs[f], e.x, e.y);
-  const double2 kz0 = dsqrt_c(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
-  const double dz = regs[par_regions[p]].dz;
-  KZ0[c] = kz0;
-  C0[c] = dexp_c(kz0.y * dz, -kz0.x * dz);
+  const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+  const double2 kz0 = dsqrt_c(k0sq.x, k0sq.y);
+  const double dz = regs[(size_t)r * nd + par_regions[p]].dz;
+  const double2 c0 = dexp_c(kz0.y * dz, -kz0.x * dz);
+  C0[c] = c0;
+  ColTC q;
+  q.c0 = make_float2((float)c0.x, (float)c0.y);
+  q.kz0 = make_float2((float)kz0.x, (float)kz0.y);
+  q.k0sq = make_float2((float)k0sq.x, (float)k0sq.y);
+  q.dz = (float)dz;
+  q.pad = 0.f;
+  col[c] = q;
+}
+
+// Principal complex square root in FP32 with the conventions of dsqrt_c (a
+// zero imaginary part keeps its sign, so real permittivities held as
+// re - 0.0im give decaying evanescent roots).
+__device__ __forceinline__ float2 fsqrt_c(float x, float y) {
+  if (x == 0.f && y == 0.f) return make_float2(0.f, y);
+  if (y == 0.f) return x > 0.f ? make_float2(sqrtf(x), y) : make_float2(0.f, copysignf(sqrtf(-x), y));
+  const float t = sqrtf((fabsf(x) + hypotf(x, y)) * 0.5f);
+  if (x >= 0.f) return make_float2(t, y / (2.f * t));
+  return make_float2(fabsf(y) / (2.f * t), copysignf(t, y));
+}
+
+// exp(re + i im) - 1 for a modest phase |im| (a few radians), all in FP32:
+// cos t - 1 = -2 sin^2(t/2) and expm1 keep it accurate relative to its own
+// magnitude.
+__device__ __forceinline__ float2 cexpm1_ff(float re, float im) {
+  const float h = sinf(0.5f * im), sn = sinf(im);
+  const float cm1 = -2.0f * h * h;
+  const float em = expm1f(re);
+  return make_float2(fmaf(em, 1.0f + cm1, cm1), (em + 1.0f) * sn);
 }
 
 // B^T of the k-space class: rows 2c, 2c + 1 = Re, Im of D[o][c] - c0[c] =
-// c0 (exp(-i (kz - kz0) dz) - 1) as TF32 pairs [2 ncol][Kp], zero for o >= K
-__global__ void k_build_d_tc(float* Bh, float* Bl, const double2* KZ, const double2* KZ0, const double2* C0, int K,
-                             int Kp, int nf, const RegionT* regs, const int* par_regions, const int* par_eps,
-                             int npar) {
+// c0 (exp(-i (kz - kz0) dz) - 1) as TF32 pairs [2 ncol][Kp], zero for o >= K.
+// kz - kz0 = -kt^2 / (kz + kz0) has no cancellation, so FP32 carries it to
+// ~1e-7 of its own size; the phase (kz - kz0) dz is a few radians at most.
+// KT2[o] = kx^2 + ky^2 at the orbit representative.
+__global__ void k_build_d_tc(float* Bh, float* Bl, const float* KT2, const ColTC* col, int K, int Kp, int ncol) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= Kp) return;
-  const int ncol = nf * npar;
+  const float kt2 = o < K ? KT2[o] : 0.f;
   for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
     float2 v = make_float2(0.f, 0.f);
     if (o < K) {
-      const int f = c / npar, p = c % npar;
-      const double dz = regs[par_regions[p]].dz;
-      const double2 kz = KZ[((size_t)par_eps[p] * nf + f) * K + o];
-      const double2 kz0 = KZ0[c];
-      const float2 m1 = cexpm1_f((kz.y - kz0.y) * dz, -(kz.x - kz0.x) * dz);
-      const float2 c0 = make_float2((float)C0[c].x, (float)C0[c].y);
-      v = make_float2(c0.x * m1.x - c0.y * m1.y, c0.x * m1.y + c0.y * m1.x);
+      const ColTC q = col[c];
+      const float2 kz = fsqrt_c(q.k0sq.x - kt2, q.k0sq.y);
+      const float2 den = make_float2(kz.x + q.kz0.x, kz.y + q.kz0.y);
+      const float dn = den.x * den.x + den.y * den.y;
+      const float2 dkz = make_float2(-kt2 * den.x / dn, kt2 * den.y / dn);   // -kt2 / den
+      const float2 m1 = cexpm1_ff(dkz.y * q.dz, -dkz.x * q.dz);
+      v = make_float2(q.c0.x * m1.x - q.c0.y * m1.y, q.c0.x * m1.y + q.c0.y * m1.x);
     }
     put_tf32(Bh, Bl, (size_t)(2 * c) * Kp + o, v.x);
     put_tf32(Bh, Bl, (size_t)(2 * c + 1) * Kp + o, v.y);
@@ -380,22 +426,23 @@ __global__ void k_build_e_tc(float* Bh, float* Bl, const int* supp, int Kd, int 
       const int reg = pix_regions[c % npx];
       const RegionT g = regs[reg];
       const double2 k0 = K0[c];
-      double re, im;
       if (g.klass == 2) {
-        re = k0.y * g.dz;   // propagator1D: exp(-i k0 dz)
-        im = -k0.x * g.dz;
+        v = cexpm1_f(k0.y * g.dz, -k0.x * g.dz);   // propagator1D: exp(-i k0 dz), a large phase
       } else {
+        // tilt and surface phases are small (k0 t ~ 0.1 rad): FP32 carries
+        // them to ~1e-8 rad
         const int x = supp[s] % nx, y = supp[s] / nx;
-        const double t = g.tx * X[x] + g.ty * Y[y];
-        re = k0.y * t;
-        im = -k0.x * t;
+        const float2 kf = make_float2((float)k0.x, (float)k0.y);
+        const float t = fmaf((float)g.tx, (float)X[x], (float)g.ty * (float)Y[y]);
+        float re = kf.y * t, im = -kf.x * t;
         if (surf) {
-          const double2 sv = surf[(size_t)reg * npix + supp[s]];
-          re += k0.x * sv.y + k0.y * sv.x;
-          im -= k0.x * sv.x - k0.y * sv.y;
+          const double2 sd = surf[(size_t)reg * npix + supp[s]];
+          const float2 sv = make_float2((float)sd.x, (float)sd.y);
+          re += kf.x * sv.y + kf.y * sv.x;
+          im -= kf.x * sv.x - kf.y * sv.y;
         }
+        v = cexpm1_ff(re, im);
       }
-      v = cexpm1_f(re, im);
     }
     put_tf32(Bh, Bl, (size_t)(2 * c) * Kdp + s, v.x);
     put_tf32(Bh, Bl, (size_t)(2 * c + 1) * Kdp + s, v.y);
@@ -407,17 +454,21 @@ __global__ void k_build_e_tc(float* Bh, float* Bl, const int* supp, int Kd, int 
 // H[r][c] = sum_z out[z][2c..2c+1][r] + cc[c] g[r] (cc = null: 1), then
 // P[m][m'] = X + iY and P[m'][m] = X - iY with X = H[2t], Y = H[2t+1], as
 // k_scatter_herm; disk regions get diag(DG) from the left.
+// One thread per (column c, pair t), t fastest: the reads of out are float2
+// runs along m, the writes stay inside one column's matrix.  nrep > 1 (the
+// pixel class of a group solve, the same for every request): the matrices of
+// column (f, q) are written for frequencies f, f + nf, ...
 template <typename PT>
 __global__ void k_scatter_herm_tc(PT* P, const float* out, int Mp, int splits, const double2* cc, const double* g,
                                   int nf, int ncols, const RegionT* regs, const int* cls_regions, int nd, int nm,
-                                  const double2* DG, const int2* tri, int T) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= T) return;
-  const int2 mp = tri[t];
+                                  const double2* DG, const int2* tri, int T, int nrep) {
   const int ncol = nf * ncols;
   const size_t plane = (size_t)2 * ncol * Mp;
-  const double g0 = g[2 * t], g1 = g[2 * t + 1];
-  for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
+  const size_t total = (size_t)ncol * T;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i / T), t = (int)(i % T);
+    const int2 mp = tri[t];
+    const double g0 = g[2 * t], g1 = g[2 * t + 1];
     const int f = c / ncols, q = c % ncols;
     const int j = cls_regions[q];
     double xr = 0.0, xi = 0.0, yr = 0.0, yi = 0.0;
@@ -440,21 +491,23 @@ __global__ void k_scatter_herm_tc(PT* P, const float* out, int Mp, int splits, c
       p1 = bf::cmul(DG[(size_t)c * nm + mp.x], p1);
       p2 = bf::cmul(DG[(size_t)c * nm + mp.y], p2);
     }
-    PT* Pj = P + ((size_t)f * nd + j) * nm * nm;
-    Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
-    if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
+    for (int r = 0; r < nrep; ++r) {
+      PT* Pj = P + ((size_t)(r * nf + f) * nd + j) * nm * nm;
+      Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
+      if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
+    }
   }
 }
 
-// D[o][f*npar + p] = exp(-i kz dz_p) (the k-space class GEMM operand)
+// D[o][(r nf + f) npar + p] = exp(-i kz dz_p) (the k-space class GEMM
+// operand); r is the request of a group solve, whose regions are regs[r nd ..].
 template <typename C>
-__global__ void k_build_d(C* D, const double2* KZ, int K, int nf, const RegionT* regs, const int* par_regions,
-                          const int* par_eps, int npar) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;   // f * npar + p
-  const int ncol = nf * npar;
+__global__ void k_build_d(C* D, const double2* KZ, int K, int nf, int ncol, int nd, const RegionT* regs,
+                          const int* par_regions, const int* par_eps, int npar) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;   // (r nf + f) npar + p
   if (c >= ncol) return;
-  const int f = c / npar, p = c % npar;
-  const double dz = regs[par_regions[p]].dz;
+  const int F = c / npar, p = c % npar, f = F % nf, r = F / nf;
+  const double dz = regs[(size_t)r * nd + par_regions[p]].dz;
   const double2* kzp = KZ + ((size_t)par_eps[p] * nf + f) * K;
   for (int o = blockIdx.y; o < K; o += gridDim.y) {
     const double2 kz = kzp[o];
@@ -541,7 +594,7 @@ __global__ void k_build_diag(double2* DG, const double2* K0, int nf, int npx, co
 // disk regions get the propagation diag(exp(-i kz_m dz)) from the left.
 template <typename PT>
 __global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const RegionT* regs,
-                            const int* cls_regions, int nd, int nm, const double2* DG) {
+                            const int* cls_regions, int nd, int nm, const double2* DG, int nrep) {
   using C = double2;
   const int mm = blockIdx.x * blockDim.x + threadIdx.x;
   if (mm >= nm * nm) return;
@@ -551,7 +604,7 @@ __global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const R
     const RegionT g = regs[j];
     C v = Gm[(size_t)mm * (nf * ncols) + c];
     if (DG && g.klass == 1) v = bf::cmul(DG[(size_t)c * nm + mm / nm], v);
-    P[(((size_t)f * nd + j) * nm) * nm + mm] = dto<PT>(v);
+    for (int r = 0; r < nrep; ++r) P[(((size_t)(r * nf + f) * nd + j) * nm) * nm + mm] = dto<PT>(v);
   }
 }
 
@@ -560,7 +613,8 @@ __global__ void k_scatter_p(PT* P, const double2* Gm, int nf, int ncols, const R
 // P[m][m'] = X + iY and P[m'][m] = X - iY; disk regions get diag(DG) from the left.
 template <typename PT>
 __global__ void k_scatter_herm(PT* P, const double2* H, int nf, int ncols, const RegionT* regs,
-                               const int* cls_regions, int nd, int nm, const double2* DG, const int2* tri, int T) {
+                               const int* cls_regions, int nd, int nm, const double2* DG, const int2* tri, int T,
+                               int nrep) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= T) return;
   const int2 mp = tri[t];
@@ -575,9 +629,11 @@ __global__ void k_scatter_herm(PT* P, const double2* H, int nf, int ncols, const
       p1 = bf::cmul(DG[(size_t)c * nm + mp.x], p1);
       p2 = bf::cmul(DG[(size_t)c * nm + mp.y], p2);
     }
-    PT* Pj = P + ((size_t)f * nd + j) * nm * nm;
-    Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
-    if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
+    for (int r = 0; r < nrep; ++r) {
+      PT* Pj = P + ((size_t)(r * nf + f) * nd + j) * nm * nm;
+      Pj[(size_t)mp.x * nm + mp.y] = dto<PT>(p1);
+      if (mp.x != mp.y) Pj[(size_t)mp.y * nm + mp.x] = dto<PT>(p2);
+    }
   }
 }
 
@@ -1298,10 +1354,11 @@ struct TfCache {
   DBuf Vr, Wr, tri;
   int T = 0;
   bool herm_w = false;
-  // BF_PREC_TF32: the real rows of both classes as TF32 hi/lo pairs [Mp][Kp],
+  // tensor-core path: the real rows of both classes as TF32 hi/lo pairs [Mp][Kp],
   // [Mp][Kdp] (rows padded to a multiple of 128, K to a multiple of 32) and
   // their FP64 row sums (gW, gV)
   DBuf Wh, Wl, Vh, Vl, gW, gV;
+  DBuf KT2;   // kx^2 + ky^2 at each orbit representative (FP32)
   int Kp = 0, Kdp = 0, Mp = 0;
   std::vector<int2> rep_h;
 };
@@ -1311,7 +1368,7 @@ static size_t tf_cache_bytes(const void* p) {
   const TfCache* c = static_cast<const TfCache*>(p);
   size_t b = 0;
   for (const DBuf* d : {&c->W, &c->V, &c->Vr, &c->Wr, &c->tri, &c->rep, &c->supp, &c->U, &c->Phi, &c->members,
-                        &c->Wh, &c->Wl, &c->Vh, &c->Vl, &c->gW, &c->gV})
+                        &c->Wh, &c->Wl, &c->Vh, &c->Vl, &c->gW, &c->gV, &c->KT2})
     b += d->p ? d->n : 0;
   return b;
 }
@@ -1329,7 +1386,7 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
   // which a stack changes after creation (bf_stack_set_distance moves the
   // disks), so gap updates of an optimiser reuse them.
   if (c.modes_id == md->id && c.mode == mode) return BF_OK;
-  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.Wr, &c.tri, &c.Wh, &c.Wl, &c.Vh, &c.Vl, &c.gW, &c.gV}) d->release();
+  for (DBuf* d : {&c.W, &c.V, &c.Vr, &c.Wr, &c.tri, &c.Wh, &c.Wl, &c.Vh, &c.Vl, &c.gW, &c.gV, &c.KT2}) d->release();
   cudaStream_t st = h->stream();
   const int nx = s->nx, ny = s->ny, nm = md->nm;
   const size_t npix = (size_t)nx * ny;
@@ -1436,6 +1493,14 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
       TCK(cudaMemsetAsync(c.gW.p, 0, sizeof(double) * c.Mp, st));
       bf::note_launch();
       k_rowsum<<<2 * c.T, 256, 0, st>>>(c.gW.as<double>(), Ad.as<double>(), c.K);
+      std::vector<float> kt2(c.K);
+      for (int o = 0; o < c.K; ++o) {
+        const double kx = s->kX[c.rep_h[o].x], ky = s->kY[c.rep_h[o].y];
+        kt2[o] = (float)(kx * kx + ky * ky);
+      }
+      TCKS(c.KT2.alloc(h, sizeof(float) * c.K));
+      TCK(cudaMemcpyAsync(c.KT2.p, kt2.data(), sizeof(float) * c.K, cudaMemcpyHostToDevice, st));
+      TCK(cudaStreamSynchronize(st));   // kt2 is a local host array
     } else if (c.herm_w) {
       TCKS(c.Wr.alloc(h, sizeof(float) * 2 * (size_t)c.T * c.K));
       k_build_wr<<<dim3(blocks_for(c.K), c.T), 256, 0, st>>>(c.Wr.as<float>(), c.U.as<double2>(),
@@ -1502,6 +1567,33 @@ static int tf_setup(bf_handle* h, bf_stack* s, bf_modes* md, int mode, TfCache**
 }
 
 static thread_local double g_tf_gemm_flops = 0.0;   // executed real flops of the class GEMMs of this thread's last solve
+// CUDA events around each class-GEMM kernel of this thread's solve (profiling only)
+static thread_local std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_gemm_ev;
+static void gemm_ev_begin(bf_handle* h) {
+  if (!h->profiling) return;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, h->stream());
+  g_gemm_ev.emplace_back(a, b);
+}
+static void gemm_ev_end(bf_handle* h) {
+  if (!h->profiling || g_gemm_ev.empty()) return;
+  cudaEventRecord(g_gemm_ev.back().second, h->stream());
+}
+// Sum of the recorded GEMM kernel times (after the stream has synchronised).
+static double gemm_ev_collect() {
+  double ms = 0.0;
+  for (auto& e : g_gemm_ev) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, e.first, e.second) == cudaSuccess) ms += t;
+    cudaEventDestroy(e.first);
+    cudaEventDestroy(e.second);
+  }
+  g_gemm_ev.clear();
+  cudaGetLastError();
+  return ms;
+}
 
 static void tf_mark(bf_handle* h, int i) {
   if (!h->profiling) return;
@@ -1516,6 +1608,7 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
   g_tf_gemm_flops += 8.0 * (double)R * (double)K * (double)N;
   dim3 grid((N + 63) / 64, (R + 63) / 64);
   bf::note_launch();
+  gemm_ev_begin(h);
   if constexpr (std::is_same<S, double2>::value) {
     bf::k_cgemm<double2><<<grid, 256, 0, h->stream()>>>(A, B, Cm, R, K, N);
   } else {
@@ -1537,6 +1630,7 @@ static int launch_gemm(bf_handle* h, const S* A, const S* B, double2* Cm, int R,
       bf::k_sum_planes<<<blocks_for(n), 256, 0, h->stream()>>>(Cm, part.as<double2>(), n, splits);
     }
   }
+  gemm_ev_end(h);
   TCK(cudaGetLastError());
   return BF_OK;
 }
@@ -1550,6 +1644,7 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
   int splits = 1;
   while (splits < 16 && tiles * splits < 2 * 152 && K / (splits * 2) >= 256) splits *= 2;
   bf::note_launch();
+  gemm_ev_begin(h);
   if (splits == 1) {
     bf::k_rcgemm_c64<8><<<grid, 256, 0, h->stream()>>>(A, B, Hm, R, K, N, K);
   } else {
@@ -1563,6 +1658,7 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
     bf::note_launch();
     bf::k_sum_planes<<<blocks_for(n), 256, 0, h->stream()>>>(Hm, part.as<double2>(), n, splits);
   }
+  gemm_ev_end(h);
   TCK(cudaGetLastError());
   return BF_OK;
 }
@@ -1577,18 +1673,26 @@ static int tc_class_gemm(bf_handle* h, const float* Ah, const float* Al, int Mp,
   g_tf_gemm_flops += 3.0 * 2.0 * (double)Mp * (double)Kp * (double)nrows_b;   // executed TF32 MMA work
   *splits = bf::tc_gemm_splits(Mp, nrows_b, Kp);
   TCKS(out.alloc(h, sizeof(float) * (size_t)*splits * nrows_b * Mp));
+  gemm_ev_begin(h);
   const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, *splits, out.as<float>(), d_err, st);
+  gemm_ev_end(h);
   if (e) return bf_fail(h, BF_ERR_CUDA, std::string("tensor-core GEMM: ") + cudaGetErrorString((cudaError_t)e));
   return BF_OK;
 }
 
 // Propagation matrices of regions [j0, nd) for all frequencies into
 // P[f][j][m][m'] stored as S, which is also the operand storage of the class
-// GEMMs: double2 (FP64 path) or float2 (mixed path).
+// GEMMs: double2 (FP64 path) or float2 (mixed path).  A group solve (nreq > 1)
+// passes the regions of nreq requests (regs[r nd + j]) that differ only in the
+// distances of their k-space (air) regions: P then holds nreq nf frequencies
+// (request r at r nf + f), the k-space class runs nreq nf npar columns, and the
+// pixel class (disks, identical across the group) runs once and is written
+// for every request.
 template <typename S>
 static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCache& c,
                                    const std::vector<RegionT>& regs, int j0, int nf,
-                                   const std::vector<double>& freqs, int prop_kind, DBuf& P, int mode) {
+                                   const std::vector<double>& freqs, int prop_kind, DBuf& P, int mode,
+                                   int nreq = 1) {
   using C = double2;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm, nx = s->nx, ny = s->ny;
@@ -1601,7 +1705,8 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
   }
   int* tc_err = reinterpret_cast<int*>(h->d_scalar + 2);   // set by the tensor-core GEMM on a wait timeout
   if (mode == 2) TCK(cudaMemsetAsync(tc_err, 0, sizeof(int), st));
-  TCKS(P.ensure(h, sizeof(S) * (size_t)nf * nd * nm * nm));
+  if (nreq > 1 && !freg.empty()) return bf_fail(h, BF_ERR_UNSUPPORTED, "group solve with tilted air regions");
+  TCKS(P.ensure(h, sizeof(S) * (size_t)nreq * nf * nd * nm * nm));
   DBuf d_regs, d_freq, d_kt, d_list;
   TCKS(d_regs.alloc(h, sizeof(RegionT) * regs.size()));
   TCK(cudaMemcpyAsync(d_regs.p, regs.data(), sizeof(RegionT) * regs.size(), cudaMemcpyHostToDevice, st));
@@ -1616,7 +1721,7 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     DBuf lst, D, G;
     TCKS(lst.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(lst.p, kreg.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
-    const int ncol = nf * npar;
+    const int ncol = nreq * nf * npar;
     // distinct permittivities of the k-space regions (normally one: air)
     std::vector<double2> eps_list;
     std::vector<int> par_eps(npar);
@@ -1633,19 +1738,21 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
     TCK(cudaMemcpyAsync(d_eps.p, eps_list.data(), sizeof(double2) * neps, cudaMemcpyHostToDevice, st));
     TCKS(d_peps.alloc(h, sizeof(int) * npar));
     TCK(cudaMemcpyAsync(d_peps.p, par_eps.data(), sizeof(int) * npar, cudaMemcpyHostToDevice, st));
-    TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
     const bool herm = mode == 1 && c.herm_w;   // real rows of W's upper triangle
     const bool tc = mode == 2 && c.herm_w;     // the same rows on the tensor cores
-    if (!tc) TCKS(G.alloc(h, sizeof(C) * (size_t)(herm ? 2 * c.T : nm * nm) * ncol));
-    bf::note_launch();
-    k_build_kz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
-        KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
-    TCK(cudaGetLastError());
+    if (!tc) {
+      TCKS(G.alloc(h, sizeof(C) * (size_t)(herm ? 2 * c.T : nm * nm) * ncol));
+      TCKS(KZ.alloc(h, sizeof(double2) * (size_t)neps * c.K * nf));
+      bf::note_launch();
+      k_build_kz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
+          KZ.as<double2>(), c.rep.as<int2>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>(), s->dkX, s->dkY);
+      TCK(cudaGetLastError());
+    }
     if (!tc) {
       TCKS(D.alloc(h, sizeof(S) * (size_t)c.K * ncol));
       bf::note_launch();
       k_build_d<S><<<dim3(blocks_for(ncol), std::min(c.K, 65535)), 256, 0, st>>>(
-          D.as<S>(), KZ.as<double2>(), c.K, nf, dr, lst.as<int>(), d_peps.as<int>(), npar);
+          D.as<S>(), KZ.as<double2>(), c.K, nf, ncol, nd, dr, lst.as<int>(), d_peps.as<int>(), npar);
       TCK(cudaGetLastError());
       if (herm) {
         if constexpr (std::is_same<S, float2>::value)
@@ -1654,40 +1761,41 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
         TCKS(launch_gemm<S>(h, c.W.as<S>(), D.as<S>(), G.as<C>(), nm * nm, c.K, ncol));
       }
     } else {
-      DBuf KZ0, C0, Bh, Bl, out;
-      TCKS(KZ0.alloc(h, sizeof(double2) * ncol));
+      DBuf C0, col, Bh, Bl, out;
       TCKS(C0.alloc(h, sizeof(double2) * ncol));
+      TCKS(col.alloc(h, sizeof(ColTC) * ncol));
       bf::note_launch();
-      k_build_c0<<<blocks_for(ncol), 256, 0, st>>>(KZ0.as<double2>(), C0.as<double2>(), d_freq.as<double>(), nf,
-                                                   d_eps.as<double2>(), dr, lst.as<int>(), d_peps.as<int>(), npar);
+      k_build_c0<<<blocks_for(ncol), 256, 0, st>>>(C0.as<double2>(), col.as<ColTC>(), d_freq.as<double>(), nf,
+                                                   ncol, nd, d_eps.as<double2>(), dr, lst.as<int>(),
+                                                   d_peps.as<int>(), npar);
       TCK(cudaGetLastError());
       const size_t nb = (size_t)2 * ncol * c.Kp;
       TCKS(Bh.alloc(h, sizeof(float) * nb));
       TCKS(Bl.alloc(h, sizeof(float) * nb));
       bf::note_launch();
       k_build_d_tc<<<dim3(blocks_for(c.Kp), std::min(ncol, 65535)), 256, 0, st>>>(
-          Bh.as<float>(), Bl.as<float>(), KZ.as<double2>(), KZ0.as<double2>(), C0.as<double2>(), c.K, c.Kp, nf, dr,
-          lst.as<int>(), d_peps.as<int>(), npar);
+          Bh.as<float>(), Bl.as<float>(), c.KT2.as<float>(), col.as<ColTC>(), c.K, c.Kp, ncol);
       TCK(cudaGetLastError());
       int splits = 1;
       TCKS(tc_class_gemm(h, c.Wh.as<float>(), c.Wl.as<float>(), c.Mp, c.Kp, Bh.as<float>(), Bl.as<float>(),
                          2 * ncol, out, &splits, tc_err));
       bf::note_launch();
-      dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+      const unsigned gs = (unsigned)std::min<size_t>(blocks_for((size_t)ncol * c.T), 1u << 20);
       k_scatter_herm_tc<S><<<gs, 256, 0, st>>>(P.as<S>(), out.as<float>(), c.Mp, splits, C0.as<double2>(),
-                                               c.gW.as<double>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
-                                               c.tri.as<int2>(), c.T);
+                                               c.gW.as<double>(), nreq * nf, npar, dr, lst.as<int>(), nd, nm,
+                                               nullptr, c.tri.as<int2>(), c.T, 1);
       TCK(cudaGetLastError());
     }
     if (!tc) {
       bf::note_launch();
       if (herm) {
         dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
-        k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
-                                              c.tri.as<int2>(), c.T);
+        k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nreq * nf, npar, dr, lst.as<int>(), nd, nm,
+                                              nullptr, c.tri.as<int2>(), c.T, 1);
       } else {
         dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
-        k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npar, dr, lst.as<int>(), nd, nm, nullptr);
+        k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nreq * nf, npar, dr, lst.as<int>(), nd, nm, nullptr,
+                                           1);
       }
       TCK(cudaGetLastError());
     }
@@ -1736,10 +1844,10 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       TCKS(tc_class_gemm(h, c.Vh.as<float>(), c.Vl.as<float>(), c.Mp, c.Kdp, Bh.as<float>(), Bl.as<float>(),
                          2 * ncol, out, &splits, tc_err));
       bf::note_launch();
-      dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
+      const unsigned gs = (unsigned)std::min<size_t>(blocks_for((size_t)ncol * c.T), 1u << 20);
       k_scatter_herm_tc<S><<<gs, 256, 0, st>>>(P.as<S>(), out.as<float>(), c.Mp, splits, nullptr, c.gV.as<double>(),
                                                nf, npx, dr, lst.as<int>(), nd, nm, DG.as<double2>(),
-                                               c.tri.as<int2>(), c.T);
+                                               c.tri.as<int2>(), c.T, nreq);
       TCK(cudaGetLastError());
     }
     if (mode != 2) {
@@ -1747,11 +1855,11 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
       if (mode == 1) {
         dim3 gs(blocks_for(c.T), std::min(ncol, 65535));
         k_scatter_herm<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
-                                              DG.as<double2>(), c.tri.as<int2>(), c.T);
+                                              DG.as<double2>(), c.tri.as<int2>(), c.T, nreq);
       } else {
         dim3 gs(blocks_for((size_t)nm * nm), std::min(ncol, 65535));
         k_scatter_p<S><<<gs, 256, 0, st>>>(P.as<S>(), G.as<C>(), nf, npx, dr, lst.as<int>(), nd, nm,
-                                           DG.as<double2>());
+                                           DG.as<double2>(), nreq);
       }
       TCK(cudaGetLastError());
     }
@@ -1941,7 +2049,7 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
 // One transformer solve (or, with only_matrices, the propagation matrices).
 // fp64 selects FP64 class-GEMM operands; otherwise double-float operands on
 // the FP32 pipes.  Propagation matrices, inverses, chain and solve are FP64.
-// After a BF_PREC_TF32 solve has synchronised: the tensor-core GEMM's error flag.
+// After a solve with the tensor-core GEMMs has synchronised: their error flag.
 static int tc_status(bf_handle* h) {
   int e = 0;
   TCK(cudaMemcpy(&e, reinterpret_cast<int*>(h->d_scalar + 2), sizeof(int), cudaMemcpyDeviceToHost));
@@ -2006,12 +2114,15 @@ static int singular_status(bf_handle* h, const int* sing, int nf, const double* 
 
 // PT: storage of the propagation matrices, their inverses and the chain:
 // double2 (FP64 path) or float2 (mixed path); the boundary solve is FP64.
+// group_regs (a group solve of nreq requests, see bf_transformer_group): the
+// regions of every request, regs[r nd + j]; the results then cover nreq nf
+// frequencies, request r at r nf + f.
 template <typename PT>
 static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                     const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                     double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
                     double* out_pm, int mode, const TraceArgs* tb = nullptr, const CoupleArgs* cp = nullptr,
-                    const PT* P_dev = nullptr) {
+                    const PT* P_dev = nullptr, const std::vector<RegionT>* group_regs = nullptr, int nreq = 1) {
   constexpr bool fp64 = std::is_same<PT, double2>::value;
   cudaStream_t st = h->stream();
   const int nd = s->nd, nm = md->nm;
@@ -2020,10 +2131,12 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     for (auto& e : eps)
       if (std::isnan(e.real()) || std::isnan(e.imag())) e = cd(1e30, 0.0);   // transformer.jl:289
   std::vector<RegionT> regs;
-  classify(h, s, prop_kind, eps, regs);
+  if (group_regs) regs = *group_regs;
+  else classify(h, s, prop_kind, eps, regs);
   std::vector<double> fv(freqs, freqs + nf);
   DBuf P, Pinv;
   g_tf_gemm_flops = 0.0;
+  gemm_ev_collect();
   tf_mark(h, 0);
   const unsigned long long l0 = bf::launch_count();
   if (pm) {
@@ -2053,7 +2166,15 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TfCache* c = nullptr;
     TCKS(tf_setup(h, s, md, mode, &c));
     const int j0 = only_matrices ? 0 : 1;
-    TCKS(tf_propagation_matrices<PT>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P, mode));
+    TCKS(tf_propagation_matrices<PT>(h, s, md, *c, regs, j0, nf, fv, prop_kind, P, mode, nreq));
+  }
+  // a group solve continues over all requests' frequencies (request r at r nf + f)
+  std::vector<double> f_all;
+  if (nreq > 1) {
+    f_all.reserve((size_t)nreq * nf);
+    for (int r = 0; r < nreq; ++r) f_all.insert(f_all.end(), freqs, freqs + nf);
+    nf *= nreq;
+    freqs = f_all.data();
   }
   if (only_matrices) {
     // out_pm: [nf][nd] Julia (nm, nm) column-major matrices
@@ -2129,8 +2250,16 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   if (emit) {
     em.assign(as_cdp(emit), as_cdp(emit) + nm);
   } else {
-    // default emit = axion_induced_modes(coords, modes; B=nothing, diskR) (transformer.jl:285)
-    TCKS(bf_axion_induced_modes(h, md, nullptr, 0.0, s->diskR, 10e9, reinterpret_cast<double*>(em.data())));
+    // default emit = axion_induced_modes(coords, modes; B=nothing, diskR) (transformer.jl:285),
+    // computed once per (modes, diskR)
+    std::lock_guard<std::mutex> lock(md->emit_mu);
+    if (md->emit_diskR != s->diskR || (int)md->emit.size() != nm) {
+      std::vector<cd> e(nm);
+      TCKS(bf_axion_induced_modes(h, md, nullptr, 0.0, s->diskR, 10e9, reinterpret_cast<double*>(e.data())));
+      md->emit = e;
+      md->emit_diskR = s->diskR;
+    }
+    em = md->emit;
   }
   DBuf d_cr, d_em, T21, T22, ax, d_refl, boost, refl, b2;
   TCKS(d_cr.alloc(h, sizeof(ChainRegion) * nd));
@@ -2225,8 +2354,8 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     h->prof[0] = t02;      // whole solve
     h->prof[1] = t01;      // propagation matrices (class GEMMs)
     h->prof[2] = t12;      // inverses, chain, boundary solve
-    h->prof[3] = 0;
-    h->prof[4] = 0;
+    h->prof[4] = (double)g_gemm_ev.size();   // class-GEMM kernel launches
+    h->prof[3] = gemm_ev_collect();          // device ms of the class-GEMM kernels alone
     h->prof[5] = (double)(bf::launch_count() - l0);
     h->prof[6] = g_tf_gemm_flops;
     h->prof[7] = nf;
@@ -2242,7 +2371,8 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   return singular_status(h, h_sing, nf, freqs);
 }
 
-// precision: BF_PREC_FP64 (mode 0), BF_PREC_MIXED (mode 1) or BF_PREC_TF32 (mode 2)
+// precision: BF_PREC_FP64 (mode 0), BF_PREC_MIXED or BF_PREC_TF32 (mode 2: the
+// tensor-core overlap GEMMs), BF_PREC_MIXED_SIMT (mode 1: the SIMT GEMMs)
 static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
                   int precision, const double* emit, const double* reflect, const double* pm, int pm_per_freq,
                   double* out_boost, double* out_refl, double* out_beta2, int mirror_1e30, int only_matrices,
@@ -2251,7 +2381,8 @@ static int tf_run(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double*
     return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
                              out_beta2, mirror_1e30, only_matrices, out_pm, 0, tb, cp);
   return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, emit, reflect, pm, pm_per_freq, out_boost, out_refl,
-                          out_beta2, mirror_1e30, only_matrices, out_pm, precision == BF_PREC_TF32 ? 2 : 1, tb, cp);
+                          out_beta2, mirror_1e30, only_matrices, out_pm, precision == BF_PREC_MIXED_SIMT ? 1 : 2, tb,
+                          cp);
 }
 
 static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const double* freqs, int prop_kind,
@@ -2263,10 +2394,11 @@ static int tf_check(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   for (int i = 0; i < nf; ++i)
     if (!(freqs[i] > 0) || !std::isfinite(freqs[i])) return bf_fail(h, BF_ERR_INVALID, "bad frequency");
   if (prop_kind < 0 || prop_kind > 3) return bf_fail(h, BF_ERR_INVALID, "unknown propagator kind");
-  if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED && precision != BF_PREC_TF32)
+  if (precision != BF_PREC_FP64 && precision != BF_PREC_MIXED && precision != BF_PREC_TF32 &&
+      precision != BF_PREC_MIXED_SIMT)
     return bf_fail(h, BF_ERR_INVALID, "unknown precision");
-  if (precision == BF_PREC_TF32 && !bf::tc_gemm_available())
-    return bf_fail(h, BF_ERR_UNSUPPORTED, "BF_PREC_TF32: the tensor-map encoder of the driver is unavailable");
+  if ((precision == BF_PREC_MIXED || precision == BF_PREC_TF32) && !bf::tc_gemm_available())
+    return bf_fail(h, BF_ERR_UNSUPPORTED, "tensor-core GEMMs: the tensor-map encoder of the driver is unavailable");
   return BF_OK;
 }
 
@@ -2325,6 +2457,60 @@ __global__ void k_tf1d(const double* dist, int nd, const Region1D* rg, const dou
   const double2 q = make_double2(-(ax.x * t22.x + ax.y * t22.y) / d, -(ax.y * t22.x - ax.x * t22.y) / d);
   if (boost) boost[i] = q;
   beta2[i] = q.x * q.x + q.y * q.y;
+}
+
+// Cross-request batch: the transformer for nreq stacks that differ only in
+// the distances of their k-space (untilted, flat air) regions, e.g. the stacks
+// of several disk-position optimisers at one step.  One solve: the air-region
+// overlaps of all requests form one GEMM, the disk regions' matrices are
+// computed once, and the inverses, chains and boundary solves run over all
+// nreq nf (request, frequency) pairs.  Outputs request-major: beta2[r nf + f],
+// boost[(r nf + f) nm + m].
+extern "C" int bf_transformer_group(bf_handle* h, int nreq, bf_stack* const* stacks, bf_modes* md, int nf,
+                                    const double* freqs, int prop_kind, int precision, double* out_boost,
+                                    double* out_beta2) {
+  if (!h) return BF_ERR_INVALID;
+  if (nreq < 1 || !stacks || !stacks[0]) return bf_fail(h, BF_ERR_INVALID, "empty group");
+  TCKS(tf_check(h, stacks[0], md, nf, freqs, prop_kind, precision));
+  const bf_stack* s0 = stacks[0];
+  const int nd = s0->nd;
+  auto same_eps = [](cd a, cd b) {
+    return (a == b) || (std::isnan(a.real()) && std::isnan(b.real()) && a.imag() == b.imag());
+  };
+  std::vector<RegionT> all, r0;
+  all.reserve((size_t)nreq * nd);
+  for (int r = 0; r < nreq; ++r) {
+    bf_stack* sr = stacks[r];
+    if (!sr) return bf_fail(h, BF_ERR_INVALID, "null stack in group");
+    bool ok = sr->nd == nd && sr->nx == s0->nx && sr->ny == s0->ny && sr->X == s0->X && sr->Y == s0->Y &&
+              sr->diskR == s0->diskR && sr->tilt_x == s0->tilt_x && sr->tilt_y == s0->tilt_y &&
+              (sr == s0 || (sr->surf.empty() && s0->surf.empty()));
+    for (int j = 0; ok && j < nd; ++j) ok = same_eps(sr->eps[j], s0->eps[j]);
+    if (!ok)
+      return bf_fail(h, BF_ERR_INVALID,
+                     "group: stacks must share grid, disk radius, permittivities and tilts, without surface maps");
+    std::vector<cd> eps(sr->eps);
+    for (auto& e : eps)
+      if (std::isnan(e.real()) || std::isnan(e.imag())) e = cd(1e30, 0.0);   // transformer.jl:289
+    std::vector<RegionT> rg;
+    classify(h, sr, prop_kind, eps, rg);
+    if (r == 0) r0 = rg;
+    for (int j = 0; j < nd; ++j) {
+      if (rg[j].klass != r0[j].klass)
+        return bf_fail(h, BF_ERR_INVALID, "group: the stacks' regions fall in different overlap classes");
+      if (j > 0 && rg[j].klass != 0 && rg[j].dz != r0[j].dz)
+        return bf_fail(h, BF_ERR_INVALID, "group: only the distances of untilted air regions may differ");
+    }
+    all.insert(all.end(), rg.begin(), rg.end());
+  }
+  TCK(cudaSetDevice(h->device));
+  bf_stack* s = stacks[0];
+  if (precision == BF_PREC_FP64)
+    return tf_run_t<double2>(h, s, md, nf, freqs, prop_kind, nullptr, nullptr, nullptr, 0, out_boost, nullptr,
+                             out_beta2, 1, 0, nullptr, 0, nullptr, nullptr, nullptr, &all, nreq);
+  return tf_run_t<float2>(h, s, md, nf, freqs, prop_kind, nullptr, nullptr, nullptr, 0, out_boost, nullptr,
+                          out_beta2, 1, 0, nullptr, precision == BF_PREC_MIXED_SIMT ? 1 : 2, nullptr, nullptr,
+                          nullptr, &all, nreq);
 }
 
 extern "C" int bf_transformer_1d_batch(bf_handle* h, int nconf, int nd, const double* distances, const double* eps,
@@ -2584,7 +2770,8 @@ extern "C" int bf_pgrid_create(bf_handle* h, bf_stack* s, bf_modes* md, int nf, 
   if (!out) return BF_ERR_INVALID;
   *out = nullptr;
   TCKS(tf_check(h, s, md, nf, freqs, prop_kind, precision));
-  if (precision == BF_PREC_TF32) return bf_fail(h, BF_ERR_INVALID, "pgrid: BF_PREC_FP64 or BF_PREC_MIXED");
+  if (precision == BF_PREC_TF32 || precision == BF_PREC_MIXED_SIMT)
+    return bf_fail(h, BF_ERR_INVALID, "pgrid: BF_PREC_FP64 or BF_PREC_MIXED");
   if (nsp < 2 || nsp > BF_PGRID_MAX_SPACINGS || !(spacing_step > 0.0) || !std::isfinite(spacing_first))
     return bf_fail(h, BF_ERR_INVALID, "pgrid: 2..64 spacings with a positive step");
   TCK(cudaSetDevice(h->device));

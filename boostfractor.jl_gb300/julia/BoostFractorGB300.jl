@@ -16,7 +16,7 @@ const lib = get(ENV, "BFGB300_LIB", joinpath(@__DIR__, "..", "lib", "libbfgb300.
 
 const BF_PROP = Dict(propagator => 0, propagatorNoTilts => 1, propagatorMomentumSpace => 2,
                      propagator1D => 3)
-const BF_PREC = Dict(:fp64 => 0, :mixed => 1, :tf32 => 2)
+const BF_PREC = Dict(:fp64 => 0, :mixed => 1, :tf32 => 2, :mixed_simt => 3)
 
 mutable struct Handle
     ptr::Ptr{Cvoid}

@@ -52,13 +52,14 @@ extern "C" {
 /* ---- arithmetic of a solve ---------------------------------------------- */
 #define BF_PREC_FP64  0  /* complex128 fields, FP64 transforms (the plain FP64 path) */
 #define BF_PREC_MIXED 1  /* complex64 fields and transforms; FP64 phase argument kz*dz,
-                            FP64 exit (bounce-sum) accumulation, FP64 final solve */
-#define BF_PREC_TF32  2  /* transformer only, no reference counterpart: the mixed path
-                            with the overlap GEMMs on the tensor cores (split TF32,
-                            FP32 accumulation per K slice).  The tensor cores' FP32
-                            accumulation truncates, so beta^2 is only within ~1e-2 of
-                            FP64 (outside the 1e-4 bar of BF_PREC_MIXED); for coarse
-                            scans */
+                            FP64 exit (bounce-sum) accumulation, FP64 final solve.  In
+                            the transformer: complex64 propagation matrices and inverses,
+                            a double-float chain, and the Hermitian overlap GEMMs on the
+                            tensor cores (split TF32, accumulator drained every 32 K) */
+#define BF_PREC_TF32  2  /* transformer only: the same as BF_PREC_MIXED (the name of
+                            its tensor-core overlap GEMMs) */
+#define BF_PREC_MIXED_SIMT 3  /* transformer only, for comparison: BF_PREC_MIXED with the
+                            overlap GEMMs on the FP32 SIMT pipes (double-float sums) */
 
 /* ---- flags -------------------------------------------------------------- */
 #define BF_OUT_DEVICE 1  /* output pointers are device pointers (results stay in HBM) */
@@ -93,7 +94,9 @@ int bf_set_stream(bf_handle* h, void* cuda_stream);
  *   [6] propagations run in the bounce stages, [7] frequencies.
  * bf_transformer_1d_batch records [0] = [1] = device ms of its kernel, [5] = 1,
  * [7] = frequencies.  The transformer records [0] whole solve, [1] propagation
- * matrices, [2] inverses, chain and boundary solve, [5] launches, [7] frequencies.
+ * matrices, [2] inverses, chain and boundary solve, [3] the class-GEMM kernels
+ * alone, [4] class-GEMM launches, [5] launches, [6] the class GEMMs' executed
+ * real flops (three MMAs per product on the tensor cores), [7] frequencies.
  * Returns BF_ERR_INVALID when the last solve did not record a profile.
  * No reference counterpart (the reference only times with @time). */
 int bf_set_profiling(bf_handle* h, int enable);
@@ -265,6 +268,21 @@ int bf_transformer(bf_handle* h, bf_stack* s, bf_modes* m, int nf, const double*
                    int prop_kind, int precision, const double* emit, const double* reflect,
                    const double* propagation_matrices, int pm_per_freq, double* out_boost,
                    double* out_refl, double* out_beta2);
+/* bf_transformer (default emission) for nreq stacks at once that differ only in
+ * the distances of their untilted air regions -- e.g. the stacks of several
+ * disk-position optimisers at one step of each, the callers of
+ * examples/transformer_optim_utilities.jl:99-144.  The stacks must share grid,
+ * disk radius, permittivities, tilts and disk thicknesses and carry no surface
+ * maps (else BF_ERR_INVALID).  One solve: the air-region overlaps of every
+ * request form one GEMM, the disk regions' matrices are computed once, the
+ * chains and boundary solves run over all (request, frequency) pairs.
+ * Outputs request-major: out_beta2[r nf + f], out_boost[(r nf + f) nm + m]
+ * (complex, NULL allowed).  Each request's result equals its own bf_transformer
+ * within rounding.  No reference counterpart (the reference solves one stack
+ * per call). */
+int bf_transformer_group(bf_handle* h, int nreq, bf_stack* const* stacks, bf_modes* m, int nf,
+                         const double* freqs, int prop_kind, int precision, double* out_boost,
+                         double* out_beta2);
 
 /* The transformer with the antenna coupling fused after the boundary solve:
  * out_coupled[f] = |sum_m conj(boost_m) antenna_m|^2, antenna = the antenna's

@@ -174,12 +174,14 @@ def test_transformer_batched_mixed_and_injected(B):
     assert rel(got, O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=freqs[2], propagation_matrices=pm)) < FP64_TOL
 
 
+@pytest.mark.parametrize("prec", ["mixed", "mixed-simt"])
 @pytest.mark.parametrize("M,L,n", [(5, 2, 32), (8, 2, 64)])
-def test_transformer_mixed_mid_mode_counts(B, M, L, n):
+def test_transformer_mixed_mid_mode_counts(B, M, L, n, prec):
     """Mixed path at 25 and 40 modes: the register-resident complex64 inverses
     (padded to 32 and 64; the 32-pixel case has propagation matrices of
-    condition ~100, so pivoting matters) and the real-row pixel-class GEMM.
-    beta^2 within 1e-4 of the oracle."""
+    condition ~100, so pivoting matters) and the real-row pixel-class GEMM, on
+    the tensor cores (mixed) and on the SIMT pipes (mixed-simt).  beta^2
+    within 1e-4 of the oracle."""
     distance, eps, tx, ty, X, s = _stack(2, n, seed=M, surf=True)
     kw = dict(diskno=2, distance=distance, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty,
               relative_surfaces=s)
@@ -188,7 +190,7 @@ def test_transformer_mixed_mid_mode_counts(B, M, L, n):
     mo = O.seed_modes(co, ThreeDim=True, Mmax=M, Lmax=L, diskR=0.15)
     assert mb.nm == M * (2 * L + 1)
     freqs = np.array([19.6e9, 20.3e9])
-    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision=prec)
     for k, f in enumerate(freqs):
         ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
         r2 = np.sum(np.abs(ref) ** 2)
@@ -196,13 +198,14 @@ def test_transformer_mixed_mid_mode_counts(B, M, L, n):
         assert rel(b32[k], ref) < 1e-3
 
 
+@pytest.mark.parametrize("prec", ["mixed", "mixed-simt"])
 @pytest.mark.parametrize("cut", [0.15, 0.3])
-def test_transformer_mixed_modes_inside_and_beyond_mask(B, cut):
+def test_transformer_mixed_modes_inside_and_beyond_mask(B, cut, prec):
     """Laguerre-Gauss pattern_input cut at r <= 0.15 m (inside the 0.15 m disk
     mask: the k-space overlaps are Hermitian in the mode pair and the mixed
-    path runs their upper triangle as real rows) and at r <= 0.3 m (non-zero
-    outside the mask: the full complex overlap GEMM).  Mixed beta^2 within
-    1e-4 of the oracle either way."""
+    path runs their upper triangle as real rows, on the tensor cores) and at
+    r <= 0.3 m (non-zero outside the mask: the full complex overlap GEMM on the
+    SIMT pipes).  Mixed beta^2 within 1e-4 of the oracle either way."""
     from bfgb300 import workloads as W
     distance, eps, tx, ty, _, _ = _stack(3, 64, seed=53, tilt_air=True)
     X = W.symmetric_grid(64, width=0.4)
@@ -214,7 +217,7 @@ def test_transformer_mixed_modes_inside_and_beyond_mask(B, cut):
     outside = (X[:, None] ** 2 + X[None, :] ** 2) >= 0.15 ** 2
     assert np.any(np.abs(pats[:, 0, :, :, 0][:, outside]) > 0) == (cut > 0.15)
     freqs = np.array([19.4e9, 20.7e9])
-    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision="mixed")
+    b32 = B.transformer(B.SeedSetupBoundaries(cb, **kw), cb, mb, f=freqs, precision=prec)
     for k, f in enumerate(freqs):
         ref = O.transformer(O.seed_setup_boundaries(co, **kw), co, mo, f=f)
         r2 = np.sum(np.abs(ref) ** 2)
@@ -252,7 +255,7 @@ def test_transformer_full_size_lg_vs_oracle_fixture(B):
     """The full transformer workload (20 disks with surface maps, 64
     Laguerre-Gauss modes, 256x256) at three of its frequencies against the
     oracle's boost stored by tests/golden/make_c3_fixture.py: FP64 within 1e-10,
-    mixed beta^2 within 1e-4."""
+    mixed beta^2 within 1e-4 (tensor-core and SIMT overlap GEMMs)."""
     import os
     from bfgb300 import workloads as W
     fx = np.load(os.path.join(os.path.dirname(__file__), "golden", "c3_lg_oracle.npz"))
@@ -266,9 +269,12 @@ def test_transformer_full_size_lg_vs_oracle_fixture(B):
                     pattern_input=w["pattern_input"], kT_arr=w["kT_arr"])
     b64 = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"])
     b32 = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"], precision="mixed")
+    bs = B.transformer(B.SeedSetupBoundaries(c, **kw), c, m, f=fx["freqs"], diskR=w["diskR"],
+                       precision="mixed-simt")
     for k in range(len(fx["freqs"])):
         assert rel(b64[k], fx["boost"][k]) < FP64_TOL
         assert abs(np.sum(np.abs(b32[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
+        assert abs(np.sum(np.abs(bs[k]) ** 2) - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
 
 
 def _lg_reduced(B):
@@ -471,3 +477,56 @@ def test_singular_propagation_matrix_raises(B, M, precision):
         else:
             r2 = np.sum(np.abs(ref) ** 2)
             assert abs(np.sum(np.abs(got) ** 2) - r2) / r2 < MIXED_BETA2_TOL
+
+
+def _alone(B, st, modes, freqs, precision):
+    from bfgb300 import _lib
+    nf, nm = len(freqs), modes.nm
+    boost = np.empty((nf, nm), dtype=np.complex128)
+    b2 = np.empty(nf)
+    st.h.check(_lib.lib().bf_transformer(st.h.ptr, st._s, modes._m, nf, _lib.ptr(freqs), _lib.BF_PROP_3D,
+                                         B._prec(precision), None, None, None, 0,
+                                         _lib.ptr(boost.view(np.float64)), None, _lib.ptr(b2)))
+    return boost, b2
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_transformer_group_equals_alone(B, prec):
+    """A group solve of three stacks that differ only in their air gaps (one
+    step of three optimisers) gives every stack its own solve's result: FP64
+    within 1e-12, mixed beta^2 within 1e-4; the FP64 group also matches the
+    oracle.  A stack with other permittivities is refused."""
+    from bfgb300 import workloads as W, _lib
+    distance, eps, tx, ty, _, _ = _stack(4, 64, seed=61)
+    X = W.symmetric_grid(64, width=0.4)
+    pats, kt = W.lg_modes(X, X, 12, 0.03, 0.15)
+    cb, co = B.SeedCoordinateSystem(X=X, Y=X), O.seed_coordinate_system(X=X, Y=X)
+    mb = B.SeedModes(cb, ThreeDim=True, Mmax=12, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+    freqs = np.array([19.4e9, 20.05e9, 20.6e9])
+    rng = np.random.default_rng(62)
+    kws, stacks = [], []
+    for r in range(3):
+        d = np.array(distance)
+        d[1:-1:2] += rng.normal(0.0, 2e-4, len(d[1:-1:2]))
+        kw = dict(diskno=4, distance=d, epsilon=eps, relative_tilt_x=tx, relative_tilt_y=ty)
+        kws.append(kw)
+        stacks.append(B.Stack(B.SeedSetupBoundaries(cb, **kw), cb, 0.15, handle=mb.h))
+    b2g, bg = B.transformer_group(stacks, mb, freqs, precision=prec, want_boost=True)
+    for r, st in enumerate(stacks):
+        boost, b2 = _alone(B, st, mb, freqs, prec)
+        if prec == "fp64":
+            assert rel(bg[r], boost) < 1e-12
+        assert np.max(np.abs(b2g[r] - b2) / b2) < (1e-12 if prec == "fp64" else MIXED_BETA2_TOL)
+    if prec == "fp64":
+        mo = O.seed_modes(co, ThreeDim=True, Mmax=12, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt)
+        ref = O.transformer(O.seed_setup_boundaries(co, **kws[1]), co, mo, f=freqs[2])
+        assert rel(bg[1][2], ref) < FP64_TOL
+    other = np.array(eps)
+    other[2] = 9.4
+    odd = B.Stack(B.SeedSetupBoundaries(cb, diskno=4, distance=distance, epsilon=other, relative_tilt_x=tx,
+                                        relative_tilt_y=ty), cb, 0.15, handle=mb.h)
+    with pytest.raises(B.BFError) as e:
+        B.transformer_group([stacks[0], odd], mb, freqs, precision=prec)
+    assert e.value.code == _lib.BF_ERR_INVALID
+    for st in stacks + [odd]:
+        st.close()

@@ -129,3 +129,28 @@ def test_close_cancels_queued_requests(B):
     t0 = time.perf_counter()
     srv.close()
     assert time.perf_counter() - t0 < 0.5   # only the running one is waited for
+
+
+def test_transformer_steps_of_different_stacks_form_one_group(B):
+    """Queued transformer requests on different stacks with the same mode
+    basis and frequencies join one group solve (one start time); a second
+    request on a stack already in the group waits for it."""
+    import ctypes
+    import types
+    modes = types.SimpleNamespace(_m=ctypes.c_void_p(0x9990), nm=1)
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=1, dry_run=True)
+    try:
+        busy = srv.submit(0xA000, [1e10], nmax=50000, footprint_bytes=MB)
+        time.sleep(0.01)   # the worker is busy; the group queues behind it
+        f = [1e10, 1.1e10]
+        grp = [srv.submit(0xB000 + 16 * k, f, "transformer", modes=modes, nmax=1000, distance=[0.0],
+                          footprint_bytes=MB) for k in range(5)]
+        again = srv.submit(0xB000, f, "transformer", modes=modes, nmax=1000, distance=[0.0], footprint_bytes=MB)
+        r0 = srv.wait(busy, timeout_ms=20000)
+        rg = [srv.wait(i, timeout_ms=20000) for i in grp]
+        ra = srv.wait(again, timeout_ms=20000)
+        assert len({r["t_start"] for r in rg}) == 1 and rg[0]["t_start"] >= r0["t_done"]
+        assert ra["t_start"] >= rg[0]["t_done"]
+        assert srv.stats("transformer")["batched"] == 4
+    finally:
+        srv.close()
