@@ -567,7 +567,11 @@ def run_transformer(args):
 # --------------------------------------------------------------------------
 # uneven batch and serving (the request loop of bf_server)
 # --------------------------------------------------------------------------
-def _build_request_stack(B, W, h, req):
+def _build_request_stack(B, W, h, req, mode_cache=None):
+    """A request's resident stack and, for the transformer, its mode basis.
+    With mode_cache (a dict), requests on the same grid with the same mode
+    set share one basis, as optimisers of one booster design do; shared
+    bases are closed by the caller through the cache."""
     c = B.SeedCoordinateSystem(X=req["X"], Y=req["X"])
     sb = B.SeedSetupBoundaries(c, diskno=req["ndisk"], distance=req["distance"], epsilon=req["eps"],
                                relative_tilt_x=req["relative_tilt_x"], relative_tilt_y=req["relative_tilt_y"])
@@ -575,10 +579,24 @@ def _build_request_stack(B, W, h, req):
     st = B.Stack(sb, c, req["diskR"], handle=h)
     modes = None
     if req["solver"] == "transformer":
-        pats, kt = W.lg_modes(c.X, c.Y, req["M"], req["waist"], req["diskR"])
-        modes = B.SeedModes(c, ThreeDim=True, Mmax=req["M"], Lmax=0, diskR=req["diskR"], pattern_input=pats,
-                            kT_arr=kt, handle=h)
+        key = (len(req["X"]), req["M"], req["waist"], req["diskR"])
+        modes = None if mode_cache is None else mode_cache.get(key)
+        if modes is None:
+            pats, kt = W.lg_modes(c.X, c.Y, req["M"], req["waist"], req["diskR"])
+            modes = B.SeedModes(c, ThreeDim=True, Mmax=req["M"], Lmax=0, diskR=req["diskR"], pattern_input=pats,
+                                kT_arr=kt, handle=h)
+            if mode_cache is not None:
+                mode_cache[key] = modes
     return st, modes
+
+
+def _close_all(stacks, mode_cache=None):
+    for st, m in stacks:
+        if m is not None and mode_cache is None:
+            m.close()
+        st.close()
+    for m in (mode_cache or {}).values():
+        m.close()
 
 
 def _solve_plain(B, h, st, modes, req, precision="mixed"):
@@ -623,22 +641,21 @@ def run_uneven(args):
     plain = [_solve_plain(B, h, st, m, r) for (st, m), r in zip(plain_set, reqs)]
     t_plain = time.perf_counter() - t0
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
-    clock = ClockSampler(0)
-    clock.start()
-    t0 = time.perf_counter()
-    ids = [srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision="mixed")
-           for (st, m), r in zip(batch_set, reqs)]
-    res = [srv.wait(i) for i in ids]
-    t_batch = time.perf_counter() - t0
-    clocks = clock.stop()
+    try:
+        clock = ClockSampler(0)
+        clock.start()
+        t0 = time.perf_counter()
+        ids = [srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision="mixed")
+               for (st, m), r in zip(batch_set, reqs)]
+        res = [srv.wait(i) for i in ids]
+        t_batch = time.perf_counter() - t0
+        clocks = clock.stop()
+        st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
+    finally:
+        srv.close()   # before the stacks it serves
     worst = max(float(np.max(np.abs(r["beta2"] - p) / np.abs(p))) for r, p in zip(res, plain))
     fpts = sum(len(r["freqs"]) for r in reqs)
-    st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
-    srv.close()
-    for st, m in plain_set + batch_set:
-        if m is not None:
-            m.close()
-        st.close()
+    _close_all(plain_set + batch_set)
     h.close()
     _server_line(
         "beta2 freq-points/s (uneven batch of disk stacks: 5-80 disks, 64/128/256 grids, 64-1024 freqs, "
@@ -733,12 +750,16 @@ def run_serve(args, optimiser_class=False):
     else:
         reqs = W.config4_uneven(seed=5, count=nclients)
     h = B.Handle(0)
-    stacks = [_build_request_stack(B, W, h, r) for r in reqs]
+    mode_cache = {}
+    stacks = [_build_request_stack(B, W, h, r, mode_cache) for r in reqs]
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
-    # one warm-up step per client (builds the resident overlaps / plans), untimed
-    for (st, m), r in zip(stacks, reqs):
-        srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"], precision=args.serve_precision))
-    srv.close()
+    try:
+        # one warm-up step per client (builds the resident overlaps / plans), untimed
+        for (st, m), r in zip(stacks, reqs):
+            srv.wait(srv.submit(st, r["freqs"], r["solver"], modes=m, nmax=r["nmax"],
+                                precision=args.serve_precision))
+    finally:
+        srv.close()
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
     rngs = [np.random.default_rng(1000 + k) for k in range(nclients)]
     dist = [np.array(r["distance"]) for r in reqs]
@@ -751,16 +772,16 @@ def run_serve(args, optimiser_class=False):
         return srv.submit(st, r["freqs"], r["solver"], modes=m, distance=dist[k], nmax=r["nmax"],
                           precision=args.serve_precision), classes[k]
 
-    clock = ClockSampler(0)
-    clock.start()
-    recs, wall, n_arr, unfinished, failed = _open_loop(srv, nclients, args.rate, args.serve_seconds, submit_one)
-    clocks = clock.stop()
-    st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
-    srv.close()
-    for st, m in stacks:
-        if m is not None:
-            m.close()
-        st.close()
+    try:
+        clock = ClockSampler(0)
+        clock.start()
+        recs, wall, n_arr, unfinished, failed = _open_loop(srv, nclients, args.rate, args.serve_seconds,
+                                                           submit_one)
+        clocks = clock.stop()
+        st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
+    finally:
+        srv.close()   # cancels what is still queued, waits for what runs
+    _close_all(stacks, mode_cache)
     h.close()
     lat = np.array([r["latency_ms"] for r in recs]) if recs else np.zeros(1)
     per_class = {}
@@ -793,8 +814,9 @@ def run_serve_pgrid(args):
     with its own resident grid (20 disks, 256 frequencies, 8 Laguerre-Gauss
     modes, 128x128 over 1 m, 9 spacings from -200 um to +200 um, built at
     mixed precision).  Every step random-walks the per-disk shifts by
-    N(0, 10 um) inside the grid, submits a "pgrid" request, waits for beta^2
-    and thinks for an exponential time of mean 32/2000 s.  This is the
+    N(0, 10 um) inside the grid and submits a "pgrid" request; the steps
+    arrive open loop, a Poisson process of mean rate --rate (2000/s) with
+    each arrival assigned to a uniformly drawn client.  This is the
     interpolated-matrix optimiser loop: a step solves the stack at the
     interpolated matrices instead of recomputing them."""
     import torch
@@ -821,51 +843,47 @@ def run_serve_pgrid(args):
         grids.append(B.PGrid(sb, c, modes, freqs, sgrid, precision="mixed"))
     t_create = (time.perf_counter() - t0) / nclients
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
-    for g in grids:   # one warm-up step per client, untimed
-        srv.wait(srv.submit(None, freqs, "pgrid", distance=np.zeros(ndisk), pgrid=g))
-    srv.close()
+    try:
+        for g in grids:   # one warm-up step per client, untimed
+            srv.wait(srv.submit(None, freqs, "pgrid", distance=np.zeros(ndisk), pgrid=g))
+    finally:
+        srv.close()
     srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
-    deadline = time.perf_counter() + args.serve_seconds
-    errors = []
     lo, hi = sgrid[0], sgrid[-1]
+    rngs = [np.random.default_rng(1000 + k) for k in range(nclients)]
+    shifts = [np.zeros(ndisk) for _ in range(nclients)]
 
-    def client(k):
-        rng = np.random.default_rng(1000 + k)
-        sh = np.zeros(ndisk)
-        try:
-            while time.perf_counter() < deadline:
-                sh = np.clip(sh + rng.normal(0.0, 10e-6, ndisk), lo, hi)
-                srv.wait(srv.submit(None, freqs, "pgrid", distance=sh, pgrid=grids[k]))
-                time.sleep(rng.exponential(nclients / 2000.0))
-        except Exception as e:  # reported in the JSON line
-            errors.append(repr(e))
+    def submit_one(k):
+        shifts[k] = np.clip(shifts[k] + rngs[k].normal(0.0, 10e-6, ndisk), lo, hi)
+        return srv.submit(None, freqs, "pgrid", distance=shifts[k], pgrid=grids[k]), "pgrid"
 
-    clock = ClockSampler(0)
-    clock.start()
-    t0 = time.perf_counter()
-    threads = [threading.Thread(target=client, args=(k,)) for k in range(nclients)]
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    wall = time.perf_counter() - t0
-    clocks = clock.stop()
-    st_all = srv.stats()
-    srv.close()
+    try:
+        clock = ClockSampler(0)
+        clock.start()
+        recs, wall, n_arr, unfinished, failed = _open_loop(srv, nclients, args.rate, args.serve_seconds,
+                                                           submit_one)
+        clocks = clock.stop()
+        st_all = srv.stats()
+    finally:
+        srv.close()
     for g in grids:
         g.close()
     modes.close()
     h.close()
+    lat = np.array([r["latency_ms"] for r in recs]) if recs else np.zeros(1)
+    errors = [] if not failed else [f"{failed} failed requests"]
     _server_line(
-        "beta2 freq-points/s and p50/p99 latency, 32 optimiser clients, interpolated propagation-matrix grids "
-        "(20 disks, 256 freqs, 8 LG modes, 128x128)", st_all["freq_points"] / wall, st_all["completed"], wall,
-        {"config": {"workload": "serve-pgrid-optimiser-class", "clients": nclients, "disks": ndisk, "freqs": nf,
+        f"beta2 freq-points/s and p50/p99 latency, Poisson arrivals at {args.rate:g}/s from 32 optimiser clients, "
+        "interpolated propagation-matrix grids (20 disks, 256 freqs, 8 LG modes, 128x128)",
+        nf * len(recs) / wall, len(recs), wall,
+        {"config": {"workload": "serve-pgrid-optimiser-class", "arrivals": "poisson", "rate_per_s": args.rate,
+                    "clients": nclients, "disks": ndisk, "freqs": nf,
                     "modes": M, "grid": n, "spacings": len(sgrid), "spacing_range_um": [-200, 200],
-                    "think_mean_ms": 1000.0 * nclients / 2000.0, "seconds": args.serve_seconds,
-                    "workers": args.workers, "gap_step_um": 10, "precision": "mixed"},
-         "latency_ms": {"p50": st_all["p50_ms"], "p99": st_all["p99_ms"], "mean": st_all["mean_ms"],
-                        "max": st_all["max_ms"]},
-         "requests_per_s": st_all["completed"] / wall, "grid_create_s_per_client": t_create,
+                    "seconds": args.serve_seconds, "workers": args.workers, "gap_step_um": 10, "precision": "mixed"},
+         "offered": n_arr, "completed": len(recs), "unfinished_after_drain": unfinished, "failed": failed,
+         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                        "mean": float(lat.mean()), "max": float(lat.max())},
+         "requests_per_s": len(recs) / wall, "grid_create_s_per_client": t_create,
          "evictions": st_all["evictions"], "client_errors": errors[:3], "clocks": clocks})
 
 

@@ -17,7 +17,9 @@ keep the reference behaviour):
 """
 import ctypes
 import math
+import atexit
 import threading
+import weakref
 
 import numpy as np
 
@@ -367,8 +369,10 @@ class Stack:
         return out.transpose(0, 3, 2, 1), beta2
 
     def close(self):
+        """bf_stack_destroy; refused (BFError) while a server still has
+        requests on the stack, which then stays open."""
         if getattr(self, "_s", None) and self.h._h:
-            _lib.lib().bf_stack_destroy(self.h.ptr, self._s)
+            self.h.check(_lib.lib().bf_stack_destroy(self.h.ptr, self._s))
         self._s = None
 
     def __del__(self):
@@ -459,8 +463,10 @@ class Modes:
         return out.T
 
     def close(self):
+        """bf_modes_destroy; refused (BFError) while a server still has
+        requests on the basis, which then stays open."""
         if getattr(self, "_m", None) and self.h._h:
-            _lib.lib().bf_modes_destroy(self.h.ptr, self._m)
+            self.h.check(_lib.lib().bf_modes_destroy(self.h.ptr, self._m))
         self._m = None
 
     def __del__(self):
@@ -823,6 +829,20 @@ def calc_boostfactor_cost(dist_shift, itp, frequencies, sbdry, coords, modes, m_
     return itp.cost(dist_shift, m_reflect, p=-20.0)[0]
 
 
+_live_servers = weakref.WeakSet()
+
+
+@atexit.register
+def _close_servers():
+    """At interpreter exit, servers close (finishing their running solves)
+    before the stacks and mode bases they serve are collected."""
+    for srv in list(_live_servers):
+        try:
+            srv.close()
+        except Exception:
+            pass
+
+
 class Server:
     """A request loop over resident stacks (bf_server_create / bf_submit /
     bf_wait).  Requests on different stacks run concurrently on ``n_workers``
@@ -840,6 +860,7 @@ class Server:
             raise BFError(rc, "bf_server_create failed")
         self._p = p
         self._live = {}   # id -> (request struct, freqs, outputs): kept alive until completion
+        _live_servers.add(self)
 
     def _check(self, rc):
         if rc != _lib.BF_OK:

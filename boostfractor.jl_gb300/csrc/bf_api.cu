@@ -346,11 +346,13 @@ static void stack_free(bf_handle* h, bf_stack* s) {
   s->d_geo = nullptr;
 }
 
+// The copy is stream-ordered after the stack's earlier work on h's stream; a
+// copy from pageable memory is staged before cudaMemcpyAsync returns, so the
+// local vector may go away without waiting for the stream.
 static int stack_upload_geo(bf_handle* h, bf_stack* s) {
   std::vector<RegionGeo> g;
   geo_of(s, g);
   CK(cudaMemcpyAsync(s->d_geo, g.data(), sizeof(RegionGeo) * g.size(), cudaMemcpyHostToDevice, h->stream()));
-  CK(cudaStreamSynchronize(h->stream()));
   return BF_OK;
 }
 
@@ -451,6 +453,10 @@ extern "C" int bf_stack_create(bf_handle* h, int nd, const double* distance, con
 
 extern "C" int bf_stack_destroy(bf_handle* h, bf_stack* s) {
   if (!h || !s) return BF_ERR_INVALID;
+  // a serving engine's worker may be solving on it (its stream, not h's):
+  // freeing the stack's memory now would pull it from under those kernels
+  if (s->server_uses.n.load() > 0)
+    return fail(h, BF_ERR_INVALID, "stack is in use by a serving engine: destroy the server first");
   cudaStreamSynchronize(h->stream());
   stack_free(h, s);
   delete s;
@@ -488,12 +494,22 @@ size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, in
   const size_t nd = (size_t)s->nd, F = (size_t)std::max(nf, 1);
   const size_t csz = precision == BF_PREC_FP64 ? 16 : 8;
   if (solver == 2) {
-    // resident overlaps (orbit-folded k-space W, pixel V), per solve: P and
-    // its inverses/chain (FP64), the class GEMM operands and products
-    const size_t m2 = (size_t)nm * nm;
+    // resident overlaps (orbit-folded k-space W over K orbits, pixel V over
+    // the ~Kd support pixels, as real rows of the upper triangle and TF32
+    // pairs, or complex128 on the FP64 path); per solve: P, inverses and the
+    // chain per (frequency, region), and per column the class GEMM operands
+    // (16 B per orbit or support pixel) and outputs
+    const size_t m2 = (size_t)nm * nm, rows = ((m2 + nm + 127) / 128) * 128;
     const size_t K = s->kx_sym ? ((size_t)s->nx / 2 + 1) * ((size_t)s->ny / 2 + 1) : npix;
-    const size_t cache = s->tf_cache ? 0 : 16 * m2 * (K + npix) + 32 * nm * npix;
-    return cache + F * nd * (16 * 4 * m2 + 16 * (K + npix) + 16 * m2) + 16 * npix * nm * 2;
+    size_t inmask = 0;
+    for (uint8_t v : s->mask_full) inmask += v;
+    const size_t Kd = std::min(npix, 2 * inmask + 64);   // modes cut near the disk radius
+    size_t nair = 0;
+    for (size_t j = 1; j < nd; ++j) nair += s->eps[j].real() == 1.0;
+    const size_t ndisk = nd - 1 - nair;
+    const size_t cache = s->tf_cache ? 0 : (16 * rows + 8 * rows) * (K + Kd) + 32 * (size_t)nm * npix;
+    return cache + F * nd * (16 * 4 * m2 + 64) + F * (nair * (16 * K + 32 * rows) + ndisk * (16 * Kd + 32 * rows)) +
+           16 * npix * nm * 2;
   }
   if (prop_kind == BF_PROP_1D) return F * (16 * 4 * nd * npix + 64);
   const size_t slots = 2 * nd + 2;

@@ -5,6 +5,7 @@
 // -ffp-contract=off so the results match on x86-64 and aarch64.
 #pragma once
 
+#include <atomic>
 #include <complex>
 #include <mutex>
 #include <cstdint>
@@ -141,6 +142,14 @@ struct bf_stack {
   bf::RegionGeo* d_geo = nullptr;  // [region]
   Workspace* ws = nullptr;
   unsigned long long geo_version = 0;  // bumps when the geometry changes
+  // requests of a serving engine queued or running on the stack (a copy of
+  // the stack starts with none)
+  struct UseCount {
+    std::atomic<int> n{0};
+    UseCount() = default;
+    UseCount(const UseCount&) {}
+    UseCount& operator=(const UseCount&) { return *this; }
+  } server_uses;
   void* tf_cache = nullptr;            // transformer setup (mode FFT overlaps) of this stack
   void (*tf_cache_delete)(void*) = nullptr;
   size_t (*tf_cache_bytes)(const void*) = nullptr;
@@ -157,6 +166,9 @@ void bf_stack_trim(bf_stack* s);
 // with nm modes.
 // Frequencies, regions, modes and stack of a propagation-matrix grid.
 void bf_pgrid_shape(const bf_pgrid* g, int* nf, int* nd, int* nm, bf_stack** stack);
+// Serving-engine requests queued or running on a mode basis (delta +1 / -1);
+// bf_modes_destroy refuses while any are.
+void bf_modes_server_use(bf_modes* m, int delta);
 size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, int prop_kind, int precision);
 
 namespace bfhost {

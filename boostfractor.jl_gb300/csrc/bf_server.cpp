@@ -340,6 +340,11 @@ void worker(bf_server* S, int w) {
       res.push_back(S->dry() ? (size_t)std::max<unsigned long long>(R->r.footprint_bytes, 1)
                              : bf_stack_device_bytes(R->r.stack));
     }
+    if (!S->dry())
+      for (Req* R : b.reqs) {
+        R->r.stack->server_uses.n--;
+        if (R->r.solver == BF_SOLVER_TRANSFORMER) bf_modes_server_use(R->r.modes, -1);
+      }
     lock.lock();
     const double t_done = S->now();
     S->inflight -= b.need;
@@ -447,6 +452,10 @@ extern "C" int bf_server_destroy(bf_server* S) {
     for (Req* R : S->queue) {
       R->status = BF_ERR_INVALID;
       R->t_done = S->now();
+      if (!S->dry()) {
+        R->r.stack->server_uses.n--;
+        if (R->r.solver == BF_SOLVER_TRANSFORMER) bf_modes_server_use(R->r.modes, -1);
+      }
     }
     S->queue.clear();
     S->cv_work.notify_all();
@@ -536,6 +545,11 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
   }
   R->id = S->next_id++;
   R->t_submit = S->now();
+  // the stack may not be destroyed while this request is queued or running
+  if (!S->dry()) {
+    R->r.stack->server_uses.n++;
+    if (R->r.solver == BF_SOLVER_TRANSFORMER) bf_modes_server_use(R->r.modes, +1);
+  }
   if (S->t_first < 0) S->t_first = R->t_submit;
   S->stacks.emplace(q->stack, StackInfo());
   S->reqs[R->id] = R;

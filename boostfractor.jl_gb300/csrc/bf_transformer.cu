@@ -59,7 +59,12 @@ struct bf_modes {
   std::mutex emit_mu;
   double emit_diskR = -1.0;
   std::vector<cd> emit;
+  std::atomic<int> server_uses{0};   // serving-engine requests queued or running on it
 };
+
+void bf_modes_server_use(bf_modes* m, int delta) {
+  if (m) m->server_uses += delta;
+}
 
 // engine-wide helpers from bf_api.cu
 int bf_fail(bf_handle* h, int code, const std::string& msg);
@@ -1073,6 +1078,15 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
     ax[m] = make_double2(0.0, 0.0);
     em[m] = dfc_from(emit[m]);
   }
+  // one matrix entry per thread (small mode counts): the next region's P and
+  // inverse(P) are loaded into registers one region ahead, so their latency
+  // hides behind this region's products
+  const bool ahead = n2 <= nt;
+  float2 pn = make_float2(0.f, 0.f), qn = pn;
+  if (ahead && tid < n2 && nd > 1) {
+    pn = P[(((size_t)f * nd + 1) * nm) * nm + tid];
+    qn = Pinv[(((size_t)f * nd + 1) * nm) * nm + tid];
+  }
   __syncthreads();
   for (int j = 1; j < nd; ++j) {
     const ChainRegion g = cr[j];
@@ -1094,11 +1108,22 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
       U[e] = dfc_add(dfc_mul(a, t1), dfc_mul(b, t2));
       V[e] = dfc_add(dfc_mul(b, t1), dfc_mul(a, t2));
     }
-    const float2* Pj = P + (((size_t)f * nd + j) * nm) * nm;
-    const float2* Qj = Pinv + (((size_t)f * nd + j) * nm) * nm;
-    for (int e = tid; e < n2; e += nt) {
-      Ps[e] = Pj[e];
-      Qs[e] = Qj[e];
+    if (ahead) {
+      if (tid < n2) {
+        Ps[tid] = pn;
+        Qs[tid] = qn;
+        if (j + 1 < nd) {
+          pn = P[(((size_t)f * nd + j + 1) * nm) * nm + tid];
+          qn = Pinv[(((size_t)f * nd + j + 1) * nm) * nm + tid];
+        }
+      }
+    } else {
+      const float2* Pj = P + (((size_t)f * nd + j) * nm) * nm;
+      const float2* Qj = Pinv + (((size_t)f * nd + j) * nm) * nm;
+      for (int e = tid; e < n2; e += nt) {
+        Ps[e] = Pj[e];
+        Qs[e] = Qj[e];
+      }
     }
     __syncthreads();
     if (Wt)   // reads only Wt: runs alongside the product below, which rewrites T
@@ -1966,6 +1991,8 @@ extern "C" int bf_modes_create(bf_handle* h, int nx, int ny, const double* X, co
 
 extern "C" int bf_modes_destroy(bf_handle* h, bf_modes* m) {
   if (!h || !m) return BF_ERR_INVALID;
+  if (m->server_uses.load() > 0)
+    return bf_fail(h, BF_ERR_INVALID, "mode basis is in use by a serving engine: destroy the server first");
   cudaStreamSynchronize(h->stream());
   bf_dfree(h, m->d_pat);
   delete m;

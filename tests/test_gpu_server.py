@@ -121,3 +121,73 @@ def test_optimiser_gap_steps_in_submission_order(B):
         s_ref.close()
         s_srv.close()
         h.close()
+
+
+def test_optimiser_steps_of_several_stacks_share_one_solve(B):
+    """Transformer steps of six optimisers of one booster design (same mode
+    basis, grid and disks, different gaps) queued together are solved as one
+    group (bf_transformer_group); each result matches the stack solved alone
+    at the same gaps: mixed beta^2 within 1e-4, FP64 within 1e-12."""
+    from bfgb300 import workloads as W
+    h = B.Handle(0)
+    s_busy, _, _ = stack(B, h, 64, 3, 40)
+    base, c, d0 = stack(B, h, 48, 3, 41)
+    pats, kt = W.lg_modes(c.X, c.Y, 6, 0.03, 0.15)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=6, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt, handle=h)
+    rng = np.random.default_rng(42)
+    stacks, dists = [], []
+    for k in range(6):
+        st, _, _ = stack(B, h, 48, 3, 41)
+        d = d0.copy()
+        d[1:-1:2] += rng.normal(0.0, 50e-6, len(d[1:-1:2]))
+        stacks.append(st)
+        dists.append(d)
+    freqs = np.linspace(19.6e9, 20.4e9, 12)
+    srv = B.Server(n_workers=1)
+    try:
+        for prec, tol in (("mixed", 1e-4), ("fp64", TOL)):
+            busy = srv.submit(s_busy, np.linspace(19.6e9, 20.4e9, 64), "cheerleader", nmax=200, precision="mixed")
+            ids = [srv.submit(st, freqs, "transformer", modes=modes, distance=d, precision=prec)
+                   for st, d in zip(stacks, dists)]
+            srv.wait(busy, timeout_ms=120000)
+            res = [srv.wait(i, timeout_ms=120000) for i in ids]
+            assert len({r["t_start"] for r in res}) == 1   # one solve
+            for d, r in zip(dists, res):
+                base.set_distance(d)
+                alone = transformer_alone(B, h, base, modes, freqs, prec)
+                assert rel(r["beta2"], alone) < tol
+        assert srv.stats("transformer")["batched"] >= 10
+    finally:
+        srv.close()
+        modes.close()
+        for s in stacks + [base, s_busy]:
+            s.close()
+        h.close()
+
+
+def test_server_keeps_its_stacks_alive(B):
+    """A stack or mode basis with requests still queued or running on a
+    server cannot be destroyed (BF_ERR_INVALID, the objects stay open); after
+    the server is closed they can."""
+    from bfgb300 import _lib, workloads as W
+    h = B.Handle(0)
+    st, c, _ = stack(B, h, 64, 3, 50)
+    pats, kt = W.lg_modes(c.X, c.Y, 4, 0.03, 0.15)
+    modes = B.SeedModes(c, ThreeDim=True, Mmax=4, Lmax=0, diskR=0.15, pattern_input=pats, kT_arr=kt, handle=h)
+    srv = B.Server(n_workers=1)
+    try:
+        a = srv.submit(st, np.linspace(19.6e9, 20.4e9, 64), "cheerleader", nmax=200, precision="mixed")
+        b = srv.submit(st, np.linspace(19.6e9, 20.4e9, 8), "transformer", modes=modes, distance=None,
+                       precision="mixed")
+        with pytest.raises(B.BFError) as e:
+            st.close()
+        assert e.value.code == _lib.BF_ERR_INVALID and st._s is not None
+        with pytest.raises(B.BFError):
+            modes.close()
+        srv.wait(a, timeout_ms=120000)
+        srv.wait(b, timeout_ms=120000)
+    finally:
+        srv.close()
+    modes.close()
+    st.close()
+    h.close()
