@@ -30,6 +30,7 @@ __all__ = [
     "CoordinateSystem", "SeedCoordinateSystem", "SetupBoundaries", "SeedSetupBoundaries",
     "wavelength", "propagator", "propagatorNoTilts", "propagatorMomentumSpace", "propagator1D",
     "cheerleader", "dancer", "Handle", "Stack", "boost_factor", "BFError", "SingularError", "transformer_group",
+    "autotune", "autotune_report",
     "Modes", "SeedModes", "axion_induced_modes", "field2modes", "modes2field",
     "calc_propagation_matrices", "transformer", "transformer_trace_back", "Server",
     "gauss_profile", "unnormalized_match", "transformer_coupled", "transformer_1d_batch",
@@ -509,6 +510,20 @@ def modes2field(mode_coeffs, coords, modes):
     modes.h.check(_lib.lib().bf_modes2field(modes.h.ptr, modes._m, _lib.ptr(c.view(np.float64)),
                                             _lib.ptr(out.view(np.float64))))
     return out.T[:, :, None]
+
+
+def autotune(enable=True):
+    """Switch the autotuner on or off (bf_autotune); returns the previous setting."""
+    return bool(_lib.lib().bf_autotune(1 if enable else 0))
+
+
+def autotune_report():
+    """The autotuner's decisions so far, one string per tuned shape."""
+    L = _lib.lib()
+    n = L.bf_autotune_report(None, 0)
+    buf = ctypes.create_string_buffer(n + 1)
+    L.bf_autotune_report(buf, n + 1)
+    return [l for l in buf.value.decode().split("\n") if l]
 
 
 def transformer_group(stacks, modes, freqs, prop=propagator, precision="mixed", want_boost=False):

@@ -117,6 +117,9 @@ _SIGS = {
     "bf_transformer": (_c_int, [_vp, _vp, _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                 _p_dbl, _p_dbl, _p_dbl]),
     "bf_test_tc_withhold_loads": (_c_int, [_c_int]),
+    "bf_test_force_fused_variant": (_c_int, [_c_int]),
+    "bf_autotune": (_c_int, [_c_int]),
+    "bf_autotune_report": (_c_int, [ctypes.c_char_p, _c_int]),
     "bf_transformer_group": (_c_int, [_vp, _c_int, ctypes.POINTER(_vp), _vp, _c_int, _p_dbl, _c_int, _c_int, _p_dbl,
                                       _p_dbl]),
 }

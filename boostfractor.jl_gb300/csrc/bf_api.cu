@@ -20,6 +20,10 @@
 #include <cmath>
 #include <functional>
 #include <algorithm>
+#include <cstring>
+#include <atomic>
+#include <map>
+#include <array>
 #include <cstdio>
 #include <memory>
 #include <mutex>
@@ -931,6 +935,131 @@ static void prof_mark(bf_handle* h, int i) {
 // coefficients, initial and additive boxes) is cached per stack under
 // `key`; the phasor/tilt tables are cached per frequency batch; no device
 // memory is allocated once the workspace has grown to the request's size.
+// ---------------------------------------------------------------------------
+// Autotuner.  The fused stage kernel has variants that give the same results
+// bit for bit (FusedVariant: joint or separate slot propagation, 256 or 512
+// threads); which is fastest depends on the grid, the box, the precision and
+// the frequency batch.  The first solve of a shape times every valid variant
+// on its largest fused stage, three launches each on scratch copies of the
+// state and the exit accumulators, and keeps the fastest for that shape on
+// that device.  Solves on a stream being captured, and any solve while
+// tuning is switched off (bf_autotune(0)), use the rule's choice.
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+std::map<std::array<long long, 6>, int> g_fused_tuned;   // (device, N, nbx, nby, fp64, nf) -> variant
+std::vector<std::string> g_tune_log;
+std::atomic<int> g_autotune{1};
+std::atomic<int> g_force_variant{-1};
+}  // namespace
+
+bool bf_autotune_enabled() { return g_autotune.load() != 0; }
+
+void bf_tune_log(const std::string& line) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  if (g_tune_log.size() < 4096) g_tune_log.push_back(line);
+}
+
+extern "C" int bf_autotune(int enable) { return g_autotune.exchange(enable ? 1 : 0); }
+
+extern "C" int bf_autotune_report(char* out, int cap) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  std::string all;
+  for (const auto& l : g_tune_log) all += l + "\n";
+  if (out && cap > 0) {
+    const size_t n = std::min(all.size(), (size_t)cap - 1);
+    std::memcpy(out, all.data(), n);
+    out[n] = 0;
+  }
+  return (int)all.size();
+}
+
+extern "C" int bf_test_force_fused_variant(int v) { return g_force_variant.exchange(v); }
+
+template <typename C>
+static int fused_autotune(bf_handle* h, const Workspace& w, const bf::FusedArgs<C>& a, int N, bool fp64,
+                          cudaStream_t st, int* out) {
+  *out = bf::kFusedRule;
+  if (g_force_variant.load() >= 0) {
+    *out = g_force_variant.load();
+    return BF_OK;
+  }
+  if (!g_autotune.load()) return BF_OK;
+  const std::array<long long, 6> key = {h->device, N, a.nbx, a.nby, (long long)fp64, a.nfreq};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_fused_tuned.find(key);
+    if (it != g_fused_tuned.end()) {
+      *out = it->second;
+      return BF_OK;
+    }
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return BF_OK;
+  std::vector<int> cand = bf::fused_variants(N, a.nbx, a.nby, fp64);
+  cand.erase(cand.begin());   // the rule's choice is one of the explicit variants
+  size_t kbest = (size_t)-1, lbest = 0;
+  for (size_t k = 0; k < w.stage_len.size(); ++k)
+    if ((N < 64 || !bf::split_stage((int)w.stage_len[k], a.nfreq)) && w.stage_len[k] > lbest) {
+      lbest = w.stage_len[k];
+      kbest = k;
+    }
+  int best = bf::kFusedRule;
+  std::string what;
+  if (cand.size() > 1 && kbest != (size_t)-1) {
+    const size_t plane = (size_t)a.nbx * a.nby;
+    DBuf st2, ex2;
+    CKS(st2.alloc(h, sizeof(C) * (size_t)a.nfreq * a.nslots * plane));
+    CKS(ex2.alloc(h, sizeof(double2) * (size_t)std::max(w.nexit, 1) * a.nfreq * plane));
+    CK(cudaMemcpyAsync(st2.p, a.state, sizeof(C) * (size_t)a.nfreq * a.nslots * plane, cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemsetAsync(ex2.p, 0, sizeof(double2) * (size_t)std::max(w.nexit, 1) * a.nfreq * plane, st));
+    bf::FusedArgs<C> t = a;
+    t.state = st2.as<C>();
+    t.exitacc = ex2.as<double2>();
+    t.steps = w.steps.as<StepDesc>() + w.stage_off[kbest];
+    t.mg = nullptr;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float tbest = 1e30f;
+    for (int v : cand) {
+      t.variant = v;
+      float tv = 1e30f;
+      for (int rep = 0; rep < 4; ++rep) {   // the first launch warms up, the best of three counts
+        cudaEventRecord(e0, st);
+        const int e = fp64 ? bf::launch_fused_stage_d(N, *reinterpret_cast<bf::FusedArgs<double2>*>(&t), (int)lbest, st)
+                           : bf::launch_fused_stage_f(N, *reinterpret_cast<bf::FusedArgs<float2>*>(&t), (int)lbest, st);
+        cudaEventRecord(e1, st);
+        if (e || cudaEventSynchronize(e1) != cudaSuccess) {
+          tv = 1e30f;
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tv = std::min(tv, ms);
+      }
+      what += " v" + std::to_string(v) + "=" + (tv < 1e29f ? std::to_string(tv) : std::string("fail"));
+      if (tv < tbest) {
+        tbest = tv;
+        best = v;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_fused_tuned[key] = best;
+  }
+  bf_tune_log("fused N=" + std::to_string(N) + " box=" + std::to_string(a.nbx) + "x" + std::to_string(a.nby) +
+              (fp64 ? " c128" : " c64") + " nf=" + std::to_string(a.nfreq) + " -> variant " + std::to_string(best) +
+              " (ms per launch of " + std::to_string(lbest) + " steps:" + what + ")");
+  *out = best;
+  return BF_OK;
+}
+
 template <typename C>
 static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
                      const std::function<void(Plan&)>& make_plan, bool fp64, int nf,
@@ -1063,6 +1192,12 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
       a.mg = w.mg.as<C>();
     }
   }
+  a.variant = bf::kFusedRule;
+  {
+    int v = bf::kFusedRule;
+    CKS(fused_autotune<C>(h, w, a, N, fp64, st, &v));
+    a.variant = v;
+  }
   prof_mark(h, 1);
   const unsigned long long l1 = bf::launch_count();
   auto run_stages = [&]() -> int {
@@ -1085,7 +1220,7 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
     const void* ptrs[] = {a.state, a.phasor, a.tilt, a.tilt_idx, a.mask, a.coefs, a.exitacc, a.addbuf,
                           a.err, w.steps.p, a.mg};
     const long long ints[] = {nf, a.nbx, a.nby, a.nslots, a.ntab, a.fold, a.ntilt, N, (long long)fp64,
-                              (long long)w.stage_off.size(), h->device};
+                              (long long)w.stage_off.size(), h->device, a.variant};
     gkey.append(reinterpret_cast<const char*>(ptrs), sizeof(ptrs));
     gkey.append(reinterpret_cast<const char*>(ints), sizeof(ints));
     gkey.append(reinterpret_cast<const char*>(w.stage_off.data()), sizeof(size_t) * w.stage_off.size());

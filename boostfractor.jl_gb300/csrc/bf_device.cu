@@ -19,6 +19,7 @@
 #include <stdio.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "bf_common.cuh"
 #include "bf_device.cuh"
@@ -745,16 +746,57 @@ static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem,
 // 5/16 of the grid, the disk of radius 0.15 m in the reference's 1 m window.
 template <int N> constexpr int pruned_slots() { return (5 * Team<N>::RR + 15) / 16; }
 
+// Shape of one fused-stage launch: shared memory of the single and doubled
+// (joint) row tiles and whether the rule takes the joint path.
+struct FusedShape {
+  size_t smem, smem_j, smem512;
+  bool joint_rule, joint_fits, wide_fits;
+};
+template <int N>
+static FusedShape fused_shape(int nby, size_t csz) {
+  FusedShape f;
+  f.smem = fused_smem_for<N>(nby, csz, 1);
+  f.smem_j = fused_smem_for<N>(nby, csz, 2);
+  f.smem512 = fused_smem_for<N>(nby, csz, 1, 512);
+  // the joint path when the doubled row tile keeps as many CTAs per SM
+  const int ctas = (csz == 8 && N <= 128) ? 2 : 1;
+  f.joint_fits = f.smem_j <= kMaxSmem;
+  f.joint_rule = f.joint_fits && (size_t)ctas * (f.smem_j + kSmemReservedPerCta) <= kSmemPerSM &&
+                 (size_t)ctas * (f.smem + kSmemReservedPerCta) <= kSmemPerSM;
+  f.wide_fits = csz == 8 && N == 256 && f.smem512 <= kMaxSmem;
+  return f;
+}
+
+template <int N>
+static std::vector<int> fused_variants_t(int nby, bool fp64) {
+  const FusedShape f = fused_shape<N>(nby, fp64 ? 16 : 8);
+  std::vector<int> v = {kFusedRule};
+  if (f.smem > kMaxSmem) return v;
+  v.push_back(kFusedSeparate);
+  if (f.joint_fits) v.push_back(kFusedJoint);
+  if (f.wide_fits) v.push_back(kFusedWide);
+  return v;
+}
+
+std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64) {
+  (void)nbx;
+  switch (N) {
+    case 8: return fused_variants_t<8>(nby, fp64);
+    case 16: return fused_variants_t<16>(nby, fp64);
+    case 32: return fused_variants_t<32>(nby, fp64);
+    case 64: return fused_variants_t<64>(nby, fp64);
+    case 128: return fused_variants_t<128>(nby, fp64);
+    case 256: return fused_variants_t<256>(nby, fp64);
+    default: return {kFusedRule};
+  }
+}
+
 template <typename R, int N>
 static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_t st) {
   const size_t csz = sizeof(cplx_t<R>);
-  const size_t smem = fused_smem_for<N>(a.nby, csz, 1);
+  const FusedShape sh = fused_shape<N>(a.nby, csz);
+  const size_t smem = sh.smem, smem_j = sh.smem_j;
   if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
-  // the joint path when the doubled row tile keeps as many CTAs per SM
-  const int ctas = (sizeof(R) == 4 && N <= 128) ? 2 : 1;
-  const size_t smem_j = fused_smem_for<N>(a.nby, csz, 2);
-  const bool joint = smem_j <= kMaxSmem && (size_t)ctas * (smem_j + kSmemReservedPerCta) <= kSmemPerSM &&
-                     (size_t)ctas * (smem + kSmemReservedPerCta) <= kSmemPerSM;
   constexpr int G = Team<N>::G, RR = Team<N>::RR;
   const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
   if (a.mg && split_stage(nsteps, a.nfreq) && N >= 64) {
@@ -762,15 +804,27 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
       if (rv <= pruned_slots<N>()) return launch_split<R, N, pruned_slots<N>()>(a, nsteps, st);
     return launch_split<R, N, RR>(a, nsteps, st);
   }
+  // the variant: the rule's choice, or one picked by the autotuner (an
+  // invalid choice falls back to the rule)
+  bool joint = sh.joint_rule, wide = sh.wide_fits && !sh.joint_rule;
+  if (a.variant == kFusedSeparate) {
+    joint = false;
+    wide = false;
+  } else if (a.variant == kFusedJoint && sh.joint_fits) {
+    joint = true;
+    wide = false;
+  } else if (a.variant == kFusedWide && sh.wide_fits) {
+    joint = false;
+    wide = true;
+  }
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
   if constexpr (sizeof(R) == 4 && N == 256) {
     // one CTA per SM (the 256-point row tile): 512 threads (32 teams, at most
     // 128 registers each) when the team scratch still fits beside the tile
-    const size_t smem512 = fused_smem_for<N>(a.nby, csz, 1, 512);
-    if (!joint && smem512 <= kMaxSmem)
-      return rv <= pruned_slots<N>() ? launch_fused_v<R, N, false, pruned_slots<N>(), 512>(a, grid, smem512, st)
-                                     : launch_fused_v<R, N, false, Team<N>::RR, 512>(a, grid, smem512, st);
+    if (wide)
+      return rv <= pruned_slots<N>() ? launch_fused_v<R, N, false, pruned_slots<N>(), 512>(a, grid, sh.smem512, st)
+                                     : launch_fused_v<R, N, false, Team<N>::RR, 512>(a, grid, sh.smem512, st);
   }
   if constexpr ((sizeof(R) == 4 && N >= 64) || (sizeof(R) == 8 && (N == 64 || N == 128))) {
     if (rv <= pruned_slots<N>())

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace bf {
 
 // One step of a bounce stage: two field slots A (left) and B (right) that meet
@@ -44,7 +46,20 @@ struct FusedArgs {
   const StepDesc* steps;          // this stage
   int* err;                       // set to 1 if a bounded wait gave up
   C* mg;                          // row tiles of the split-phase path [step][f][2][nby][N+2], or null
+  int variant;                    // host side: fused-kernel variant (FusedVariant), 0 = by rule
 };
+
+// Variants of the fused stage kernel for stages that do not take the
+// split-phase path.  All run the same per-pixel arithmetic in the same order,
+// so they give the same results bit for bit; only their speed differs.
+enum FusedVariant {
+  kFusedRule = 0,       // joint steps when the doubled row tile keeps the CTAs per SM; 512 threads at N = 256 c64
+  kFusedSeparate = 1,   // slots propagated one after the other, 256 threads
+  kFusedJoint = 2,      // joint steps (both slots' row tiles in shared memory), 256 threads
+  kFusedWide = 3,       // slots one after the other, 512 threads (complex64, N = 256)
+};
+// The variants valid for a stage of this shape (kFusedRule first).
+std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64);
 
 // Launch the fused stage kernel (templated on the grid size N and the field
 // precision).  Returns a cudaError_t.

@@ -169,6 +169,9 @@ void bf_pgrid_shape(const bf_pgrid* g, int* nf, int* nd, int* nm, bf_stack** sta
 // Serving-engine requests queued or running on a mode basis (delta +1 / -1);
 // bf_modes_destroy refuses while any are.
 void bf_modes_server_use(bf_modes* m, int delta);
+// Autotuner switch (bf_autotune) and its log of decisions (bf_autotune_report).
+bool bf_autotune_enabled();
+void bf_tune_log(const std::string& line);
 size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, int prop_kind, int precision);
 
 namespace bfhost {

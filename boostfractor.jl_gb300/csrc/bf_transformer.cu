@@ -19,6 +19,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -346,7 +347,8 @@ __global__ void k_rowsum(double* g, const double* Ad, int K) {
 // scatter), and complex64 copies of c0, kz0, k0^2 and dz (col).
 struct ColTC {
   float2 c0, kz0, k0sq;
-  float dz, pad;
+  float dz;
+  int ef;   // row of the column's (permittivity, frequency) in DKZ
 };
 __global__ void k_build_c0(double2* C0, ColTC* col, const double* freqs, int nf, int ncol, int nd,
                            const double2* eps, const RegionT* regs, const int* par_regions, const int* par_eps,
@@ -366,7 +368,7 @@ __global__ void k_build_c0(double2* C0, ColTC* col, const double* freqs, int nf,
   q.kz0 = make_float2((float)kz0.x, (float)kz0.y);
   q.k0sq = make_float2((float)k0sq.x, (float)k0sq.y);
   q.dz = (float)dz;
-  q.pad = 0.f;
+  q.ef = par_eps[p] * nf + f;
   col[c] = q;
 }
 
@@ -382,32 +384,49 @@ __device__ __forceinline__ float2 fsqrt_c(float x, float y) {
 }
 
 // exp(re + i im) - 1 for a modest phase |im| (a few radians), all in FP32:
-// cos t - 1 = -2 sin^2(t/2) and expm1 keep it accurate relative to its own
-// magnitude.
+// with s, c = sin, cos(im/2): cos im - 1 = -2 s^2 and sin im = 2 s c, and
+// expm1, keep it accurate relative to its own magnitude (one sincosf; no
+// expm1 for a lossless phase, re = 0).
 __device__ __forceinline__ float2 cexpm1_ff(float re, float im) {
-  const float h = sinf(0.5f * im), sn = sinf(im);
-  const float cm1 = -2.0f * h * h;
-  const float em = expm1f(re);
+  float h, ch;
+  sincosf(0.5f * im, &h, &ch);
+  const float cm1 = -2.0f * h * h, sn = 2.0f * h * ch;
+  const float em = re == 0.0f ? 0.0f : expm1f(re);
   return make_float2(fmaf(em, 1.0f + cm1, cm1), (em + 1.0f) * sn);
 }
 
+// DKZ[e][f][o] = kz - kz0 = -kt^2 / (kz + kz0) in FP32 for the distinct
+// permittivities e of the k-space regions, once per (frequency, orbit): it has
+// no cancellation, so FP32 carries it to ~1e-7 of its own size.  KT2[o] =
+// kx^2 + ky^2 at the orbit representative.
+__global__ void k_build_dkz(float2* DKZ, const float* KT2, int K, const double* freqs, int nf, const double2* eps) {
+  const int o = blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= K) return;
+  const int e = blockIdx.z;
+  const float kt2 = KT2[o];
+  for (int f = blockIdx.y; f < nf; f += gridDim.y) {
+    const double2 k0 = k0_c(kC / freqs[f], eps[e].x, eps[e].y);
+    const double2 k0sq = make_double2(k0.x * k0.x - k0.y * k0.y, k0.x * k0.y + k0.y * k0.x);
+    const double2 kz0d = dsqrt_c(k0sq.x, k0sq.y);
+    const float2 kz0 = make_float2((float)kz0d.x, (float)kz0d.y);
+    const float2 kz = fsqrt_c((float)k0sq.x - kt2, (float)k0sq.y);
+    const float2 den = make_float2(kz.x + kz0.x, kz.y + kz0.y);
+    const float dn = den.x * den.x + den.y * den.y;
+    DKZ[((size_t)e * nf + f) * K + o] = make_float2(-kt2 * den.x / dn, kt2 * den.y / dn);   // -kt2 / den
+  }
+}
+
 // B^T of the k-space class: rows 2c, 2c + 1 = Re, Im of D[o][c] - c0[c] =
-// c0 (exp(-i (kz - kz0) dz) - 1) as TF32 pairs [2 ncol][Kp], zero for o >= K.
-// kz - kz0 = -kt^2 / (kz + kz0) has no cancellation, so FP32 carries it to
-// ~1e-7 of its own size; the phase (kz - kz0) dz is a few radians at most.
-// KT2[o] = kx^2 + ky^2 at the orbit representative.
-__global__ void k_build_d_tc(float* Bh, float* Bl, const float* KT2, const ColTC* col, int K, int Kp, int ncol) {
+// c0 (exp(-i (kz - kz0) dz) - 1) as TF32 pairs [2 ncol][Kp], zero for o >= K;
+// kz - kz0 from DKZ, the phase (kz - kz0) dz is a few radians at most.
+__global__ void k_build_d_tc(float* Bh, float* Bl, const float2* DKZ, const ColTC* col, int K, int Kp, int ncol) {
   const int o = blockIdx.x * blockDim.x + threadIdx.x;
   if (o >= Kp) return;
-  const float kt2 = o < K ? KT2[o] : 0.f;
   for (int c = blockIdx.y; c < ncol; c += gridDim.y) {
     float2 v = make_float2(0.f, 0.f);
     if (o < K) {
       const ColTC q = col[c];
-      const float2 kz = fsqrt_c(q.k0sq.x - kt2, q.k0sq.y);
-      const float2 den = make_float2(kz.x + q.kz0.x, kz.y + q.kz0.y);
-      const float dn = den.x * den.x + den.y * den.y;
-      const float2 dkz = make_float2(-kt2 * den.x / dn, kt2 * den.y / dn);   // -kt2 / den
+      const float2 dkz = DKZ[(size_t)q.ef * K + o];
       const float2 m1 = cexpm1_ff(dkz.y * q.dz, -dkz.x * q.dz);
       v = make_float2(q.c0.x * m1.x - q.c0.y * m1.y, q.c0.x * m1.y + q.c0.y * m1.x);
     }
@@ -682,47 +701,54 @@ __global__ void k_copy_modes(C* out, const double2* pat, int nm, int npix, int r
 // The pivot magnitudes and the pivot reciprocal are computed in the matrix's
 // own precision: FP32 for complex64 (a warp-wide FP64 instruction costs the
 // same with one lane active, at 1/64 of the FP32 rate), FP64 for complex128.
+// jl (nullable): invert only the regions jl[0 .. njl) of frequencies f0, f0 + 1, ...
+// A warp holds 32 / NM matrices, one per segment of NM lanes (shuffles of
+// width NM), so an 8 x 8 inverse does not leave 24 of 32 lanes idle.
 template <typename C, int NM>
 __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd, int j0, int nm, int nmat,
-                                                     int* sing) {
+                                                     int* sing, int f0 = 0, const int* jl = nullptr, int njl = 0) {
   using R = decltype(C().x);
   constexpr unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const int idx = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (idx >= nmat) return;   // the whole warp leaves together
-  const int nj = nd - j0;
-  const int f = idx / nj, j = j0 + idx % nj;
+  constexpr int SEG = 32 / NM;
+  const int lane = threadIdx.x & 31, sl = lane % NM;
+  const int first = (blockIdx.x * 8 + (threadIdx.x >> 5)) * SEG;
+  if (first >= nmat) return;   // the whole warp leaves together
+  const int idx = first + lane / NM;
+  const bool valid = idx < nmat;
+  const int nj = jl ? njl : nd - j0;
+  const int q = valid ? idx : first;
+  const int f = f0 + q / nj, j = jl ? jl[q % nj] : j0 + q % nj;
   const size_t off = (((size_t)f * nd + j) * nm) * nm;
   C a[NM], b[NM];
 #pragma unroll
   for (int c = 0; c < NM; ++c) {
-    if (lane < nm && c < nm) a[c] = P[off + (size_t)lane * nm + c];
-    else a[c] = bf::mk(R(lane == c ? 1 : 0), R(0));
-    b[c] = bf::mk(R(lane == c ? 1 : 0), R(0));
+    if (sl < nm && c < nm) a[c] = P[off + (size_t)sl * nm + c];
+    else a[c] = bf::mk(R(sl == c ? 1 : 0), R(0));
+    b[c] = bf::mk(R(sl == c ? 1 : 0), R(0));
   }
 #pragma unroll
   for (int c = 0; c < NM; ++c) {
-    R v = (lane >= c && lane < NM) ? a[c].x * a[c].x + a[c].y * a[c].y : R(-1);
-    int p = lane;
+    R v = sl >= c ? a[c].x * a[c].x + a[c].y * a[c].y : R(-1);
+    int p = sl;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const R vo = __shfl_xor_sync(FULL, v, o);
-      const int po = __shfl_xor_sync(FULL, p, o);
+    for (int o = NM / 2; o > 0; o >>= 1) {
+      const R vo = __shfl_xor_sync(FULL, v, o, NM);
+      const int po = __shfl_xor_sync(FULL, p, o, NM);
       if (vo > v || (vo == v && po < p)) {
         v = vo;
         p = po;
       }
     }
-    const int src = lane == c ? p : (lane == p ? c : lane);
+    const int src = sl == c ? p : (sl == p ? c : sl);
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
-      a[k].x = __shfl_sync(FULL, a[k].x, src);
-      a[k].y = __shfl_sync(FULL, a[k].y, src);
-      b[k].x = __shfl_sync(FULL, b[k].x, src);
-      b[k].y = __shfl_sync(FULL, b[k].y, src);
+      a[k].x = __shfl_sync(FULL, a[k].x, src, NM);
+      a[k].y = __shfl_sync(FULL, a[k].y, src, NM);
+      b[k].x = __shfl_sync(FULL, b[k].x, src, NM);
+      b[k].y = __shfl_sync(FULL, b[k].y, src, NM);
     }
-    if (lane == c) {
-      if (a[c].x == R(0) && a[c].y == R(0)) atomicMin(sing, f);   // exactly singular (LAPACK info > 0)
+    if (sl == c) {
+      if (valid && a[c].x == R(0) && a[c].y == R(0)) atomicMin(sing, f);   // exactly singular (LAPACK info > 0)
       const R d = a[c].x * a[c].x + a[c].y * a[c].y;
       const C inv = bf::mk(a[c].x / d, -a[c].y / d);
 #pragma unroll
@@ -735,30 +761,31 @@ __global__ void __launch_bounds__(256) k_invert_warp(const C* P, C* Pinv, int nd
 #pragma unroll
     for (int k = 0; k < NM; ++k) {
       C pa, pb;
-      pa.x = __shfl_sync(FULL, a[k].x, c);
-      pa.y = __shfl_sync(FULL, a[k].y, c);
-      pb.x = __shfl_sync(FULL, b[k].x, c);
-      pb.y = __shfl_sync(FULL, b[k].y, c);
-      if (lane != c) {
+      pa.x = __shfl_sync(FULL, a[k].x, c, NM);
+      pa.y = __shfl_sync(FULL, a[k].y, c, NM);
+      pb.x = __shfl_sync(FULL, b[k].x, c, NM);
+      pb.y = __shfl_sync(FULL, b[k].y, c, NM);
+      if (sl != c) {
         a[k] = bf::csub(a[k], bf::cmul(fct, pa));
         b[k] = bf::csub(b[k], bf::cmul(fct, pb));
       }
     }
   }
-  if (lane < nm)
+  if (valid && sl < nm)
 #pragma unroll
     for (int c = 0; c < NM; ++c)
-      if (c < nm) Pinv[off + (size_t)lane * nm + c] = b[c];
+      if (c < nm) Pinv[off + (size_t)sl * nm + c] = b[c];
 }
 
 // ---- batched inversion: Pinv[f][j] = inv(P[f][j]), j in [j0, nd) -----------
 template <typename C>
-__global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int j0, int nm, int* sing) {
+__global__ void __launch_bounds__(256) k_invert(const C* P, C* Pinv, int nd, int j0, int nm, int* sing, int f0 = 0,
+                                                const int* jl = nullptr) {
   extern __shared__ __align__(16) unsigned char sm[];
   C* W = reinterpret_cast<C*>(sm);
   double* red_v = reinterpret_cast<double*>(W + 2 * nm * nm);
   int* red_i = reinterpret_cast<int*>(red_v + 256);
-  const int f = blockIdx.y, j = j0 + blockIdx.x;
+  const int f = f0 + blockIdx.y, j = jl ? jl[blockIdx.x] : j0 + blockIdx.x;
   const size_t off = (((size_t)f * nd + j) * nm) * nm;
   C* M = Pinv + off;
   for (int e = threadIdx.x; e < nm * nm; e += blockDim.x) M[e] = P[off + e];
@@ -790,7 +817,8 @@ __device__ __forceinline__ float2 pick4(const float2 (&v)[4], int s) {
 
 template <int NB>
 __global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2* P, float2* Pinv, int nd, int j0,
-                                                                  int nm, int* sing) {
+                                                                  int nm, int* sing, int f0 = 0,
+                                                                  const int* jl = nullptr) {
   constexpr int NBB = NB / 4, NT = NBB * NBB, RPL = NB / 32;
   constexpr unsigned FULL = 0xffffffffu;
   __shared__ float2 colv[2][NB], rowv[NB];
@@ -799,7 +827,7 @@ __global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2
   __shared__ int psh;
   __shared__ float2 outs[NB * NB];
   const int tid = threadIdx.x, br = tid / NBB, bc = tid % NBB, lane = tid & 31;
-  const int f = blockIdx.y, j = j0 + blockIdx.x;
+  const int f = f0 + blockIdx.y, j = jl ? jl[blockIdx.x] : j0 + blockIdx.x;
   const size_t off = (((size_t)f * nd + j) * nm) * nm;
   float2 A[4][4];
 #pragma unroll
@@ -905,6 +933,21 @@ __global__ void __launch_bounds__((NB / 4) * (NB / 4)) k_invert_reg(const float2
     }
   __syncthreads();
   for (int e = tid; e < nm * nm; e += NT) Pinv[off + e] = outs[e];
+}
+
+// Group solves: the inverses of regions jl[0 .. njl) of request 0 (frequencies
+// [0, nf)) copied to requests 1 .. nreq-1, whose matrices there are the same.
+template <typename C>
+__global__ void k_copy_inverses(C* Pinv, int nd, int nm, int nf, int nreq, const int* jl, int njl) {
+  const size_t n2 = (size_t)nm * nm;
+  const size_t per = (size_t)nf * njl * n2;   // entries of request 0 to copy
+  const size_t total = per * (nreq - 1);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = 1 + i / per, q = i % per;
+    const size_t e = q % n2, fj = q / n2;
+    const int f = (int)(fj / njl), j = jl[fj % njl];
+    Pinv[(((r * nf + f) * nd) + j) * n2 + e] = Pinv[(((size_t)f * nd) + j) * n2 + e];
+  }
 }
 
 // ---- the chain: one CTA per frequency ---------------------------------------
@@ -1323,6 +1366,113 @@ __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22
   }
 }
 
+// The boundary solve of k_final_solve for nm <= NM (8 or 16), one segment of
+// NM lanes per frequency (32 / NM frequencies per warp): lane r holds row r of
+// [T22 | axion_beam | T21 reflect] in registers, the pivot search is a shuffle
+// argmax (largest |a|^2, lowest row on ties), the pivot row is broadcast by
+// shuffles.  Every entry goes through the operations of k_final_solve in the
+// same order (LU with partial pivoting, then back substitution); only the
+// CTA-wide reductions and barriers are gone.
+template <int NM>
+__global__ void __launch_bounds__(256) k_final_solve_warp(const double2* T21g, const double2* T22g,
+                                                          const double2* axg, const double2* reflect, int nm,
+                                                          double2* boost, double2* refl, double* beta2, int* sing,
+                                                          int nf) {
+  constexpr unsigned FULL = 0xffffffffu;
+  constexpr int W = NM + 2, SEG = 32 / NM;
+  const int lane = threadIdx.x & 31, sl = lane % NM;
+  const int first = (blockIdx.x * 8 + (threadIdx.x >> 5)) * SEG;
+  if (first >= nf) return;   // the whole warp leaves together
+  const int fi = first + lane / NM;
+  const bool valid = fi < nf;
+  const int f = valid ? fi : first;
+  const double2* T21 = T21g + (size_t)f * nm * nm;
+  const double2* T22 = T22g + (size_t)f * nm * nm;
+  const bool row = sl < nm;
+  double2 a[W];
+#pragma unroll
+  for (int k = 0; k < W; ++k) a[k] = make_double2(0.0, 0.0);
+  if (row) {
+#pragma unroll
+    for (int k = 0; k < NM; ++k)
+      if (k < nm) a[k] = T22[sl * nm + k];
+    a[NM] = axg[(size_t)f * nm + sl];
+    double2 acc = make_double2(0.0, 0.0);
+    if (reflect)
+      for (int k = 0; k < nm; ++k) acc = bf::cadd(acc, bf::cmul(T21[sl * nm + k], reflect[k]));
+    a[NM + 1] = acc;
+  }
+  auto bcast = [&](double2 v, int src) {
+    return make_double2(__shfl_sync(FULL, v.x, src, NM), __shfl_sync(FULL, v.y, src, NM));
+  };
+#pragma unroll
+  for (int c = 0; c < NM; ++c) {
+    if (c >= nm) break;
+    double v = (row && sl >= c) ? a[c].x * a[c].x + a[c].y * a[c].y : -1.0;
+    int p = (row && sl >= c) ? sl : NM;
+#pragma unroll
+    for (int o = NM / 2; o > 0; o >>= 1) {
+      const double vo = __shfl_xor_sync(FULL, v, o, NM);
+      const int po = __shfl_xor_sync(FULL, p, o, NM);
+      if (vo > v || (vo == v && po < p)) { v = vo; p = po; }
+    }
+    if (p >= nm) p = c;
+    // swap rows c and p
+    const int src = sl == c ? p : (sl == p ? c : sl);
+#pragma unroll
+    for (int k = 0; k < W; ++k) a[k] = bcast(a[k], src);
+    const double2 piv = bcast(a[c], c);
+    if (valid && sl == 0 && piv.x == 0.0 && piv.y == 0.0) atomicMin(sing, f);   // T22 exactly singular
+    const double d = piv.x * piv.x + piv.y * piv.y;
+    const double2 l = a[c];
+    const double2 fac = make_double2((l.x * piv.x + l.y * piv.y) / d, (l.y * piv.x - l.x * piv.y) / d);
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      if (k <= c || (k >= nm && k < NM)) continue;
+      const double2 pk = bcast(a[k], c);
+      if (row && sl > c) a[k] = bf::csub(a[k], bf::cmul(fac, pk));
+    }
+    if (row && sl > c) a[c] = make_double2(0.0, 0.0);
+  }
+  // back substitution for both right-hand sides, rows nm-1 .. 0
+  double2 x0[NM], x1[NM];
+#pragma unroll
+  for (int r = NM - 1; r >= 0; --r) {
+    if (r >= nm) {
+      x0[r] = x1[r] = make_double2(0.0, 0.0);
+      continue;
+    }
+    double2 acc0 = a[NM], acc1 = a[NM + 1];
+#pragma unroll
+    for (int k = r + 1; k < NM; ++k) {
+      if (k >= nm) break;
+      acc0 = bf::csub(acc0, bf::cmul(a[k], x0[k]));
+      acc1 = bf::csub(acc1, bf::cmul(a[k], x1[k]));
+    }
+    const double2 pv = a[r];
+    const double dd = pv.x * pv.x + pv.y * pv.y;
+    const double2 s0 = make_double2((acc0.x * pv.x + acc0.y * pv.y) / dd, (acc0.y * pv.x - acc0.x * pv.y) / dd);
+    const double2 s1 = make_double2((acc1.x * pv.x + acc1.y * pv.y) / dd, (acc1.y * pv.x - acc1.x * pv.y) / dd);
+    x0[r] = bcast(s0, r);
+    x1[r] = bcast(s1, r);
+  }
+  if (valid && row) {
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      if (m == sl) {
+        boost[(size_t)f * nm + m] = make_double2(-x0[m].x, -x0[m].y);
+        if (refl) refl[(size_t)f * nm + m] = make_double2(-x1[m].x, -x1[m].y);
+      }
+  }
+  if (valid && sl == 0 && beta2) {
+    double s = 0.0;
+#pragma unroll
+    for (int m = 0; m < NM; ++m)
+      if (m < nm) s += x0[m].x * x0[m].x + x0[m].y * x0[m].y;
+    beta2[f] = s;
+  }
+}
+
 // axion_induced_modes / field2modes: c_m = sum conj(Psi_m) B_hat
 __global__ void k_project(double2* out, const double2* pat, const double2* Bn, int nm, int npix) {
   const int m = blockIdx.x;
@@ -1692,11 +1842,82 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
 // (FP32) = A [Mp][Kp] times the 2 ncol real rows of B^T [2 ncol][Kp] (TF32
 // hi/lo pairs), K cut into slices only when the output tiles alone would
 // leave SMs idle; k_scatter_herm_tc sums the slices in FP64.
+// The K slicing of the tensor-core GEMM, per (device, M, N, K): the
+// heuristic's count, or, with the autotuner on, the fastest of 1, 2, 4, 8
+// slices timed once on the first call's operands (the output of the trials is
+// scratch; every count gives the same sums up to FP32 rounding of the slices).
+static std::mutex g_split_mu;
+static std::map<std::array<long long, 4>, int> g_split_tuned;
+
+static int tc_pick_splits(bf_handle* h, const float* Ah, const float* Al, int Mp, int Kp, const float* Bh,
+                          const float* Bl, int nrows_b, int* d_err, int* splits) {
+  cudaStream_t st = h->stream();
+  *splits = bf::tc_gemm_splits(Mp, nrows_b, Kp);
+  if (!bf_autotune_enabled()) return BF_OK;
+  const std::array<long long, 4> key = {h->device, Mp, nrows_b, Kp};
+  {
+    std::lock_guard<std::mutex> lock(g_split_mu);
+    auto it = g_split_tuned.find(key);
+    if (it != g_split_tuned.end()) {
+      *splits = it->second;
+      return BF_OK;
+    }
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  TCK(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return BF_OK;
+  const int ktiles = Kp / 32;
+  std::vector<int> cand;
+  for (int sp : {1, 2, 4, 8})
+    if (sp == 1 || ktiles / sp >= 8) cand.push_back(sp);
+  int best = *splits;
+  std::string what;
+  if (cand.size() > 1) {
+    DBuf tmp;
+    TCKS(tmp.alloc(h, sizeof(float) * (size_t)cand.back() * nrows_b * Mp));
+    cudaEvent_t e0, e1;
+    TCK(cudaEventCreate(&e0));
+    TCK(cudaEventCreate(&e1));
+    float tbest = 1e30f;
+    for (int sp : cand) {
+      float tv = 1e30f;
+      for (int rep = 0; rep < 3; ++rep) {   // the first run warms up
+        cudaEventRecord(e0, st);
+        const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, sp, tmp.as<float>(), d_err, st);
+        cudaEventRecord(e1, st);
+        if (e || cudaEventSynchronize(e1) != cudaSuccess) {
+          tv = 1e30f;
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tv = std::min(tv, ms);
+      }
+      what += " " + std::to_string(sp) + ":" + std::to_string(tv);
+      if (tv < tbest) {
+        tbest = tv;
+        best = sp;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGetLastError();
+  }
+  {
+    std::lock_guard<std::mutex> lock(g_split_mu);
+    g_split_tuned[key] = best;
+  }
+  bf_tune_log("tc_gemm M=" + std::to_string(Mp) + " N=" + std::to_string(nrows_b) + " K=" + std::to_string(Kp) +
+              " -> " + std::to_string(best) + " K slices (ms per launch by slices:" + what + ")");
+  *splits = best;
+  return BF_OK;
+}
+
 static int tc_class_gemm(bf_handle* h, const float* Ah, const float* Al, int Mp, int Kp, const float* Bh,
                          const float* Bl, int nrows_b, DBuf& out, int* splits, int* d_err) {
   cudaStream_t st = h->stream();
   g_tf_gemm_flops += 3.0 * 2.0 * (double)Mp * (double)Kp * (double)nrows_b;   // executed TF32 MMA work
-  *splits = bf::tc_gemm_splits(Mp, nrows_b, Kp);
+  TCKS(tc_pick_splits(h, Ah, Al, Mp, Kp, Bh, Bl, nrows_b, d_err, splits));
   TCKS(out.alloc(h, sizeof(float) * (size_t)*splits * nrows_b * Mp));
   gemm_ev_begin(h);
   const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, *splits, out.as<float>(), d_err, st);
@@ -1794,12 +2015,18 @@ static int tf_propagation_matrices(bf_handle* h, bf_stack* s, bf_modes* md, TfCa
                                                    ncol, nd, d_eps.as<double2>(), dr, lst.as<int>(),
                                                    d_peps.as<int>(), npar);
       TCK(cudaGetLastError());
+      DBuf DKZ;
+      TCKS(DKZ.alloc(h, sizeof(float2) * (size_t)neps * nf * c.K));
+      bf::note_launch();
+      k_build_dkz<<<dim3(blocks_for(c.K), std::min(nf, 65535), neps), 256, 0, st>>>(
+          DKZ.as<float2>(), c.KT2.as<float>(), c.K, d_freq.as<double>(), nf, d_eps.as<double2>());
+      TCK(cudaGetLastError());
       const size_t nb = (size_t)2 * ncol * c.Kp;
       TCKS(Bh.alloc(h, sizeof(float) * nb));
       TCKS(Bl.alloc(h, sizeof(float) * nb));
       bf::note_launch();
       k_build_d_tc<<<dim3(blocks_for(c.Kp), std::min(ncol, 65535)), 256, 0, st>>>(
-          Bh.as<float>(), Bl.as<float>(), c.KT2.as<float>(), col.as<ColTC>(), c.K, c.Kp, ncol);
+          Bh.as<float>(), Bl.as<float>(), DKZ.as<float2>(), col.as<ColTC>(), c.K, c.Kp, ncol);
       TCK(cudaGetLastError());
       int splits = 1;
       TCKS(tc_class_gemm(h, c.Wh.as<float>(), c.Wl.as<float>(), c.Mp, c.Kp, Bh.as<float>(), Bl.as<float>(),
@@ -2239,27 +2466,61 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   int* d_sing = reinterpret_cast<int*>(h->d_scalar + 3);
   TCK(cudaMemsetAsync(d_sing, 0x7f, 2 * sizeof(int), st));
   int h_sing[2] = {0x7f7f7f7f, 0x7f7f7f7f};
-  if (nm <= 16) {
-    const int nmat = (nd - 1) * nf;
-    bf::note_launch();
-    if (nm <= 8) k_invert_warp<D2, 8><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing);
-    else k_invert_warp<D2, 16><<<(nmat + 7) / 8, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing);
-    TCK(cudaGetLastError());
-  } else if (std::is_same<D2, float2>::value && nm <= 64) {
-    dim3 grid(nd - 1, nf);
-    bf::note_launch();
-    if constexpr (std::is_same<D2, float2>::value) {
-      if (nm <= 32) k_invert_reg<32><<<grid, 64, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
-      else k_invert_reg<64><<<grid, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
+  // inverses of regions [1, nd) for frequencies [f0, f0 + nfi), or of the
+  // regions jl[0 .. njl) only
+  auto invert = [&](int f0, int nfi, const int* jl, int njl) -> int {
+    const int nj = jl ? njl : nd - 1;
+    if (nfi <= 0 || nj <= 0) return BF_OK;
+    if (nm <= 16) {
+      const int nmat = nj * nfi;
+      bf::note_launch();
+      if (nm <= 8)
+        k_invert_warp<D2, 8><<<(nmat + 31) / 32, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing, f0, jl,
+                                                             njl);
+      else
+        k_invert_warp<D2, 16><<<(nmat + 15) / 16, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, nmat, d_sing, f0, jl,
+                                                              njl);
+    } else if (std::is_same<D2, float2>::value && nm <= 64) {
+      dim3 grid(nj, nfi);
+      bf::note_launch();
+      if constexpr (std::is_same<D2, float2>::value) {
+        if (nm <= 32) k_invert_reg<32><<<grid, 64, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing, f0, jl);
+        else k_invert_reg<64><<<grid, 256, 0, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing, f0, jl);
+      }
+    } else {
+      const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
+      TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
+      dim3 grid(nj, nfi);
+      bf::note_launch();
+      k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing, f0, jl);
     }
     TCK(cudaGetLastError());
+    return BF_OK;
+  };
+  if (nreq > 1) {
+    // a group: request 0 inverts every region; the others only their own
+    // (k-space) air regions and take the disk regions' inverses from request 0
+    const int nf0 = nf / nreq;
+    std::vector<int> own, shared;
+    for (int j = 1; j < nd; ++j) (regs[j].klass == 0 ? own : shared).push_back(j);
+    DBuf d_own, d_shared;
+    TCKS(invert(0, nf0, nullptr, 0));
+    if (!own.empty()) {
+      TCKS(d_own.alloc(h, sizeof(int) * own.size()));
+      TCK(cudaMemcpyAsync(d_own.p, own.data(), sizeof(int) * own.size(), cudaMemcpyHostToDevice, st));
+      TCKS(invert(nf0, nf - nf0, d_own.as<int>(), (int)own.size()));
+    }
+    if (!shared.empty()) {
+      TCKS(d_shared.alloc(h, sizeof(int) * shared.size()));
+      TCK(cudaMemcpyAsync(d_shared.p, shared.data(), sizeof(int) * shared.size(), cudaMemcpyHostToDevice, st));
+      const size_t total = (size_t)nf0 * shared.size() * nm * nm * (nreq - 1);
+      bf::note_launch();
+      k_copy_inverses<D2><<<(unsigned)std::min<size_t>(blocks_for(total), 1u << 20), 256, 0, st>>>(
+          Pinv.as<D2>(), nd, nm, nf0, nreq, d_shared.as<int>(), (int)shared.size());
+      TCK(cudaGetLastError());
+    }
   } else {
-    const size_t smem = sizeof(D2) * 2 * nm * nm + 256 * (sizeof(double) + sizeof(int));
-    TCK(cudaFuncSetAttribute(k_invert<D2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
-    dim3 grid(nd - 1, nf);
-    bf::note_launch();
-    k_invert<D2><<<grid, 256, smem, st>>>(Pd, Pinv.as<D2>(), nd, 1, nm, d_sing);
-    TCK(cudaGetLastError());
+    TCKS(invert(0, nf, nullptr, 0));
   }
   // chain coefficients: step j uses n_left = sqrt(eps[j]), n_right = sqrt(eps[j-1])
   std::vector<ChainRegion> cr(nd);
@@ -2353,7 +2614,20 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
   TCKS(boost.alloc(h, sizeof(cd) * (size_t)nf * nm));
   if (reflect) TCKS(refl.alloc(h, sizeof(cd) * (size_t)nf * nm));
   TCKS(b2.alloc(h, sizeof(double) * nf));
-  {
+  if (nm <= 16) {
+    bf::note_launch();
+    if (nm <= 8)
+      k_final_solve_warp<8><<<(nf + 31) / 32, 256, 0, st>>>(T21.as<double2>(), T22.as<double2>(), ax.as<double2>(),
+                                                          reflect ? d_refl.as<double2>() : nullptr, nm,
+                                                          boost.as<double2>(), reflect ? refl.as<double2>() : nullptr,
+                                                          b2.as<double>(), d_sing + 1, nf);
+    else
+      k_final_solve_warp<16><<<(nf + 15) / 16, 256, 0, st>>>(T21.as<double2>(), T22.as<double2>(), ax.as<double2>(),
+                                                           reflect ? d_refl.as<double2>() : nullptr, nm,
+                                                           boost.as<double2>(), reflect ? refl.as<double2>() : nullptr,
+                                                           b2.as<double>(), d_sing + 1, nf);
+    TCK(cudaGetLastError());
+  } else {
     const size_t smem = sizeof(double2) * nm * (nm + 2) + 256 * (sizeof(double) + sizeof(int));
     TCK(cudaFuncSetAttribute(k_final_solve<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();

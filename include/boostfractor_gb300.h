@@ -433,7 +433,25 @@ int bf_wait(bf_server* s, unsigned long long id, int timeout_ms, int* status, do
 int bf_server_stats(bf_server* s, int solver, double* out);
 const char* bf_server_last_error(const bf_server* s);
 
+/* ---- autotuner --------------------------------------------------------------- */
+/* No counterpart in the reference.  The first solve of each shape times the
+ * fused stage kernel's variants (joint or separate slot propagation, 256 or 512
+ * threads; all give the same results bit for bit) on scratch copies of its
+ * largest stage, and the tensor-core GEMM's K slicing (1, 2, 4 or 8 slices),
+ * and keeps the fastest per device and shape for the rest of the process.
+ * bf_autotune(0) switches this off (rule-based choices), bf_autotune(1) on
+ * (the default); returns the previous setting.  bf_autotune_report copies the
+ * decisions taken so far, one line each, into out (cap bytes, NUL-terminated)
+ * and returns the full length. */
+int bf_autotune(int enable);
+int bf_autotune_report(char* out, int cap);
+
 /* ---- test hooks ------------------------------------------------------------ */
+/* No counterpart in the reference.  Force one fused stage kernel variant
+ * (0 = the rule, 1 = separate, 2 = joint, 3 = 512 threads; -1 = back to the
+ * autotuner) for every later solve of this process, to check that they agree;
+ * returns the previous setting. */
+int bf_test_force_fused_variant(int variant);
 /* No counterpart in the reference.  While `on` is non-zero, the tensor-core
  * overlap GEMM (BF_PREC_TF32) issues no operand copies, so its MMA warp's
  * bounded wait runs out after ~2 s and the solve returns BF_ERR_TIMEOUT with

@@ -339,3 +339,35 @@ def test_cheerleader_full_size_vs_oracle_fixture(B):
         assert rel(R64[k], fx["exit_field"][k]) < FP64_TOL
         assert abs(b64[k] - fx["beta2"][k]) / fx["beta2"][k] < FP64_TOL
         assert abs(b32[k] - fx["beta2"][k]) / fx["beta2"][k] < MIXED_BETA2_TOL
+
+
+@pytest.mark.parametrize("n,ndisk,nf", [(128, 3, 48), (256, 2, 24)])
+def test_fused_variants_agree_bit_for_bit(B, n, ndisk, nf):
+    """The fused stage kernel's variants (the rule, separate slots, joint
+    slots, 512 threads at 256x256 complex64) give identical results, so the
+    autotuner's choice never changes a result; the autotuner logs a decision
+    for the shape."""
+    from bfgb300 import _lib
+    L = _lib.lib()
+    distance, eps, tx, ty, X, _ = _stack_case(n, ndisk, seed=23)
+    cb, co = coords_pair(B, X)
+    sbb, _ = bdry_pair(B, cb, co, distance, eps, tx, ty)
+    st = B.Stack(sbb, cb, 0.15)
+    freqs = np.linspace(19.5e9, 20.5e9, nf)
+    try:
+        for prec in ("mixed", "fp64"):
+            ref = None
+            for v in (0, 1, 2, 3):
+                L.bf_test_force_fused_variant(v)
+                R, _, b2 = st.cheerleader(freqs, nmax=10, precision=prec)
+                if ref is None:
+                    ref = (R, b2)
+                else:
+                    assert np.array_equal(R, ref[0]) and np.array_equal(b2, ref[1]), (prec, v)
+            L.bf_test_force_fused_variant(-1)
+            R, _, b2 = st.cheerleader(freqs, nmax=10, precision=prec)   # tuned
+            assert np.array_equal(R, ref[0]) and np.array_equal(b2, ref[1])
+        assert any(f"N={n}" in line for line in B.autotune_report())
+    finally:
+        L.bf_test_force_fused_variant(-1)
+        st.close()
