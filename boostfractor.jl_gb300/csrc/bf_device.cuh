@@ -81,6 +81,9 @@ bool split_stage(int nsteps, int nfreq);
 // the kernel expired.
 int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
                    int splits, float* out, int* d_err, cudaStream_t st);
+// True when the output tiles of an M x N product alone give every SM about
+// four tiles (K slicing then only adds output traffic).
+bool tc_gemm_fills_gpu(int M, int N);
 // K slices for an M x N x Kp product: enough work units to keep every SM busy.
 int tc_gemm_splits(int M, int N, int Kp);
 bool tc_gemm_available();

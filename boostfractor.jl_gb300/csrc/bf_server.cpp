@@ -7,9 +7,11 @@
 // (bf_submit), keeps every stack's geometry and workspace resident on the
 // device, and runs admitted requests concurrently on its workers' streams:
 //   * workers: n_workers host threads, each owning one bf_handle (one stream);
-//     a stack's workspace lives with the worker that grew it (its "home") until
-//     the workspace is released, so a stack never pays a reallocation for
-//     changing streams;
+//     a stack's bounce-loop workspace lives with the worker that grew it (its
+//     "home") until the workspace is released, so a stack never pays a
+//     reallocation for changing streams; transformer solves keep only the
+//     overlap cache, which any worker's stream uses as it is, so their stacks
+//     run on whichever worker is free;
 //   * admission: the request's footprint + the bytes resident in served stacks
 //     + the running requests' footprints must fit the budget; idle stacks'
 //     workspaces are released least recently used first to make room; a queued
@@ -58,7 +60,7 @@ struct Req {
 };
 
 struct StackInfo {
-  int home = -1;      // worker holding the stack's workspace, -1 = none
+  int home = -1;      // worker holding the stack's bounce-loop workspace, -1 = none
   bool busy = false;
   double last_used = 0;
   size_t resident = 0;
@@ -154,12 +156,17 @@ bool mergeable(const Req* a, const Req* b) {
 }
 
 // The next batch worker w may start, or an empty batch.  Caller holds the lock.
+// Whether request R's stack holds workspace on a worker other than w.
+bool bound_elsewhere(const StackInfo& si, const Req* R, int w) {
+  return R->r.solver != BF_SOLVER_TRANSFORMER && si.home >= 0 && si.home != w;
+}
+
 Batch pick(bf_server* S, int w) {
   Batch b;
   for (size_t qi = 0; qi < S->queue.size(); ++qi) {
     Req* R = S->queue[qi];
     StackInfo& si = S->stacks[R->r.stack];
-    if (si.busy || (si.home >= 0 && si.home != w)) continue;
+    if (si.busy || bound_elsewhere(si, R, w)) continue;
     // the workspace the stack already holds is reused by the solve
     const size_t need = R->est > si.resident ? R->est - si.resident : 0;
     if (!make_room(S, need, R->r.stack)) {
@@ -192,7 +199,7 @@ Batch pick(bf_server* S, int w) {
         for (Req* G : b.reqs) dup |= G->r.stack == Q->r.stack;
         if (dup) continue;
         StackInfo& qs = S->stacks[Q->r.stack];
-        if (qs.busy || (qs.home >= 0 && qs.home != w)) continue;
+        if (qs.busy) continue;
         // an earlier queued request on Q's stack keeps its turn
         bool earlier = false;
         for (size_t qk = 0; qk < qj && !earlier; ++qk)
@@ -214,7 +221,7 @@ Batch pick(bf_server* S, int w) {
     for (Req* G : b.reqs) {
       StackInfo& gi = S->stacks[G->r.stack];
       gi.busy = true;
-      gi.home = w;
+      if (G->r.solver != BF_SOLVER_TRANSFORMER) gi.home = w;
     }
     S->inflight += b.need;
     return b;

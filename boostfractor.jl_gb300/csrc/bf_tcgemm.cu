@@ -379,6 +379,10 @@ size_t tc_gemm_smem_bytes() { return (size_t)kStages * kStageBytes + 1024 + 256;
 
 bool tc_gemm_available() { return encoder() != nullptr; }
 
+bool tc_gemm_fills_gpu(int M, int N) {
+  return (long)(M / kTM) * ((N + kTN - 1) / kTN) >= 4L * sm_count();
+}
+
 int tc_gemm_splits(int M, int N, int Kp) {
   const long tiles = (long)(M / kTM) * ((N + kTN - 1) / kTN);
   const int ktiles = Kp / kTK;

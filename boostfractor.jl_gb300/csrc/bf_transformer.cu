@@ -1842,10 +1842,13 @@ static int launch_rgemm(bf_handle* h, const float* A, const float2* B, double2* 
 // (FP32) = A [Mp][Kp] times the 2 ncol real rows of B^T [2 ncol][Kp] (TF32
 // hi/lo pairs), K cut into slices only when the output tiles alone would
 // leave SMs idle; k_scatter_herm_tc sums the slices in FP64.
-// The K slicing of the tensor-core GEMM, per (device, M, N, K): the
-// heuristic's count, or, with the autotuner on, the fastest of 1, 2, 4, 8
-// slices timed once on the first call's operands (the output of the trials is
-// scratch; every count gives the same sums up to FP32 rounding of the slices).
+// The K slicing of the tensor-core GEMM, per (device, M, N rounded up to a
+// power of two, K): the heuristic's count, or, with the autotuner on, the
+// fastest of 1, 2, 4, 8 slices timed once on the first call's operands (the
+// output of the trials is scratch; every count gives the same sums up to FP32
+// rounding of the slices).  Products whose output tiles already fill the GPU
+// keep one slice untimed, so that group solves of varying size (a new N each)
+// trigger no trials while serving.
 static std::mutex g_split_mu;
 static std::map<std::array<long long, 4>, int> g_split_tuned;
 
@@ -1853,8 +1856,10 @@ static int tc_pick_splits(bf_handle* h, const float* Ah, const float* Al, int Mp
                           const float* Bl, int nrows_b, int* d_err, int* splits) {
   cudaStream_t st = h->stream();
   *splits = bf::tc_gemm_splits(Mp, nrows_b, Kp);
-  if (!bf_autotune_enabled()) return BF_OK;
-  const std::array<long long, 4> key = {h->device, Mp, nrows_b, Kp};
+  if (!bf_autotune_enabled() || bf::tc_gemm_fills_gpu(Mp, nrows_b)) return BF_OK;
+  long long nb = 1;
+  while (nb < nrows_b) nb <<= 1;
+  const std::array<long long, 4> key = {h->device, Mp, nb, Kp};
   {
     std::lock_guard<std::mutex> lock(g_split_mu);
     auto it = g_split_tuned.find(key);
@@ -2599,8 +2604,9 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();
     // one thread per matrix entry up to 1024 (at 64 modes one CTA per frequency
-    // owns the SM's shared memory, and 32 warps hide the serial TwoSum chains)
-    const int nthr = std::min(1024, std::max(128, (nm * nm + 31) / 32 * 32));
+    // owns the SM's shared memory, and 32 warps hide the serial TwoSum chains;
+    // at few modes small CTAs, many per SM, keep every warp busy)
+    const int nthr = std::min(1024, std::max(32, (nm * nm + 31) / 32 * 32));
     k_chain_df<<<nf, nthr, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                       t_in_smem ? nullptr : T21df.as<DFc>(), t_in_smem ? nullptr : T22df.as<DFc>(),
                                       ax.as<double2>(), T21.as<double2>(),

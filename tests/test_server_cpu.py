@@ -154,3 +154,28 @@ def test_transformer_steps_of_different_stacks_form_one_group(B):
         assert srv.stats("transformer")["batched"] == 4
     finally:
         srv.close()
+
+
+def test_transformer_stack_runs_on_any_free_worker(B):
+    """A transformer stack keeps no workspace bound to one worker's stream, so
+    its next step starts on whichever worker is free: after each step, a long
+    bounce-loop request occupies one of the two workers, and the step that
+    follows starts at once on the other (a stack pinned to the worker that ran
+    it would wait, in about half of the trials, for the long request)."""
+    import ctypes
+    import types
+    modes = types.SimpleNamespace(_m=ctypes.c_void_p(0x9990), nm=1)
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        f = [1e10]
+        for trial in range(8):
+            r = srv.wait(srv.submit(0xC000, f, "transformer", modes=modes, nmax=1000, distance=[0.0],
+                                    footprint_bytes=MB), timeout_ms=20000)
+            long_id = srv.submit(0xD000 + 16 * trial, f, nmax=150000, footprint_bytes=MB)
+            time.sleep(0.01)   # one worker has taken the long request
+            r = srv.wait(srv.submit(0xC000, f, "transformer", modes=modes, nmax=1000, distance=[0.0],
+                                    footprint_bytes=MB), timeout_ms=20000)
+            rl = srv.wait(long_id, timeout_ms=20000)
+            assert r["t_done"] < rl["t_done"], trial
+    finally:
+        srv.close()
