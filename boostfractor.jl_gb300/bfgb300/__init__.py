@@ -951,6 +951,10 @@ class Server:
                 "batched", "evictions"]
         return dict(zip(keys, out.tolist()))
 
+    def reset_stats(self):
+        """Start a new statistics window (after warm-up requests)."""
+        self._check(_lib.lib().bf_server_reset_stats(self._p))
+
     def close(self):
         if getattr(self, "_p", None):
             _lib.lib().bf_server_destroy(self._p)

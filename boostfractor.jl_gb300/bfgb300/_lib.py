@@ -91,6 +91,7 @@ _SIGS = {
     "bf_poll": (_c_int, [_vp, _ull, ctypes.POINTER(_c_int), _p_dbl]),
     "bf_wait": (_c_int, [_vp, _ull, _c_int, ctypes.POINTER(_c_int), _p_dbl]),
     "bf_server_stats": (_c_int, [_vp, _c_int, _p_dbl]),
+    "bf_server_reset_stats": (_c_int, [_vp]),
     "bf_server_last_error": (ctypes.c_char_p, [_vp]),
     "bf_stack_create": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                  _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, ctypes.POINTER(_vp)]),

@@ -74,6 +74,9 @@ int bf_fail(bf_handle* h, int code, const std::string& msg) { return fail(h, cod
 // neither waits for the rest of the device, so handles working on different
 // streams (the serving engine's workers) do not serialise each other.  Freed
 // blocks stay in the pool for the next request; bf_destroy trims the pool.
+// An allocation reuses a block freed on another stream only once that free
+// has completed: the pool may not make one worker's stream wait for the work
+// another worker has in flight (it grows instead).
 static cudaMemPool_t device_pool(int device) {
   static std::mutex mu;
   static cudaMemPool_t pools[64] = {};
@@ -91,6 +94,8 @@ static cudaMemPool_t device_pool(int device) {
     }
     unsigned long long keep = ~0ull;
     cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    int no = 0;
+    cudaMemPoolSetAttribute(p, cudaMemPoolReuseAllowInternalDependencies, &no);
     pools[device] = p;
   }
   return pools[device];

@@ -620,4 +620,19 @@ extern "C" int bf_server_stats(bf_server* S, int solver, double* out) {
   return BF_OK;
 }
 
+extern "C" int bf_server_reset_stats(bf_server* S) {
+  if (!S) return BF_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  for (int k = 0; k < 4; ++k) {
+    S->lat[k].clear();
+    S->fpts[k] = 0.0;
+    S->failed[k] = 0;
+    S->batched[k] = 0;
+  }
+  S->evictions = 0;
+  S->t_first = -1.0;
+  S->t_last = 0.0;
+  return BF_OK;
+}
+
 extern "C" const char* bf_server_last_error(const bf_server* S) { return S ? S->err.c_str() : ""; }

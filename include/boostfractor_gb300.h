@@ -431,14 +431,20 @@ int bf_wait(bf_server* s, unsigned long long id, int timeout_ms, int* status, do
  * the first submission to the last completion, requests solved as part of
  * another's batch, stack workspaces released for admission. */
 int bf_server_stats(bf_server* s, int solver, double* out);
+/* Starts a new statistics window (e.g. after warm-up requests): the counters
+ * and latencies of bf_server_stats restart from zero; requests queued or
+ * running are counted when they complete. */
+int bf_server_reset_stats(bf_server* s);
 const char* bf_server_last_error(const bf_server* s);
 
 /* ---- autotuner --------------------------------------------------------------- */
 /* No counterpart in the reference.  The first solve of each shape times the
- * fused stage kernel's variants (joint or separate slot propagation, 256 or 512
- * threads; all give the same results bit for bit) on scratch copies of its
- * largest stage, and the tensor-core GEMM's K slicing (1, 2, 4 or 8 slices),
- * and keeps the fastest per device and shape for the rest of the process.
+ * fused stage kernel's variants (joint or separate slot propagation, 256, 384
+ * or 512 threads, twiddles in registers or shared memory, 2 or 3 CTAs per SM;
+ * all give the same results bit for bit) on scratch copies of its largest
+ * stage, and the tensor-core GEMM's K slicing (1, 2, 4 or 8 slices, for GEMMs
+ * whose output tiles do not already fill the GPU), and keeps the fastest per
+ * device and shape for the rest of the process.
  * bf_autotune(0) switches this off (rule-based choices), bf_autotune(1) on
  * (the default); returns the previous setting.  bf_autotune_report copies the
  * decisions taken so far, one line each, into out (cap bytes, NUL-terminated)
@@ -448,9 +454,11 @@ int bf_autotune_report(char* out, int cap);
 
 /* ---- test hooks ------------------------------------------------------------ */
 /* No counterpart in the reference.  Force one fused stage kernel variant
- * (0 = the rule, 1 = separate, 2 = joint, 3 = 512 threads; -1 = back to the
- * autotuner) for every later solve of this process, to check that they agree;
- * returns the previous setting. */
+ * (0 = the rule, 1 = separate, 2 = joint, 3 = 512 threads, 4 = joint with
+ * 384 threads and shared twiddles, 5 = separate at 3 CTAs per SM with shared
+ * twiddles; a variant that does not apply to a stage's shape runs the rule;
+ * -1 = back to the autotuner) for every later solve of this process, to check
+ * that they agree; returns the previous setting. */
 int bf_test_force_fused_variant(int variant);
 /* No counterpart in the reference.  While `on` is non-zero, the tensor-core
  * overlap GEMM (BF_PREC_TF32) issues no operand copies, so its MMA warp's

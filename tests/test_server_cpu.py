@@ -179,3 +179,19 @@ def test_transformer_stack_runs_on_any_free_worker(B):
             assert r["t_done"] < rl["t_done"], trial
     finally:
         srv.close()
+
+
+def test_reset_stats_starts_a_new_window(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        for i in [srv.submit(0xE000 + 16 * k, [1e10, 2e10], nmax=1000, footprint_bytes=MB) for k in range(3)]:
+            srv.wait(i, timeout_ms=20000)
+        assert srv.stats()["completed"] == 3
+        srv.reset_stats()
+        s = srv.stats()
+        assert s["completed"] == 0 and s["freq_points"] == 0 and s["p99_ms"] == 0 and s["wall_s"] == 0
+        srv.wait(srv.submit(0xE000, [1e10], nmax=1000, footprint_bytes=MB), timeout_ms=20000)
+        s = srv.stats()
+        assert s["completed"] == 1 and s["freq_points"] == 1
+    finally:
+        srv.close()
