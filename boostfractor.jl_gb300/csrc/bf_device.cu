@@ -163,6 +163,28 @@ constexpr int kSmemHeader = 128;
 
 template <int N> __host__ __device__ constexpr int fused_pitch() { return N + 2; }
 
+// Kernel-shape options of the fused stage (a bit mask): the inter-pass
+// twiddles from a shared table instead of registers; team exchanges in two
+// halves through half-size scratch; each column task's folded phasor row
+// copied into the team's shared buffer (cp.async) while the team runs the
+// forward transform, instead of loaded from L2 after it.  None changes the
+// arithmetic.
+constexpr int kModeTwShared = 1, kModeHalf = 2, kModeStage = 4;
+
+// Complex elements of one team's shared region: its exchange scratch, then
+// (kModeStage) the N/2-entry phasor row buffer.
+template <int N, int MODE> __host__ __device__ constexpr int team_region() {
+  return Team<N>::template scratch<(MODE & kModeHalf) != 0>() + ((MODE & kModeStage) ? N / 2 : 0);
+}
+
+__device__ __forceinline__ void cp_async16(void* dst_smem, const void* src_global) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((unsigned)__cvta_generic_to_shared(dst_smem)),
+               "l"(src_global)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 template <typename C, int N>
 struct FusedCtx {
   using T = Team<N>;
@@ -174,9 +196,9 @@ struct FusedCtx {
 // are stored pre-masked, so only register slots r < ceil(nbx/G) can hold box
 // pixels.  A slot feeding an exit adds its (masked) input to the FP64 exit
 // accumulator on the way.
-template <typename C, int N, int NZ, int NT>
+template <typename C, int N, int NZ, int NT, bool HALF = false>
 __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int slot, int exitk, C* M,
-                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g) {
+                                             C* scr, const C* tw, int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
   constexpr int NTEAM = NT;
@@ -207,7 +229,7 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
         }
       }
     }
-    X::T::template forward<NZ>(v, tw, scr, g);
+    X::T::template forward<NZ, HALF>(v, tw, scr, g);
     if (act) {
 #pragma unroll
       for (int j = 0; j < CC; ++j)
@@ -219,20 +241,31 @@ __device__ __forceinline__ void fused_phase1(const FusedArgs<C>& a, int f, int s
 }
 
 // Phase 2: per column kx, forward FFT along y, phasor, inverse FFT along y,
-// in place in M (only the nby box rows are read and written).
-template <typename C, int N, int NZ, int NT>
+// in place in M (only the nby box rows are read and written).  STAGE: the
+// column's folded phasor row is copied into the team's buffer behind its
+// scratch (cp.async, issued before the forward transform) and read from there.
+template <typename C, int N, int NZ, int NT, bool HALF = false, bool STAGE = false>
 __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, C* M, C* scr,
-                                             const C (&tw)[Team<N>::RR], int team, int g) {
+                                             const C* tw, int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
   constexpr int NTEAM = NT;
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
+  C* qb = STAGE ? scr + X::T::template scratch<HALF>() : nullptr;
   for (int base = 0; base < N; base += NTEAM) {
     const int kx = base + team;
     const bool act = kx < N;
     if (!__any_sync(0xffffffffu, act)) continue;
+    if constexpr (STAGE) {
+      if (act && a.fold) {
+        constexpr int E = 16 / sizeof(C);   // elements per 16-byte chunk
+        const C* row = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
+        for (int c = g; c < (N / 2) / E; c += G) cp_async16(qb + c * E, row + c * E);
+      }
+      cp_async_commit();
+    }
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -242,11 +275,15 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
         if (act && y < nby) v[r] = M[y * P + kx];
       }
     }
-    X::T::template forward<NZ>(v, tw, scr, g);
+    X::T::template forward<NZ, HALF>(v, tw, scr, g);
+    if constexpr (STAGE) {
+      cp_async_wait_all();
+      __syncwarp();
+    }
     if (act) {
       if (a.fold) {
         // bins k and N-1-k share a phasor; ky = g*CC + j + RR*q < N/2 exactly when q < G/2
-        const C* Qrow = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
+        const C* Qrow = STAGE ? qb : Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
 #pragma unroll
         for (int j = 0; j < CC; ++j)
 #pragma unroll
@@ -262,7 +299,9 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
           for (int q = 0; q < G; ++q) v[j * G + q] = cmul(v[j * G + q], Qrow[g * CC + j + RR * q]);
       }
     }
-    X::T::inverse(v, tw, scr, g);
+    // (the inverse's exchange syncs the warp: every lane has read the buffer
+    // before the next task's copies overwrite it)
+    X::T::template inverse<HALF>(v, tw, scr, g);
     if (act) {
 #pragma unroll
       for (int r = 0; r < RR; ++r) {
@@ -279,10 +318,10 @@ __device__ __forceinline__ void fused_phase2(const FusedArgs<C>& a, const C* Q, 
 // Phase 3: inverse FFT along x of every box row, tilt/surface map, then the
 // epilogue: store the propagated field into obuf (first of two propagations)
 // or apply the boundary mix and write the new (masked) fields.
-template <typename C, int N, bool MIX, int NZ, int NT>
+template <typename C, int N, bool MIX, int NZ, int NT, bool HALF = false>
 __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, int region,
                                              bool prop_is_b, C* M, C* scr, C* obuf,
-                                             const C (&tw)[Team<N>::RR], int team, int g) {
+                                             const C* tw, int team, int g) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
   constexpr int NTEAM = NT;
@@ -308,7 +347,7 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
     for (int j = 0; j < CC; ++j)
 #pragma unroll
       for (int q = 0; q < G; ++q) v[j * G + q] = act ? M[y * P + g * CC + j + RR * q] : czero<C>();
-    X::T::inverse(v, tw, scr, g);
+    X::T::template inverse<HALF>(v, tw, scr, g);
     if (!act) continue;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -353,9 +392,9 @@ __device__ __forceinline__ void fused_phase3(const FusedArgs<C>& a, const StepDe
 // tasks of a slot that is not propagated (pa / pb false) are skipped.
 
 // Phase 1, joint: forward FFT along x of the box rows of A (tasks < nby) and B.
-template <typename C, int N, int NZ, int NT, bool SPLIT>
+template <typename C, int N, int NZ, int NT, bool SPLIT, bool HALF = false>
 __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
-                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts,
+                                             C* scr, const C* tw, int team, int g, int t0, int ts,
                                              bool pa, bool pb) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
@@ -389,7 +428,7 @@ __device__ __forceinline__ void joint_phase1(const FusedArgs<C>& a, const StepDe
         }
       }
     }
-    X::T::template forward<NZ>(v, tw, scr, g);
+    X::T::template forward<NZ, HALF>(v, tw, scr, g);
     if (act) {
       C* M = isb ? MB : MA;
 #pragma unroll
@@ -417,15 +456,18 @@ __device__ __forceinline__ void prefetch_qrow(const FusedArgs<C>& a, const C* QA
 }
 
 // Phase 2, joint: columns of A (tasks < N) and of B, each with its region's phasor.
-template <typename C, int N, int NZ, int NT, bool SPLIT>
+// STAGE as fused_phase2 (the fused kernel only).
+template <typename C, int N, int NZ, int NT, bool SPLIT, bool HALF = false, bool STAGE = false>
 __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA, const C* QB, C* MA, C* MB, C* scr,
-                                             const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts) {
+                                             const C* tw, int team, int g, int t0, int ts) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
+  static_assert(!(SPLIT && STAGE), "staged phasor rows: fused kernel only");
   const int nby = a.nby;
   const int QW = a.fold ? N / 2 : N;
   const int rv = (nby + G - 1) / G;
   const int T0 = SPLIT ? t0 : 0, TS = SPLIT ? ts : NT;
+  C* qb = STAGE ? scr + X::T::template scratch<HALF>() : nullptr;
   for (int base = T0; base < 2 * N; base += TS) {
     const int t = base + team;
     const bool act = t < 2 * N && (!SPLIT || (t >= N ? QB : QA) != nullptr);
@@ -434,7 +476,17 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
     const int kx = act ? (isb ? t - N : t) : 0;
     C* M = isb ? MB : MA;
     const C* Q = isb ? QB : QA;
-    prefetch_qrow<C, N, SPLIT>(a, QA, QB, t + TS, g);
+    if constexpr (STAGE) {
+      if (act && a.fold) {
+        constexpr int E = 16 / sizeof(C);   // elements per 16-byte chunk
+        const C* row = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
+        for (int c = g; c < (N / 2) / E; c += G) cp_async16(qb + c * E, row + c * E);
+      }
+      cp_async_commit();
+      if (!a.fold) prefetch_qrow<C, N, SPLIT>(a, QA, QB, t + TS, g);
+    } else {
+      prefetch_qrow<C, N, SPLIT>(a, QA, QB, t + TS, g);
+    }
     C v[RR];
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -444,10 +496,14 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
         if (act && y < nby) v[r] = M[y * P + kx];
       }
     }
-    X::T::template forward<NZ>(v, tw, scr, g);
+    X::T::template forward<NZ, HALF>(v, tw, scr, g);
+    if constexpr (STAGE) {
+      cp_async_wait_all();
+      __syncwarp();
+    }
     if (act) {
       if (a.fold) {
-        const C* Qrow = Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
+        const C* Qrow = STAGE ? qb : Q + (size_t)(kx < N / 2 ? kx : N - 1 - kx) * QW;
 #pragma unroll
         for (int j = 0; j < CC; ++j)
 #pragma unroll
@@ -463,7 +519,8 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
           for (int q = 0; q < G; ++q) v[j * G + q] = cmul(v[j * G + q], Qrow[g * CC + j + RR * q]);
       }
     }
-    X::T::inverse(v, tw, scr, g);
+    // (the inverse's exchange syncs the warp before the buffer is refilled)
+    X::T::template inverse<HALF>(v, tw, scr, g);
     if (act) {
 #pragma unroll
       for (int r = 0; r < RR; ++r) {
@@ -480,9 +537,9 @@ __device__ __forceinline__ void joint_phase2(const FusedArgs<C>& a, const C* QA,
 // Phase 3, joint: inverse FFT along x of the box rows of A and B, times the
 // region's tilt/surface map, written back in place into the row's first nbx
 // entries (the team's exchange has already consumed the row).
-template <typename C, int N, int NZ, int NT, bool SPLIT>
+template <typename C, int N, int NZ, int NT, bool SPLIT, bool HALF = false>
 __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDesc& sd, int f, C* MA, C* MB,
-                                             C* scr, const C (&tw)[Team<N>::RR], int team, int g, int t0, int ts,
+                                             C* scr, const C* tw, int team, int g, int t0, int ts,
                                              bool pa, bool pb) {
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, CC = X::CC, P = X::P;
@@ -506,7 +563,7 @@ __device__ __forceinline__ void joint_phase3(const FusedArgs<C>& a, const StepDe
     for (int j = 0; j < CC; ++j)
 #pragma unroll
       for (int q = 0; q < G; ++q) v[j * G + q] = act ? M[y * P + g * CC + j + RR * q] : czero<C>();
-    X::T::inverse(v, tw, scr, g);
+    X::T::template inverse<HALF>(v, tw, scr, g);
     if (!act) continue;
 #pragma unroll
     for (int r = 0; r < RR; ++r) {
@@ -553,23 +610,39 @@ __device__ __forceinline__ void joint_mix(const FusedArgs<C>& a, const StepDesc&
 // with both slots propagated take the joint path (twice the row tile in
 // shared memory).  NZ: box lines occupy at most NZ of a thread's RR register
 // slots (x = g + G r < nbx, y = g + G r < nby only for r < NZ), so the first
-// forward pass is pruned and the inverse stores only NZ slots.
-template <typename R, int N, bool JOINT, int NZ, int THREADS>
-__global__ void __launch_bounds__(THREADS, (sizeof(R) == 4 && N <= 128) ? 2 : 1)
-k_fused_stage(FusedArgs<cplx_t<R>> a) {
+// forward pass is pruned and the inverse stores only NZ slots.  MINB: CTAs
+// per SM the registers are sized for.  MODE: kModeTwShared | kModeHalf |
+// kModeStage (fewer registers or less shared memory per warp, so more warps
+// per SM, and phasor rows staged ahead); the arithmetic, and so every result,
+// is the same.
+template <typename R, int N, bool JOINT, int NZ, int THREADS, int MINB, int MODE>
+__global__ void __launch_bounds__(THREADS, MINB) k_fused_stage(FusedArgs<cplx_t<R>> a) {
   using C = cplx_t<R>;
   using X = FusedCtx<C, N>;
   constexpr int G = X::G, RR = X::RR, P = X::P;
+  constexpr int NTEAM = THREADS / G;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int nby = a.nby;
   C* M = reinterpret_cast<C*>(smem_raw + kSmemHeader);
   C* scr_all = M + (JOINT ? 2 : 1) * nby * P;
   const int tid = threadIdx.x, team = tid / G, g = tid % G;
-  C* scr = scr_all + team * X::T::SCR;
+  constexpr bool HALF = (MODE & kModeHalf) != 0, STAGE = (MODE & kModeStage) != 0;
+  C* scr = scr_all + team * team_region<N, MODE>();
   const StepDesc sd = a.steps[blockIdx.x];
   const int f = blockIdx.y;
-  C tw[RR];
-  team_twiddles<N>(tw, g);
+  C twr[RR];
+  const C* tw = twr;
+  if constexpr ((MODE & kModeTwShared) != 0) {
+    // tw[g][s] = W_N^(g s) behind the teams' regions, rows RR + 1 apart so
+    // that the G threads of a team reading their s-th twiddle hit distinct banks
+    C* tws = scr_all + NTEAM * team_region<N, MODE>();
+    for (int i = tid; i < G * RR; i += THREADS)
+      tws[(i / RR) * (RR + 1) + i % RR] = root1024<C>((i / RR) * (i % RR) * (1024 / N));
+    __syncthreads();
+    tw = tws + g * (RR + 1);
+  } else {
+    team_twiddles<N>(twr, g);
+  }
   const int QW = a.fold ? N / 2 : N;
   auto qptr = [&](int region) -> const C* {
     return a.phasor + ((size_t)f * a.ntab + region) * (size_t)(QW * QW);
@@ -577,30 +650,30 @@ k_fused_stage(FusedArgs<cplx_t<R>> a) {
   const bool pa = sd.ra >= 0, pb = sd.rb >= 0;
   if (JOINT && pa && pb) {
     C* MB = M + nby * P;
-    constexpr int nteam = THREADS / G;
     prefetch_qrow<C, N, false>(a, qptr(sd.ra), qptr(sd.rb), team, g);
-    joint_phase1<C, N, NZ, THREADS / G, false>(a, sd, f, M, MB, scr, tw, team, g, 0, nteam, true, true);
-    joint_phase2<C, N, NZ, THREADS / G, false>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g, 0, nteam);
-    joint_phase3<C, N, NZ, THREADS / G, false>(a, sd, f, M, MB, scr, tw, team, g, 0, nteam, true, true);
+    joint_phase1<C, N, NZ, NTEAM, false, HALF>(a, sd, f, M, MB, scr, tw, team, g, 0, NTEAM, true, true);
+    joint_phase2<C, N, NZ, NTEAM, false, HALF, STAGE>(a, qptr(sd.ra), qptr(sd.rb), M, MB, scr, tw, team, g, 0,
+                                                      NTEAM);
+    joint_phase3<C, N, NZ, NTEAM, false, HALF>(a, sd, f, M, MB, scr, tw, team, g, 0, NTEAM, true, true);
     joint_mix<C, N>(a, sd, f, M, MB, true, true, threadIdx.x, blockDim.x);
   } else if (pa && pb) {
     // A~ is parked in the A slot itself until the boundary mix
     C* obuf = a.state + ((size_t)f * a.nslots + sd.sa) * (size_t)(nby * a.nbx);
-    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, false, NZ, THREADS / G>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, false, NZ, NTEAM, HALF>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
     __syncthreads();
-    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
+    fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, NTEAM, HALF>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
   } else if (pa) {
-    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.ra), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.ra), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, NTEAM, HALF>(a, sd, f, sd.ra, false, M, scr, nullptr, tw, team, g);
   } else if (pb) {
-    fused_phase1<C, N, NZ, THREADS / G>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
-    fused_phase2<C, N, NZ, THREADS / G>(a, qptr(sd.rb), M, scr, tw, team, g);
-    fused_phase3<C, N, true, NZ, THREADS / G>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
+    fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
+    fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.rb), M, scr, tw, team, g);
+    fused_phase3<C, N, true, NZ, NTEAM, HALF>(a, sd, f, sd.rb, true, M, scr, nullptr, tw, team, g);
   }
 }
 
@@ -694,10 +767,11 @@ size_t split_tile_bytes(int N, int nby, int nfreq, int nsteps, bool fp64) {
 // Whether a stage of `nsteps` steps x `nfreq` frequencies takes the split path.
 bool split_stage(int nsteps, int nfreq) { return (long long)nsteps * nfreq < sm_count(); }
 
-template <int N>
+template <int N, int MODE = 0>
 static size_t fused_smem_for(int nby, size_t csz, int tiles = 1, int threads = kFusedThreads) {
   const size_t nteam = threads / Team<N>::G;
-  return kSmemHeader + csz * ((size_t)tiles * nby * fused_pitch<N>() + nteam * Team<N>::SCR);
+  const size_t twt = (MODE & kModeTwShared) ? (size_t)Team<N>::G * (Team<N>::RR + 1) : 0;   // twiddle table
+  return kSmemHeader + csz * ((size_t)tiles * nby * fused_pitch<N>() + nteam * team_region<N, MODE>() + twt);
 }
 
 static size_t smem_for(int N, int nby, size_t csz) {
@@ -732,12 +806,13 @@ static const size_t kSmemPerSM = 228 * 1024, kSmemReservedPerCta = 1024;
 // maximum, the same value for every launch: launches of one kernel with
 // different sizes from several host threads (the serving engine's workers)
 // must not lower it under one another.
-template <typename R, int N, bool JOINT, int NZ, int THREADS = kFusedThreads>
+template <typename R, int N, bool JOINT, int NZ, int THREADS = kFusedThreads,
+          int MINB = (sizeof(R) == 4 && N <= 128) ? 2 : 1, int MODE = 0>
 static int launch_fused_v(const FusedArgs<cplx_t<R>>& a, dim3 grid, size_t smem, cudaStream_t st) {
-  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ, THREADS>,
+  cudaError_t e = cudaFuncSetAttribute(k_fused_stage<R, N, JOINT, NZ, THREADS, MINB, MODE>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxSmem);
   if (e != cudaSuccess) return (int)e;
-  k_fused_stage<R, N, JOINT, NZ, THREADS><<<grid, THREADS, smem, st>>>(a);
+  k_fused_stage<R, N, JOINT, NZ, THREADS, MINB, MODE><<<grid, THREADS, smem, st>>>(a);
   return (int)cudaGetLastError();
 }
 
@@ -749,9 +824,18 @@ template <int N> constexpr int pruned_slots() { return (5 * Team<N>::RR + 15) / 
 // Shape of one fused-stage launch: shared memory of the single and doubled
 // (joint) row tiles and whether the rule takes the joint path.
 struct FusedShape {
-  size_t smem, smem_j, smem512;
+  size_t smem, smem_j, smem512, smem_jl, smem_sl, smem_js, smem_ss;
   bool joint_rule, joint_fits, wide_fits;
+  // complex64, N = 128: joint steps with 320 threads at 2 CTAs per SM and
+  // shared twiddles (lean), separate slots at 3 CTAs per SM and shared
+  // twiddles (lean), joint steps with staged phasor rows, separate slots at 3
+  // CTAs per SM with shared twiddles and staged phasor rows
+  bool joint_lean_fits, sep_lean_fits, joint_staged_fits, sep_staged_fits;
 };
+constexpr int kLeanJointThreads = 320;
+constexpr int kModeLean = kModeTwShared | kModeHalf;
+constexpr int kModeJointStaged = kModeHalf | kModeStage;
+constexpr int kModeSepStaged = kModeTwShared | kModeHalf | kModeStage;
 template <int N>
 static FusedShape fused_shape(int nby, size_t csz) {
   FusedShape f;
@@ -764,29 +848,43 @@ static FusedShape fused_shape(int nby, size_t csz) {
   f.joint_rule = f.joint_fits && (size_t)ctas * (f.smem_j + kSmemReservedPerCta) <= kSmemPerSM &&
                  (size_t)ctas * (f.smem + kSmemReservedPerCta) <= kSmemPerSM;
   f.wide_fits = csz == 8 && N == 256 && f.smem512 <= kMaxSmem;
+  f.smem_jl = fused_smem_for<N, kModeLean>(nby, csz, 2, kLeanJointThreads);
+  f.smem_sl = fused_smem_for<N, kModeLean>(nby, csz, 1, kFusedThreads);
+  f.smem_js = fused_smem_for<N, kModeJointStaged>(nby, csz, 2, kFusedThreads);
+  f.smem_ss = fused_smem_for<N, kModeSepStaged>(nby, csz, 1, kFusedThreads);
+  const bool c128 = csz == 8 && N == 128;
+  f.joint_lean_fits = c128 && 2 * (f.smem_jl + kSmemReservedPerCta) <= kSmemPerSM;
+  f.sep_lean_fits = c128 && 3 * (f.smem_sl + kSmemReservedPerCta) <= kSmemPerSM;
+  f.joint_staged_fits = c128 && 2 * (f.smem_js + kSmemReservedPerCta) <= kSmemPerSM;
+  f.sep_staged_fits = c128 && 3 * (f.smem_ss + kSmemReservedPerCta) <= kSmemPerSM;
   return f;
 }
 
 template <int N>
-static std::vector<int> fused_variants_t(int nby, bool fp64) {
+static std::vector<int> fused_variants_t(int nbx, int nby, bool fp64) {
   const FusedShape f = fused_shape<N>(nby, fp64 ? 16 : 8);
+  // the lean variants exist for boxes within the pruned register slots only
+  const bool pruned = (std::max(nbx, nby) + Team<N>::G - 1) / Team<N>::G <= pruned_slots<N>();
   std::vector<int> v = {kFusedRule};
   if (f.smem > kMaxSmem) return v;
   v.push_back(kFusedSeparate);
   if (f.joint_fits) v.push_back(kFusedJoint);
   if (f.wide_fits) v.push_back(kFusedWide);
+  if (f.joint_lean_fits && pruned) v.push_back(kFusedJointLean);
+  if (f.sep_lean_fits && pruned) v.push_back(kFusedSeparateLean);
+  if (f.joint_staged_fits && pruned) v.push_back(kFusedJointStaged);
+  if (f.sep_staged_fits && pruned) v.push_back(kFusedSeparateStaged);
   return v;
 }
 
 std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64) {
-  (void)nbx;
   switch (N) {
-    case 8: return fused_variants_t<8>(nby, fp64);
-    case 16: return fused_variants_t<16>(nby, fp64);
-    case 32: return fused_variants_t<32>(nby, fp64);
-    case 64: return fused_variants_t<64>(nby, fp64);
-    case 128: return fused_variants_t<128>(nby, fp64);
-    case 256: return fused_variants_t<256>(nby, fp64);
+    case 8: return fused_variants_t<8>(nbx, nby, fp64);
+    case 16: return fused_variants_t<16>(nbx, nby, fp64);
+    case 32: return fused_variants_t<32>(nbx, nby, fp64);
+    case 64: return fused_variants_t<64>(nbx, nby, fp64);
+    case 128: return fused_variants_t<128>(nbx, nby, fp64);
+    case 256: return fused_variants_t<256>(nbx, nby, fp64);
     default: return {kFusedRule};
   }
 }
@@ -819,6 +917,19 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
   }
   dim3 grid(nsteps, a.nfreq);
   COUNT_LAUNCH();
+  if constexpr (sizeof(R) == 4 && N == 128) {
+    if (rv <= pruned_slots<N>()) {
+      constexpr int NZ = pruned_slots<N>();
+      if (a.variant == kFusedJointLean && sh.joint_lean_fits)
+        return launch_fused_v<R, N, true, NZ, kLeanJointThreads, 2, kModeLean>(a, grid, sh.smem_jl, st);
+      if (a.variant == kFusedSeparateLean && sh.sep_lean_fits)
+        return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeLean>(a, grid, sh.smem_sl, st);
+      if (a.variant == kFusedJointStaged && sh.joint_staged_fits)
+        return launch_fused_v<R, N, true, NZ, kFusedThreads, 2, kModeJointStaged>(a, grid, sh.smem_js, st);
+      if (a.variant == kFusedSeparateStaged && sh.sep_staged_fits)
+        return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeSepStaged>(a, grid, sh.smem_ss, st);
+    }
+  }
   if constexpr (sizeof(R) == 4 && N == 256) {
     // one CTA per SM (the 256-point row tile): 512 threads (32 teams, at most
     // 128 registers each) when the team scratch still fits beside the tile

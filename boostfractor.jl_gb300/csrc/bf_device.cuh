@@ -57,6 +57,10 @@ enum FusedVariant {
   kFusedSeparate = 1,   // slots propagated one after the other, 256 threads
   kFusedJoint = 2,      // joint steps (both slots' row tiles in shared memory), 256 threads
   kFusedWide = 3,       // slots one after the other, 512 threads (complex64, N = 256)
+  kFusedJointLean = 4,  // joint steps, 320 threads, 2 CTAs per SM, shared twiddles (complex64, N = 128)
+  kFusedSeparateLean = 5,  // slots one after the other, 256 threads, 3 CTAs per SM, shared twiddles (c64, N = 128)
+  kFusedJointStaged = 6,   // joint steps, 256 threads, phasor rows staged by cp.async (complex64, N = 128)
+  kFusedSeparateStaged = 7,  // as kFusedSeparateLean, phasor rows staged by cp.async (complex64, N = 128)
 };
 // The variants valid for a stage of this shape (kFusedRule first).
 std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64);

@@ -9,6 +9,8 @@
 // Afterwards thread g holds X[(g*C + j) + RR*q] in v[j*G + q].  The inverse is
 // the exact adjoint (same exchange, conjugate roots) and returns the points to
 // the x[g + G*r] layout, unnormalised (a factor N).
+// With C = 2 the exchange can also run in two halves through a scratch tile of
+// half the size (HALF): the same data movement, two more warp syncs.
 #pragma once
 
 #include "bf_common.cuh"
@@ -183,41 +185,79 @@ struct Team {
   // scratch tile of one team, in complex elements; the pad staggers the tiles
   // of teams sharing a half-warp across shared-memory banks
   static constexpr int SCR = RR * G + (G < 16 ? G : 0);
+  // the half-size tile of the two-half exchange: G rows of G points; the pad
+  // puts the two teams of a half-warp on opposite halves of the banks
+  static constexpr int SCRH = (RR / 2) * G + (G < 16 ? G : 0);
+  template <bool HALF> __host__ __device__ static constexpr int scratch() { return HALF ? SCRH : SCR; }
 
   __device__ static __forceinline__ int swz(int s, int g) { return s * G + (g ^ (s / C)); }
 
   // forward: v[r] = x[g + G r]  ->  v[j*G + q] = X[(g*C + j) + RR*q];
-  // NZ < RR: the caller guarantees v[NZ ..] == 0 (pruned first pass)
-  template <int NZ = RR, typename Cx>
-  __device__ static __forceinline__ void forward(Cx (&v)[RR], const Cx (&tw)[RR], Cx* scr, int g) {
+  // NZ < RR: the caller guarantees v[NZ ..] == 0 (pruned first pass);
+  // tw: the thread's RR inter-pass twiddles (registers or shared memory)
+  template <int NZ = RR, bool HALF = false, typename Cx>
+  __device__ static __forceinline__ void forward(Cx (&v)[RR], const Cx* tw, Cx* scr, int g) {
     reg_dft_nz<RR, false, NZ>(v);
 #pragma unroll
     for (int s = 1; s < RR; ++s) v[s] = cmul(v[s], tw[s]);
+    if constexpr (HALF) {
+      static_assert(C == 2, "two-half exchange");
+      // half j moves the points s = C t + j: row t, column g ^ t of the tile
+      Cx w[RR];
 #pragma unroll
-    for (int s = 0; s < RR; ++s) scr[swz(s, g)] = v[s];
-    __syncwarp();
+      for (int j = 0; j < C; ++j) {
 #pragma unroll
-    for (int j = 0; j < C; ++j)
+        for (int t = 0; t < G; ++t) scr[t * G + (g ^ t)] = v[C * t + j];
+        __syncwarp();
 #pragma unroll
-      for (int gp = 0; gp < G; ++gp) v[j * G + gp] = scr[swz(g * C + j, gp)];
-    __syncwarp();
+        for (int gp = 0; gp < G; ++gp) w[j * G + gp] = scr[g * G + (gp ^ g)];
+        __syncwarp();
+      }
+#pragma unroll
+      for (int s = 0; s < RR; ++s) v[s] = w[s];
+    } else {
+#pragma unroll
+      for (int s = 0; s < RR; ++s) scr[swz(s, g)] = v[s];
+      __syncwarp();
+#pragma unroll
+      for (int j = 0; j < C; ++j)
+#pragma unroll
+        for (int gp = 0; gp < G; ++gp) v[j * G + gp] = scr[swz(g * C + j, gp)];
+      __syncwarp();
+    }
 #pragma unroll
     for (int j = 0; j < C; ++j) reg_dft_sub<false>(v, j);
   }
 
   // inverse (adjoint of forward, unnormalised): v[j*G + q] = X[(g*C + j) + RR*q] -> v[r] = N x[g + G r]
-  template <typename Cx>
-  __device__ static __forceinline__ void inverse(Cx (&v)[RR], const Cx (&tw)[RR], Cx* scr, int g) {
+  template <bool HALF = false, typename Cx>
+  __device__ static __forceinline__ void inverse(Cx (&v)[RR], const Cx* tw, Cx* scr, int g) {
 #pragma unroll
     for (int j = 0; j < C; ++j) reg_dft_sub<true>(v, j);
+    if constexpr (HALF) {
+      static_assert(C == 2, "two-half exchange");
+      Cx w[RR];
 #pragma unroll
-    for (int j = 0; j < C; ++j)
+      for (int j = 0; j < C; ++j) {
 #pragma unroll
-      for (int gp = 0; gp < G; ++gp) scr[swz(g * C + j, gp)] = v[j * G + gp];
-    __syncwarp();
+        for (int gp = 0; gp < G; ++gp) scr[g * G + (gp ^ g)] = v[j * G + gp];
+        __syncwarp();
 #pragma unroll
-    for (int s = 0; s < RR; ++s) v[s] = scr[swz(s, g)];
-    __syncwarp();
+        for (int t = 0; t < G; ++t) w[C * t + j] = scr[t * G + (g ^ t)];
+        __syncwarp();
+      }
+#pragma unroll
+      for (int s = 0; s < RR; ++s) v[s] = w[s];
+    } else {
+#pragma unroll
+      for (int j = 0; j < C; ++j)
+#pragma unroll
+        for (int gp = 0; gp < G; ++gp) scr[swz(g * C + j, gp)] = v[j * G + gp];
+      __syncwarp();
+#pragma unroll
+      for (int s = 0; s < RR; ++s) v[s] = scr[swz(s, g)];
+      __syncwarp();
+    }
 #pragma unroll
     for (int s = 1; s < RR; ++s) v[s] = cmulc(v[s], tw[s]);
     reg_dft<RR, true, 0>(v);

@@ -439,8 +439,9 @@ const char* bf_server_last_error(const bf_server* s);
 
 /* ---- autotuner --------------------------------------------------------------- */
 /* No counterpart in the reference.  The first solve of each shape times the
- * fused stage kernel's variants (joint or separate slot propagation, 256, 384
- * or 512 threads, twiddles in registers or shared memory, 2 or 3 CTAs per SM;
+ * fused stage kernel's variants (joint or separate slot propagation, 256, 320
+ * or 512 threads, twiddles in registers or shared memory, 2 or 3 CTAs per SM,
+ * phasor rows read from L2 or staged in shared memory;
  * all give the same results bit for bit) on scratch copies of its largest
  * stage, and the tensor-core GEMM's K slicing (1, 2, 4 or 8 slices, for GEMMs
  * whose output tiles do not already fill the GPU), and keeps the fastest per
@@ -455,8 +456,10 @@ int bf_autotune_report(char* out, int cap);
 /* ---- test hooks ------------------------------------------------------------ */
 /* No counterpart in the reference.  Force one fused stage kernel variant
  * (0 = the rule, 1 = separate, 2 = joint, 3 = 512 threads, 4 = joint with
- * 384 threads and shared twiddles, 5 = separate at 3 CTAs per SM with shared
- * twiddles; a variant that does not apply to a stage's shape runs the rule;
+ * 320 threads and shared twiddles, 5 = separate at 3 CTAs per SM with shared
+ * twiddles, 6 = joint with phasor rows staged in shared memory, 7 = 5 with
+ * staged phasor rows; a variant that does not apply to a stage's shape runs
+ * the rule;
  * -1 = back to the autotuner) for every later solve of this process, to check
  * that they agree; returns the previous setting. */
 int bf_test_force_fused_variant(int variant);

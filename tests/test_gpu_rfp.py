@@ -344,9 +344,12 @@ def test_cheerleader_full_size_vs_oracle_fixture(B):
 @pytest.mark.parametrize("n,ndisk,nf", [(128, 3, 48), (256, 2, 24)])
 def test_fused_variants_agree_bit_for_bit(B, n, ndisk, nf):
     """The fused stage kernel's variants (the rule, separate slots, joint
-    slots, 512 threads at 256x256 complex64) give identical results, so the
-    autotuner's choice never changes a result; the autotuner logs a decision
-    for the shape."""
+    slots, 512 threads at 256x256 complex64, and at 128x128 complex64 the lean
+    ones: shared twiddles and two-half exchanges, joint at 320 threads or
+    separate at 3 CTAs per SM, and both with phasor rows staged by cp.async)
+    give identical results, so the autotuner's
+    choice never changes a result; the autotuner logs a decision for the
+    shape."""
     from bfgb300 import _lib
     L = _lib.lib()
     distance, eps, tx, ty, X, _ = _stack_case(n, ndisk, seed=23)
@@ -357,7 +360,7 @@ def test_fused_variants_agree_bit_for_bit(B, n, ndisk, nf):
     try:
         for prec in ("mixed", "fp64"):
             ref = None
-            for v in (0, 1, 2, 3):
+            for v in range(8):
                 L.bf_test_force_fused_variant(v)
                 R, _, b2 = st.cheerleader(freqs, nmax=10, precision=prec)
                 if ref is None:
