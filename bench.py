@@ -272,6 +272,9 @@ def run_ours(args):
         over["nmax"] = args.nmax
     w = workload(rank, **over)
     nf, nmax = len(w["freqs"]), w["nmax"]
+    if args.fused_variant is not None:
+        from bfgb300 import _lib
+        _lib.lib().bf_test_force_fused_variant(args.fused_variant)
     h = B.Handle(dev)
     stream = torch.cuda.current_stream()
     h.set_stream(stream.cuda_stream)
@@ -410,6 +413,9 @@ def run_ours(args):
         "e2e": {"value": nf / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "path": "bf_cheerleader (one-shot C ABI, pinned host buffers; stack upload, tables, solve, D2H)"},
         "clocks": clk,
+        # the fused-stage variant per stage shape (autotuner decisions, or the forced one)
+        "fused_variant": (f"forced {args.fused_variant}" if args.fused_variant is not None
+                          else [ln for ln in B.autotune_report() if ln.startswith("fused")]),
     }
     if ws == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(w)
@@ -1199,6 +1205,8 @@ def main():
     ap.add_argument("--nf", type=int, default=0, help="override frequency count (testing only)")
     ap.add_argument("--nmax", type=int, default=None, help="override nmax (testing only)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fused-variant", type=int, default=None,
+                    help="force one fused-stage kernel variant (0-8, bit-identical results; profiling only)")
     ap.add_argument("--workload", default="cheerleader",
                     choices=["cheerleader", "transformer", "uneven", "serve", "serve-opt", "serve-pgrid", "1d", "peaks",
                              "c1", "pgrid"])

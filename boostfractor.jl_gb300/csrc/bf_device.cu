@@ -824,15 +824,17 @@ template <int N> constexpr int pruned_slots() { return (5 * Team<N>::RR + 15) / 
 // Shape of one fused-stage launch: shared memory of the single and doubled
 // (joint) row tiles and whether the rule takes the joint path.
 struct FusedShape {
-  size_t smem, smem_j, smem512, smem_jl, smem_sl, smem_js, smem_ss;
+  size_t smem, smem_j, smem512, smem_jl, smem_sl, smem_js, smem_ss, smem_s5;
   bool joint_rule, joint_fits, wide_fits;
   // complex64, N = 128: joint steps with 320 threads at 2 CTAs per SM and
   // shared twiddles (lean), separate slots at 3 CTAs per SM and shared
   // twiddles (lean), joint steps with staged phasor rows, separate slots at 3
-  // CTAs per SM with shared twiddles and staged phasor rows
-  bool joint_lean_fits, sep_lean_fits, joint_staged_fits, sep_staged_fits;
+  // CTAs per SM with shared twiddles and staged phasor rows, separate slots
+  // with 20 teams (160 threads: 38 box rows in two rounds) at 3 CTAs per SM
+  // with staged phasor rows
+  bool joint_lean_fits, sep_lean_fits, joint_staged_fits, sep_staged_fits, sep5_staged_fits;
 };
-constexpr int kLeanJointThreads = 320;
+constexpr int kLeanJointThreads = 320, kSep5Threads = 160;
 constexpr int kModeLean = kModeTwShared | kModeHalf;
 constexpr int kModeJointStaged = kModeHalf | kModeStage;
 constexpr int kModeSepStaged = kModeTwShared | kModeHalf | kModeStage;
@@ -852,11 +854,13 @@ static FusedShape fused_shape(int nby, size_t csz) {
   f.smem_sl = fused_smem_for<N, kModeLean>(nby, csz, 1, kFusedThreads);
   f.smem_js = fused_smem_for<N, kModeJointStaged>(nby, csz, 2, kFusedThreads);
   f.smem_ss = fused_smem_for<N, kModeSepStaged>(nby, csz, 1, kFusedThreads);
+  f.smem_s5 = fused_smem_for<N, kModeJointStaged>(nby, csz, 1, kSep5Threads);
   const bool c128 = csz == 8 && N == 128;
   f.joint_lean_fits = c128 && 2 * (f.smem_jl + kSmemReservedPerCta) <= kSmemPerSM;
   f.sep_lean_fits = c128 && 3 * (f.smem_sl + kSmemReservedPerCta) <= kSmemPerSM;
   f.joint_staged_fits = c128 && 2 * (f.smem_js + kSmemReservedPerCta) <= kSmemPerSM;
   f.sep_staged_fits = c128 && 3 * (f.smem_ss + kSmemReservedPerCta) <= kSmemPerSM;
+  f.sep5_staged_fits = c128 && 3 * (f.smem_s5 + kSmemReservedPerCta) <= kSmemPerSM;
   return f;
 }
 
@@ -874,6 +878,7 @@ static std::vector<int> fused_variants_t(int nbx, int nby, bool fp64) {
   if (f.sep_lean_fits && pruned) v.push_back(kFusedSeparateLean);
   if (f.joint_staged_fits && pruned) v.push_back(kFusedJointStaged);
   if (f.sep_staged_fits && pruned) v.push_back(kFusedSeparateStaged);
+  if (f.sep5_staged_fits && pruned) v.push_back(kFusedSeparate160Staged);
   return v;
 }
 
@@ -928,6 +933,8 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
         return launch_fused_v<R, N, true, NZ, kFusedThreads, 2, kModeJointStaged>(a, grid, sh.smem_js, st);
       if (a.variant == kFusedSeparateStaged && sh.sep_staged_fits)
         return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeSepStaged>(a, grid, sh.smem_ss, st);
+      if (a.variant == kFusedSeparate160Staged && sh.sep5_staged_fits)
+        return launch_fused_v<R, N, false, NZ, kSep5Threads, 3, kModeJointStaged>(a, grid, sh.smem_s5, st);
     }
   }
   if constexpr (sizeof(R) == 4 && N == 256) {

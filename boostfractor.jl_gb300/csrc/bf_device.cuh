@@ -61,6 +61,7 @@ enum FusedVariant {
   kFusedSeparateLean = 5,  // slots one after the other, 256 threads, 3 CTAs per SM, shared twiddles (c64, N = 128)
   kFusedJointStaged = 6,   // joint steps, 256 threads, phasor rows staged by cp.async (complex64, N = 128)
   kFusedSeparateStaged = 7,  // as kFusedSeparateLean, phasor rows staged by cp.async (complex64, N = 128)
+  kFusedSeparate160Staged = 8,  // slots one after the other, 160 threads, 3 CTAs per SM, staged rows (c64, N = 128)
 };
 // The variants valid for a stage of this shape (kFusedRule first).
 std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64);

@@ -24,8 +24,7 @@
 //   * The first call on a device performs the set-up: with that device
 //     current it resolves the scratch's device address with
 //     cudaGetSymbolAddress (which also loads this module's device globals if
-//     the runtime deferred that) and caches it for the device.  Make that
-//     first call before any stream capture begins.
+//     the runtime deferred that) and caches it for the device.
 //   * The host arrays X, Y, kX, kY (and the surface map of the 3D kind) are
 //     copied into the scratch with cudaMemcpyAsync on the handle's stream.
 //     From pageable memory the runtime stages them before the call returns;

@@ -148,7 +148,7 @@ int bf_propagate(bf_handle* h, int prop_kind, int precision,
  * with cudaFree's implicit synchronisation.
  *   - nx, ny <= BF_NOALLOC_MAX_N; larger grids return BF_ERR_INVALID.
  *   - The first call on a device does the set-up (cudaGetSymbolAddress of the
- *     scratch with that device current); make it before any stream capture.
+ *     scratch with that device current) and caches the address.
  *   - One scratch per device for the whole process: overlapping calls (other
  *     streams, other threads) race on it; serialise them.
  * X, Y, kX, kY, surface are host arrays as in bf_propagate, copied on the
@@ -439,8 +439,8 @@ const char* bf_server_last_error(const bf_server* s);
 
 /* ---- autotuner --------------------------------------------------------------- */
 /* No counterpart in the reference.  The first solve of each shape times the
- * fused stage kernel's variants (joint or separate slot propagation, 256, 320
- * or 512 threads, twiddles in registers or shared memory, 2 or 3 CTAs per SM,
+ * fused stage kernel's variants (joint or separate slot propagation, 160,
+ * 256, 320 or 512 threads, twiddles in registers or shared memory, 2 or 3 CTAs per SM,
  * phasor rows read from L2 or staged in shared memory;
  * all give the same results bit for bit) on scratch copies of its largest
  * stage, and the tensor-core GEMM's K slicing (1, 2, 4 or 8 slices, for GEMMs
@@ -458,6 +458,7 @@ int bf_autotune_report(char* out, int cap);
  * (0 = the rule, 1 = separate, 2 = joint, 3 = 512 threads, 4 = joint with
  * 320 threads and shared twiddles, 5 = separate at 3 CTAs per SM with shared
  * twiddles, 6 = joint with phasor rows staged in shared memory, 7 = 5 with
+ * staged phasor rows, 8 = separate with 160 threads at 3 CTAs per SM and
  * staged phasor rows; a variant that does not apply to a stage's shape runs
  * the rule;
  * -1 = back to the autotuner) for every later solve of this process, to check

@@ -346,7 +346,8 @@ def test_fused_variants_agree_bit_for_bit(B, n, ndisk, nf):
     """The fused stage kernel's variants (the rule, separate slots, joint
     slots, 512 threads at 256x256 complex64, and at 128x128 complex64 the lean
     ones: shared twiddles and two-half exchanges, joint at 320 threads or
-    separate at 3 CTAs per SM, and both with phasor rows staged by cp.async)
+    separate at 3 CTAs per SM, and both with phasor rows staged by cp.async,
+    and separate slots with 160 threads at 3 CTAs per SM with staged rows)
     give identical results, so the autotuner's
     choice never changes a result; the autotuner logs a decision for the
     shape."""
@@ -360,7 +361,7 @@ def test_fused_variants_agree_bit_for_bit(B, n, ndisk, nf):
     try:
         for prec in ("mixed", "fp64"):
             ref = None
-            for v in range(8):
+            for v in range(9):
                 L.bf_test_force_fused_variant(v)
                 R, _, b2 = st.cheerleader(freqs, nmax=10, precision=prec)
                 if ref is None:
