@@ -836,8 +836,8 @@ struct FusedShape {
 };
 constexpr int kLeanJointThreads = 320, kSep5Threads = 160;
 constexpr int kModeLean = kModeTwShared | kModeHalf;
-constexpr int kModeJointStaged = kModeHalf | kModeStage;
-constexpr int kModeSepStaged = kModeTwShared | kModeHalf | kModeStage;
+constexpr int kModeHalfStaged = kModeHalf | kModeStage;
+constexpr int kModeLeanStaged = kModeTwShared | kModeHalf | kModeStage;
 template <int N>
 static FusedShape fused_shape(int nby, size_t csz) {
   FusedShape f;
@@ -852,9 +852,9 @@ static FusedShape fused_shape(int nby, size_t csz) {
   f.wide_fits = csz == 8 && N == 256 && f.smem512 <= kMaxSmem;
   f.smem_jl = fused_smem_for<N, kModeLean>(nby, csz, 2, kLeanJointThreads);
   f.smem_sl = fused_smem_for<N, kModeLean>(nby, csz, 1, kFusedThreads);
-  f.smem_js = fused_smem_for<N, kModeJointStaged>(nby, csz, 2, kFusedThreads);
-  f.smem_ss = fused_smem_for<N, kModeSepStaged>(nby, csz, 1, kFusedThreads);
-  f.smem_s5 = fused_smem_for<N, kModeJointStaged>(nby, csz, 1, kSep5Threads);
+  f.smem_js = fused_smem_for<N, kModeHalfStaged>(nby, csz, 2, kFusedThreads);
+  f.smem_ss = fused_smem_for<N, kModeLeanStaged>(nby, csz, 1, kFusedThreads);
+  f.smem_s5 = fused_smem_for<N, kModeHalfStaged>(nby, csz, 1, kSep5Threads);
   const bool c128 = csz == 8 && N == 128;
   f.joint_lean_fits = c128 && 2 * (f.smem_jl + kSmemReservedPerCta) <= kSmemPerSM;
   f.sep_lean_fits = c128 && 3 * (f.smem_sl + kSmemReservedPerCta) <= kSmemPerSM;
@@ -930,11 +930,11 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
       if (a.variant == kFusedSeparateLean && sh.sep_lean_fits)
         return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeLean>(a, grid, sh.smem_sl, st);
       if (a.variant == kFusedJointStaged && sh.joint_staged_fits)
-        return launch_fused_v<R, N, true, NZ, kFusedThreads, 2, kModeJointStaged>(a, grid, sh.smem_js, st);
+        return launch_fused_v<R, N, true, NZ, kFusedThreads, 2, kModeHalfStaged>(a, grid, sh.smem_js, st);
       if (a.variant == kFusedSeparateStaged && sh.sep_staged_fits)
-        return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeSepStaged>(a, grid, sh.smem_ss, st);
+        return launch_fused_v<R, N, false, NZ, kFusedThreads, 3, kModeLeanStaged>(a, grid, sh.smem_ss, st);
       if (a.variant == kFusedSeparate160Staged && sh.sep5_staged_fits)
-        return launch_fused_v<R, N, false, NZ, kSep5Threads, 3, kModeJointStaged>(a, grid, sh.smem_s5, st);
+        return launch_fused_v<R, N, false, NZ, kSep5Threads, 3, kModeHalfStaged>(a, grid, sh.smem_s5, st);
     }
   }
   if constexpr (sizeof(R) == 4 && N == 256) {
