@@ -693,7 +693,7 @@ def _size_class(r):
     return f"{r['solver']} {band} disks {r['n']}^2 {nfb} f"
 
 
-def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0):
+def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0, weights=None):
     """Open-loop arrivals: a Poisson process of `rate` requests/s for
     `seconds`, each arrival assigned to a uniformly drawn client; the
     dispatcher submits at the scheduled time whatever the state of earlier
@@ -702,13 +702,14 @@ def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0):
     server's submit-to-completion time plus the dispatcher's lag.  Completions
     are collected after the window (no polling thread competes with the
     dispatcher); requests still pending `drain_s` after the window are
-    counted as unfinished.  Returns (records, wall seconds from the first
+    counted as unfinished.  weights: the clients' shares of the arrivals
+    (default uniform).  Returns (records, wall seconds from the first
     arrival to the last completion, arrivals, unfinished, failed)."""
     import gc
     rng = np.random.default_rng(seed)
     n = int(rng.poisson(rate * seconds))
     t_arr = np.sort(rng.uniform(0.0, seconds, n))
-    who = rng.integers(0, nclients, n)
+    who = rng.integers(0, nclients, n) if weights is None else rng.choice(nclients, n, p=weights)
     sent = []
     gc.disable()   # no collector pause inside the dispatch loop
     try:
@@ -742,48 +743,76 @@ def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0):
     return recs, wall, n, unfinished, failed
 
 
+def _optimiser_requests(nclients):
+    """The optimiser class: 20-disk, 256-frequency transformer requests (8
+    Laguerre-Gauss modes, 128x128 over 1 m), one seeded booster per client."""
+    from bfgb300 import workloads as W
+    reqs = []
+    for k in range(nclients):
+        rng = np.random.default_rng(500 + k)
+        distance, eps, tx, ty = W.booster(20, rng.uniform(7.5e-3, 8.5e-3, 20))
+        reqs.append(dict(solver="transformer", ndisk=20, n=128, nf=256, distance=distance, eps=eps,
+                         relative_tilt_x=tx, relative_tilt_y=ty, X=W.symmetric_grid(128), diskR=0.15,
+                         freqs=np.linspace(19.5e9, 20.5e9, 256), nmax=0, M=8, waist=0.03))
+    return reqs
+
+
 def run_serve(args, optimiser_class=False):
     """Serving loop, open loop: boost-factor solves arrive as a Poisson
     process of mean rate --rate (2000 requests/s) for --serve-seconds; each
-    arrival is a step of one of 32 disk-position optimiser clients (drawn
-    uniformly), which moves that client's gaps by N(0, 10 um) and submits a
-    solve of its resident stack (bf_request.distance).  Stacks follow the
-    uneven-batch size distribution, or, with optimiser_class, are all
-    20-disk, 256-frequency transformer requests (8 Laguerre-Gauss modes,
-    128x128 over 1 m).  Latency percentiles are reported per request class."""
+    arrival is a step of one client, which moves that client's gaps by
+    N(0, 10 um) and submits a solve of its resident stack
+    (bf_request.distance).
+    - optimiser_class (serve-opt): 32 optimiser clients (20-disk,
+      256-frequency transformer requests), drawn uniformly.
+    - otherwise (serve, the configuration-4 mix): the same 32 optimiser
+      clients as interactive requests in the server's latency lane
+      (--lane-workers reserved workers on high-priority streams) plus 16
+      background clients whose stacks follow the uneven-batch distribution
+      (5-80 disks, 64/128/256 grids, 64-1024 frequencies, dancers and
+      transformers), at --bg-rate of the arrivals' rate.
+    Latency percentiles are reported per request class."""
     import torch
     torch.cuda.set_device(0)
     import build as _b
     _b.build()
     import bfgb300 as B
     from bfgb300 import workloads as W
-    nclients = 32
-    if optimiser_class:
-        reqs = []
-        for k in range(nclients):
-            rng = np.random.default_rng(500 + k)
-            distance, eps, tx, ty = W.booster(20, rng.uniform(7.5e-3, 8.5e-3, 20))
-            reqs.append(dict(solver="transformer", ndisk=20, n=128, nf=256, distance=distance, eps=eps,
-                             relative_tilt_x=tx, relative_tilt_y=ty, X=W.symmetric_grid(128), diskR=0.15,
-                             freqs=np.linspace(19.5e9, 20.5e9, 256), nmax=0, M=8, waist=0.03))
-    else:
-        reqs = W.config4_uneven(seed=5, count=nclients)
+    n_int = 32
+    reqs = _optimiser_requests(n_int)
+    lanes = [0] * n_int
+    classes = ["interactive: " + _size_class(r) for r in reqs] if not optimiser_class else \
+        [_size_class(r) for r in reqs]
+    n_bg = 0
+    if not optimiser_class:
+        bg = W.config4_uneven(seed=5, count=16)
+        n_bg = len(bg)
+        reqs = reqs + bg
+        lanes = [1] * n_int + [0] * n_bg
+        classes = classes + ["background: " + _size_class(r) for r in bg]
+    nclients = len(reqs)
     h = B.Handle(0)
     mode_cache = {}
     stacks = [_build_request_stack(B, W, h, r, mode_cache) for r in reqs]
-    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers)
+    n_lane = 0 if optimiser_class else args.lane_workers
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers + n_lane)
     try:
+        if n_lane:
+            srv.set_latency_lane(n_lane)
+
         # untimed warm-up on the serving server itself: one step per client
         # (builds the resident overlaps / plans), then two bursts of one step
-        # from every client at once (the group solves a burst forms and their
-        # one-time tuning); the statistics window starts after it
-        def warm(r, st, m):
+        # from every interactive client at once (the group solves a burst
+        # forms and their one-time tuning); the statistics window starts after it
+        def warm(k):
+            st, m = stacks[k]
+            r = reqs[k]
             return srv.submit(st, r["freqs"], r["solver"], modes=m, distance=r["distance"], nmax=r["nmax"],
-                              precision=args.serve_precision)
-        for (st, m), r in zip(stacks, reqs):
-            srv.wait(warm(r, st, m))
+                              precision=args.serve_precision, lane=lanes[k])
+        for k in range(nclients):
+            srv.wait(warm(k))
         for _ in range(2):
-            for i in [warm(r, st, m) for (st, m), r in zip(stacks, reqs)]:
+            for i in [warm(k) for k in range(n_int)]:
                 srv.wait(i)
         srv.reset_stats()
     except BaseException:
@@ -791,20 +820,25 @@ def run_serve(args, optimiser_class=False):
         raise
     rngs = [np.random.default_rng(1000 + k) for k in range(nclients)]
     dist = [np.array(r["distance"]) for r in reqs]
-    classes = [_size_class(r) for r in reqs]
+    weights = None
+    if n_bg:
+        # background arrivals at bg_rate / rate of all arrivals
+        pb = min(max(args.bg_rate / args.rate, 0.0), 1.0)
+        weights = np.array([(1.0 - pb) / n_int] * n_int + [pb / n_bg] * n_bg)
 
     def submit_one(k):
         dist[k] = W.optimiser_step(dist[k], rngs[k])
         st, m = stacks[k]
         r = reqs[k]
         return srv.submit(st, r["freqs"], r["solver"], modes=m, distance=dist[k], nmax=r["nmax"],
-                          precision=args.serve_precision), classes[k]
+                          precision=args.serve_precision, lane=lanes[k]), classes[k]
 
     try:
         clock = ClockSampler(0)
         clock.start()
         recs, wall, n_arr, unfinished, failed = _open_loop(srv, nclients, args.rate, args.serve_seconds,
-                                                           submit_one)
+                                                           submit_one, weights=weights,
+                                                           drain_s=20.0 if optimiser_class else 120.0)
         clocks = clock.stop()
         st_all, st_d, st_t = srv.stats(), srv.stats("dancer"), srv.stats("transformer")
     finally:
@@ -818,16 +852,22 @@ def run_serve(args, optimiser_class=False):
         per_class[cl] = {"requests": int(len(v)), "p50_ms": float(np.percentile(v, 50)),
                          "p99_ms": float(np.percentile(v, 99)), "max_ms": float(v.max())}
     fpts = float(sum(len(reqs[r["client"]]["freqs"]) for r in recs))
-    name = ("20-disk 256-frequency transformer requests (8 LG modes, 128x128)" if optimiser_class
-            else "stacks of the uneven-batch distribution")
+    if optimiser_class:
+        metric = (f"beta2 freq-points/s and p50/p99 latency, Poisson arrivals at {args.rate:g}/s from 32 "
+                  f"optimiser clients, 20-disk 256-frequency transformer requests (8 LG modes, 128x128)")
+        workload = "serve-optimiser-class"
+    else:
+        metric = (f"beta2 freq-points/s and per-class p50/p99 latency, Poisson arrivals at {args.rate:g}/s: 32 "
+                  f"optimiser clients (20-disk 256-frequency transformer, latency lane) and 16 clients of the "
+                  f"uneven-batch distribution ({args.bg_rate:g}/s)")
+        workload = "serve-configuration-4-mix"
     _server_line(
-        f"beta2 freq-points/s and p50/p99 latency, Poisson arrivals at {args.rate:g}/s from 32 optimiser clients, "
-        f"{name}",
-        fpts / wall, len(recs), wall,
-        {"config": {"workload": "serve-optimiser-class" if optimiser_class else "serve-uneven-mix",
-                    "arrivals": "poisson", "rate_per_s": args.rate, "clients": nclients,
-                    "seconds": args.serve_seconds, "workers": args.workers, "hbm_budget_gb": 180,
-                    "gap_step_um": 10, "precision": args.serve_precision},
+        metric, fpts / wall, len(recs), wall,
+        {"config": {"workload": workload, "arrivals": "poisson", "rate_per_s": args.rate,
+                    "clients": nclients, "background_clients": n_bg,
+                    "background_rate_per_s": args.bg_rate if n_bg else 0.0,
+                    "seconds": args.serve_seconds, "workers": args.workers, "lane_workers": n_lane,
+                    "hbm_budget_gb": 180, "gap_step_um": 10, "precision": args.serve_precision},
          "offered": n_arr, "completed": len(recs), "unfinished_after_drain": unfinished, "failed": failed,
          "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                         "mean": float(lat.mean()), "max": float(lat.max())},
@@ -1212,6 +1252,10 @@ def main():
                              "c1", "pgrid"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
+    ap.add_argument("--lane-workers", type=int, default=2,
+                    help="serve: workers reserved, on high-priority streams, for the interactive clients")
+    ap.add_argument("--bg-rate", type=float, default=1.0,
+                    help="serve: arrivals per second of the uneven-batch background clients")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: mean Poisson arrival rate, requests/s")
     ap.add_argument("--serve-precision", default="mixed", help="serving: precision of the transformer requests")

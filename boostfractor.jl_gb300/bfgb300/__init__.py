@@ -883,11 +883,12 @@ class Server:
             raise BFError(rc, msg.decode() if msg else "")
 
     def submit(self, stack, freqs, solver="cheerleader", modes=None, distance=None, nmax=400, prop=None,
-               precision="mixed", beta2_scale=0.0, want_boost=False, footprint_bytes=0, pgrid=None):
+               precision="mixed", beta2_scale=0.0, want_boost=False, footprint_bytes=0, pgrid=None, lane=0):
         """Queue one solve; returns its id.  ``stack`` is a Stack (or, dry-run, any
         non-zero integer token), ``distance`` the stack's new region distances.
         solver="pgrid": ``pgrid`` is a PGrid, ``stack`` may be None (the grid's),
-        ``freqs`` the grid's frequencies and ``distance`` the per-disk shifts."""
+        ``freqs`` the grid's frequencies and ``distance`` the per-disk shifts.
+        lane=1 marks an interactive request (see set_latency_lane)."""
         if pgrid is not None:
             stack = pgrid.stack if stack is None else stack
             modes = None
@@ -911,6 +912,7 @@ class Server:
         q.out_boost = _lib.ptr(None if boost is None else boost.view(np.float64))
         q.footprint_bytes = int(footprint_bytes)
         q.pgrid = pgrid._g if pgrid is not None else None
+        q.lane = int(lane)
         rid = _lib._ull()
         self._check(_lib.lib().bf_submit(self._p, ctypes.byref(q), ctypes.byref(rid)))
         self._live[rid.value] = (q, fr, dist, b2, boost)
@@ -950,6 +952,11 @@ class Server:
         keys = ["completed", "failed", "freq_points", "p50_ms", "p99_ms", "mean_ms", "max_ms", "wall_s",
                 "batched", "evictions"]
         return dict(zip(keys, out.tolist()))
+
+    def set_latency_lane(self, n_lane):
+        """Reserve the last n_lane workers, on high-priority streams, for
+        requests submitted with lane=1 (before the first submit)."""
+        self._check(_lib.lib().bf_server_set_latency_lane(self._p, int(n_lane)))
 
     def reset_stats(self):
         """Start a new statistics window (after warm-up requests)."""

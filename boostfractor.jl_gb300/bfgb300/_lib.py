@@ -51,7 +51,7 @@ class BFRequest(ctypes.Structure):
     _fields_ = [("solver", _c_int), ("stack", _vp), ("modes", _vp), ("nf", _c_int), ("freqs", _p_dbl),
                 ("distance", _p_dbl), ("nmax", _c_int), ("prop_kind", _c_int), ("precision", _c_int),
                 ("beta2_scale", _c_dbl), ("out_beta2", _p_dbl), ("out_boost", _p_dbl),
-                ("footprint_bytes", _ull), ("pgrid", _vp)]
+                ("footprint_bytes", _ull), ("pgrid", _vp), ("lane", _c_int)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/boostfractor_gb300.h
@@ -92,6 +92,7 @@ _SIGS = {
     "bf_wait": (_c_int, [_vp, _ull, _c_int, ctypes.POINTER(_c_int), _p_dbl]),
     "bf_server_stats": (_c_int, [_vp, _c_int, _p_dbl]),
     "bf_server_reset_stats": (_c_int, [_vp]),
+    "bf_server_set_latency_lane": (_c_int, [_vp, _c_int]),
     "bf_server_last_error": (ctypes.c_char_p, [_vp]),
     "bf_stack_create": (_c_int, [_vp, _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_int,
                                  _c_int, _p_dbl, _p_dbl, _p_dbl, _p_dbl, _c_dbl, ctypes.POINTER(_vp)]),

@@ -83,9 +83,10 @@ bool split_stage(int nsteps, int nfreq);
 // holding TF32-rounded hi/lo parts, M a multiple of 128, Kp of 32, bases
 // 16-byte aligned.  The tensor-memory accumulator is drained into FP32
 // registers every 32 K-elements.  *d_err becomes non-zero if a bounded wait in
-// the kernel expired.
+// the kernel expired.  max_ctas > 0 caps the persistent grid (SMs left to
+// other streams); 0 = one CTA per SM.
 int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
-                   int splits, float* out, int* d_err, cudaStream_t st);
+                   int splits, float* out, int* d_err, cudaStream_t st, int max_ctas = 0);
 // True when the output tiles of an M x N product alone give every SM about
 // four tiles (K slicing then only adds output traffic).
 bool tc_gemm_fills_gpu(int M, int N);

@@ -23,6 +23,7 @@ struct bf_handle {
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t user_stream = nullptr;  // set by bf_set_stream; work goes there when non-null
+  int sm_cap = 0;   // > 0: persistent kernels launch at most this many CTAs (SMs left to other streams)
   unsigned long long budget = 0;       // 0 = unlimited
   unsigned long long used = 0;
   std::unordered_map<void*, size_t> allocs;

@@ -23,6 +23,8 @@
 //     transformer requests on different stacks that differ only in their air
 //     gaps (the steps of several disk-position optimisers) join one group
 //     solve (bf_transformer_group), up to kMaxGroup requests;
+//   * latency lane (bf_server_set_latency_lane): the last workers take only
+//     requests marked lane = 1, on high-priority streams;
 //   * completion: beta^2 (and the transformer boost) are copied to the caller's
 //     buffers, then the status becomes final; bf_poll / bf_wait report it.
 #include <algorithm>
@@ -79,6 +81,8 @@ struct bf_server {
   unsigned long long budget = 0;
   std::vector<bf_handle*> hs;
   std::vector<std::thread> th;
+  int n_workers = 0, n_lane = 0;            // the last n_lane workers serve lane 1 only
+  std::vector<cudaStream_t> lane_streams;   // their high-priority streams
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<Req*> queue;
@@ -107,9 +111,10 @@ int server_fail(bf_server* s, int code, const std::string& msg) {
 }
 
 // Release the workspace of idle stacks, least recently used first, until
-// `need` more bytes fit the budget.  Caller holds the lock.
-bool make_room(bf_server* S, size_t need, const bf_stack* keep) {
-  while (S->resident + S->inflight + need > S->budget) {
+// `need` more bytes fit under `cap` (the budget, or the normal requests' part
+// of it).  Caller holds the lock.
+bool make_room(bf_server* S, size_t need, const bf_stack* keep, size_t cap) {
+  while (S->resident + S->inflight + need > cap) {
     bf_stack* victim = nullptr;
     double oldest = 1e300;
     for (auto& kv : S->stacks)
@@ -155,21 +160,27 @@ bool mergeable(const Req* a, const Req* b) {
          a->r.beta2_scale == b->r.beta2_scale;
 }
 
-// The next batch worker w may start, or an empty batch.  Caller holds the lock.
 // Whether request R's stack holds workspace on a worker other than w.
 bool bound_elsewhere(const StackInfo& si, const Req* R, int w) {
   return R->r.solver != BF_SOLVER_TRANSFORMER && si.home >= 0 && si.home != w;
 }
 
+// The next batch worker w may start, or an empty batch.  Caller holds the lock.
 Batch pick(bf_server* S, int w) {
   Batch b;
+  const bool lane_worker = w >= S->n_workers - S->n_lane;
+  // with a latency lane, normal requests use at most 7/8 of the budget, so
+  // that the lane's (small) requests are never held back for memory
+  const size_t normal_cap = S->n_lane ? S->budget - S->budget / 8 : S->budget;
   for (size_t qi = 0; qi < S->queue.size(); ++qi) {
     Req* R = S->queue[qi];
+    if (lane_worker && R->r.lane == 0) continue;
     StackInfo& si = S->stacks[R->r.stack];
     if (si.busy || bound_elsewhere(si, R, w)) continue;
+    const size_t cap = R->r.lane ? S->budget : normal_cap;
     // the workspace the stack already holds is reused by the solve
     const size_t need = R->est > si.resident ? R->est - si.resident : 0;
-    if (!make_room(S, need, R->r.stack)) {
+    if (!make_room(S, need, R->r.stack, cap)) {
       if (++R->passed_over > kMaxPassOver) return b;  // hold the line for it
       continue;
     }
@@ -182,7 +193,7 @@ Batch pick(bf_server* S, int w) {
       Req* Q = S->queue[qj];
       if (Q->r.stack != R->r.stack) continue;
       if (!mergeable(R, Q) || nf + Q->r.nf > kMaxBatchFreqs) break;
-      if (S->resident + S->inflight + b.need + Q->est > S->budget) break;
+      if (S->resident + S->inflight + b.need + Q->est > cap) break;
       b.reqs.push_back(Q);
       b.need += Q->est;
       nf += Q->r.nf;
@@ -192,21 +203,23 @@ Batch pick(bf_server* S, int w) {
     // a lone transformer request gathers the queued steps of other stacks
     // that can share its solve
     if (b.reqs.size() == 1 && R->r.solver == BF_SOLVER_TRANSFORMER) {
+      // the queue position of each stack's first queued request (one pass,
+      // so that a long queue costs linear time here, not quadratic)
+      std::unordered_map<const bf_stack*, size_t> first;
+      first.reserve(S->stacks.size());
+      for (size_t qk = 0; qk < S->queue.size(); ++qk) first.emplace(S->queue[qk]->r.stack, qk);
       for (size_t qj = qi + 1; qj < S->queue.size() && (int)b.reqs.size() < kMaxGroup; ++qj) {
         Req* Q = S->queue[qj];
-        if (!groupable(S, R, Q)) continue;
+        if (!groupable(S, R, Q) || (lane_worker && Q->r.lane == 0)) continue;
         bool dup = false;
         for (Req* G : b.reqs) dup |= G->r.stack == Q->r.stack;
         if (dup) continue;
         StackInfo& qs = S->stacks[Q->r.stack];
         if (qs.busy) continue;
         // an earlier queued request on Q's stack keeps its turn
-        bool earlier = false;
-        for (size_t qk = 0; qk < qj && !earlier; ++qk)
-          earlier = S->queue[qk] != R && S->queue[qk]->r.stack == Q->r.stack;
-        if (earlier) continue;
+        if (first[Q->r.stack] != qj) continue;
         const size_t qneed = Q->est > qs.resident ? Q->est - qs.resident : 0;
-        if (S->resident + S->inflight + b.need + qneed > S->budget) break;
+        if (S->resident + S->inflight + b.need + qneed > cap) break;
         b.reqs.push_back(Q);
         b.need += qneed;
         Q->in_batch = 1;
@@ -446,6 +459,7 @@ extern "C" int bf_server_create(int device, unsigned long long hbm_budget_bytes,
   } else if (!S->budget) {
     S->budget = ~0ull;
   }
+  S->n_workers = n_workers;
   for (int w = 0; w < n_workers; ++w) S->th.emplace_back(worker, S, w);
   *out = S;
   return BF_OK;
@@ -472,6 +486,7 @@ extern "C" int bf_server_destroy(bf_server* S) {
   if (!S->dry())
     for (auto& kv : S->stacks) bf_stack_trim(kv.first);
   for (bf_handle* h : S->hs) bf_destroy(h);
+  for (cudaStream_t st : S->lane_streams) cudaStreamDestroy(st);
   for (auto& kv : S->reqs) delete kv.second;
   delete S;
   return BF_OK;
@@ -499,6 +514,7 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
     return server_fail(S, BF_ERR_INVALID, "unknown precision for this solver");
   if (S->dry() && !q->footprint_bytes)
     return server_fail(S, BF_ERR_INVALID, "a dry-run request needs footprint_bytes");
+  if (q->lane != 0 && q->lane != 1) return server_fail(S, BF_ERR_INVALID, "lane must be 0 or 1");
   Req* R = new Req();
   R->r = *q;
   R->freqs.assign(q->freqs, q->freqs + q->nf);
@@ -544,11 +560,13 @@ extern "C" int bf_submit(bf_server* S, const bf_request* q, unsigned long long* 
     delete R;
     return server_fail(S, BF_ERR_INVALID, "server is shutting down");
   }
-  if (R->est > S->budget) {
+  const size_t cap = (S->n_lane && R->r.lane == 0) ? S->budget - S->budget / 8 : S->budget;
+  if (R->est > cap) {
     const size_t est = R->est;
     delete R;
     return server_fail(S, BF_ERR_NOMEM, "request footprint of " + std::to_string(est) +
-                                            " bytes exceeds the server's HBM budget");
+                                            " bytes exceeds the server's HBM budget" +
+                                            (cap < S->budget ? " less the latency lane's eighth" : ""));
   }
   R->id = S->next_id++;
   R->t_submit = S->now();
@@ -617,6 +635,47 @@ extern "C" int bf_server_stats(bf_server* S, int solver, double* out) {
   out[7] = S->t_first < 0 ? 0.0 : S->t_last - S->t_first;
   out[8] = nb;
   out[9] = (double)S->evictions;
+  return BF_OK;
+}
+
+extern "C" int bf_server_set_latency_lane(bf_server* S, int n_lane) {
+  if (!S) return BF_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  if (n_lane < 1 || n_lane >= S->n_workers)
+    return server_fail(S, BF_ERR_INVALID, "the latency lane needs 1 .. n_workers - 1 workers");
+  if (S->n_lane != 0 || S->next_id != 1)
+    return server_fail(S, BF_ERR_INVALID, "set the latency lane once, before the first request");
+  if (!S->dry()) {
+    if (cudaSetDevice(S->device) != cudaSuccess) {
+      cudaGetLastError();
+      return server_fail(S, BF_ERR_CUDA, "cudaSetDevice");
+    }
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) {
+      cudaGetLastError();
+      return server_fail(S, BF_ERR_CUDA, "cudaDeviceGetStreamPriorityRange");
+    }
+    // the persistent tensor-core GEMM of the normal workers leaves the lane's
+    // share of the SMs free, so a lane kernel never waits for a whole GEMM
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, S->device) != cudaSuccess || sms < 2) {
+      cudaGetLastError();
+      sms = 0;
+    }
+    const int reserve = sms ? std::max(1, sms * n_lane / S->n_workers) : 0;
+    for (int w = 0; w < S->n_workers - n_lane && sms; ++w) S->hs[w]->sm_cap = sms - reserve;
+    // the workers are idle (no request yet), so their handles may change streams
+    for (int k = 0; k < n_lane; ++k) {
+      cudaStream_t st = nullptr;
+      if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+        cudaGetLastError();
+        return server_fail(S, BF_ERR_CUDA, "cudaStreamCreateWithPriority");
+      }
+      S->lane_streams.push_back(st);
+      bf_set_stream(S->hs[S->n_workers - n_lane + k], st);
+    }
+  }
+  S->n_lane = n_lane;
   return BF_OK;
 }
 

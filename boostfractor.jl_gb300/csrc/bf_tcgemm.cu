@@ -393,7 +393,7 @@ int tc_gemm_splits(int M, int N, int Kp) {
 }
 
 int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const float* Blo, int M, int N, int Kp,
-                   int splits, float* out, int* d_err, cudaStream_t st) {
+                   int splits, float* out, int* d_err, cudaStream_t st, int max_ctas) {
   if (Kp % kTK || M % kTM || M < kTM || N < 1 || splits < 1) return (int)cudaErrorInvalidValue;
   // TMA: 16-byte aligned bases (pool allocations) and row strides
   for (const float* p : {Ahi, Alo, Bhi, Blo})
@@ -411,7 +411,9 @@ int tc_gemm_tf32x3(const float* Ahi, const float* Alo, const float* Bhi, const f
   const size_t smem = tc_gemm_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(k_tc_gemm_tf32x3, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  const int grid = std::min(units, sm_count());
+  // persistent CTAs: one per SM, or fewer when the caller leaves SMs to
+  // other streams (a serving engine's latency lane)
+  const int grid = std::min(units, max_ctas > 0 ? std::min(max_ctas, sm_count()) : sm_count());
   note_launch();
   k_tc_gemm_tf32x3<<<grid, kThreads, smem, st>>>(mAhi, mAlo, mBhi, mBlo, out, M, N, ktiles, per, mt, nt, units,
                                                  g_withhold.load() ? 1 : 0, d_err);

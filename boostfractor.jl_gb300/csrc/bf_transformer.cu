@@ -1888,7 +1888,7 @@ static int tc_pick_splits(bf_handle* h, const float* Ah, const float* Al, int Mp
       float tv = 1e30f;
       for (int rep = 0; rep < 3; ++rep) {   // the first run warms up
         cudaEventRecord(e0, st);
-        const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, sp, tmp.as<float>(), d_err, st);
+        const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, sp, tmp.as<float>(), d_err, st, h->sm_cap);
         cudaEventRecord(e1, st);
         if (e || cudaEventSynchronize(e1) != cudaSuccess) {
           tv = 1e30f;
@@ -1925,7 +1925,7 @@ static int tc_class_gemm(bf_handle* h, const float* Ah, const float* Al, int Mp,
   TCKS(tc_pick_splits(h, Ah, Al, Mp, Kp, Bh, Bl, nrows_b, d_err, splits));
   TCKS(out.alloc(h, sizeof(float) * (size_t)*splits * nrows_b * Mp));
   gemm_ev_begin(h);
-  const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, *splits, out.as<float>(), d_err, st);
+  const int e = bf::tc_gemm_tf32x3(Ah, Al, Bh, Bl, Mp, nrows_b, Kp, *splits, out.as<float>(), d_err, st, h->sm_cap);
   gemm_ev_end(h);
   if (e) return bf_fail(h, BF_ERR_CUDA, std::string("tensor-core GEMM: ") + cudaGetErrorString((cudaError_t)e));
   return BF_OK;

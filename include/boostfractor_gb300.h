@@ -410,6 +410,7 @@ typedef struct bf_request {
   double* out_boost;           /* transformer: host nf x nm complex, or NULL */
   unsigned long long footprint_bytes;  /* 0 = the server's estimate */
   bf_pgrid* pgrid;             /* BF_SOLVER_PGRID: the grid (its stack is `stack`); else NULL */
+  int lane;                    /* 0 = normal, 1 = latency lane (bf_server_set_latency_lane) */
 } bf_request;
 
 int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_workers, int flags,
@@ -417,6 +418,16 @@ int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_work
 /* Cancels queued requests (status BF_ERR_INVALID), waits for running ones,
  * releases the workspaces grown on served stacks and the workers. */
 int bf_server_destroy(bf_server* s);
+/* No counterpart in the reference.  Reserves the last n_lane workers (at
+ * least one worker stays normal) for requests with lane = 1, on streams of
+ * the device's highest priority, so that short interactive requests (an
+ * optimiser's steps) are not queued behind long ones and their kernels are
+ * scheduled ahead of those of the other workers; the persistent tensor-core
+ * GEMM of the normal workers then leaves the lane's share of the SMs
+ * (n_lane / n_workers) free, and normal requests are admitted within 7/8 of
+ * the HBM budget (the last eighth is the lane's).  Normal workers still take
+ * lane-1 requests when idle.  Call once, before the first bf_submit. */
+int bf_server_set_latency_lane(bf_server* s, int n_lane);
 int bf_submit(bf_server* s, const bf_request* req, unsigned long long* id);
 /* Non-blocking: *status = BF_PENDING, or the request's final status (BF_OK or
  * an error code).  Reporting a final status releases the id.  times (NULL or

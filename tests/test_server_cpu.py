@@ -195,3 +195,54 @@ def test_reset_stats_starts_a_new_window(B):
         assert s["completed"] == 1 and s["freq_points"] == 1
     finally:
         srv.close()
+
+
+def test_latency_lane_workers_take_only_lane_requests(B):
+    """With one of two workers reserved for lane 1, a second long normal
+    request waits for the first (the lane worker does not take it), while a
+    lane-1 request starts at once on the reserved worker."""
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        srv.set_latency_lane(1)
+        with pytest.raises(Exception):
+            srv.set_latency_lane(1)   # once only
+        first = srv.submit(0xF000, [1e10], nmax=100000, footprint_bytes=MB)
+        time.sleep(0.01)
+        second = srv.submit(0xF010, [1e10], nmax=100000, footprint_bytes=MB)
+        fast = srv.submit(0xF020, [1e10], nmax=1000, footprint_bytes=MB, lane=1)
+        rf, r1, r2 = (srv.wait(i, timeout_ms=20000) for i in (fast, first, second))
+        assert r2["t_start"] >= r1["t_done"]
+        assert rf["t_done"] < r1["t_done"]
+    finally:
+        srv.close()
+
+
+def test_latency_lane_needs_a_normal_worker_and_a_valid_lane(B):
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        with pytest.raises(Exception):
+            srv.set_latency_lane(2)
+        with pytest.raises(Exception):
+            srv.submit(0xF100, [1e10], nmax=10, footprint_bytes=MB, lane=2)
+    finally:
+        srv.close()
+
+
+def test_latency_lane_keeps_an_eighth_of_the_budget(B):
+    """With a latency lane, normal requests are admitted within 7/8 of the
+    budget: one that needs more is refused at submit, and while a normal
+    request holds 7/8, a lane request still starts at once."""
+    srv = B.Server(hbm_budget_bytes=800 * MB, n_workers=3, dry_run=True)
+    try:
+        srv.set_latency_lane(1)
+        with pytest.raises(Exception):
+            srv.submit(0xF200, [1e10], nmax=10, footprint_bytes=750 * MB)   # > 700 MB
+        big = srv.submit(0xF210, [1e10], nmax=100000, footprint_bytes=700 * MB)
+        time.sleep(0.01)
+        other = srv.submit(0xF220, [1e10], nmax=1000, footprint_bytes=50 * MB)   # waits for memory
+        fast = srv.submit(0xF230, [1e10], nmax=1000, footprint_bytes=50 * MB, lane=1)
+        rb, ro, rf = (srv.wait(i, timeout_ms=20000) for i in (big, other, fast))
+        assert rf["t_done"] < rb["t_done"]
+        assert ro["t_start"] >= rb["t_done"]
+    finally:
+        srv.close()
