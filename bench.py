@@ -718,9 +718,11 @@ def _open_loop(srv, nclients, rate, seconds, submit_one, seed=77, drain_s=20.0, 
             dt = t0 + t_arr[i] - time.perf_counter()
             if dt > 0:
                 time.sleep(dt)
-            lag = time.perf_counter() - (t0 + t_arr[i])
+            t_s = time.perf_counter()
+            lag = t_s - (t0 + t_arr[i])
             rid, cls = submit_one(int(who[i]))
-            sent.append((rid, {"client": int(who[i]), "cls": cls, "lag_s": lag}))
+            sent.append((rid, {"client": int(who[i]), "cls": cls, "lag_s": lag,
+                               "submit_s": time.perf_counter() - t_s}))
     finally:
         gc.enable()
     deadline = time.perf_counter() + drain_s
@@ -795,7 +797,8 @@ def run_serve(args, optimiser_class=False):
     mode_cache = {}
     stacks = [_build_request_stack(B, W, h, r, mode_cache) for r in reqs]
     n_lane = 0 if optimiser_class else args.lane_workers
-    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers + n_lane)
+    srv = B.Server(0, hbm_budget_bytes=int(180e9), n_workers=args.workers + n_lane,
+                   reserve_hbm=not optimiser_class)
     try:
         if n_lane:
             srv.set_latency_lane(n_lane)
@@ -875,6 +878,8 @@ def run_serve(args, optimiser_class=False):
          "requests_per_s": len(recs) / wall, "per_solver": {"dancer": st_d, "transformer": st_t},
          "dispatch_lag_ms_p99": float(np.percentile([1e3 * r["lag_s"] for r in recs], 99)) if recs else None,
          "dispatch_lag_ms_max": float(max(1e3 * r["lag_s"] for r in recs)) if recs else None,
+         "submit_call_ms_p99": float(np.percentile([1e3 * r["submit_s"] for r in recs], 99)) if recs else None,
+         "submit_call_ms_max": float(max(1e3 * r["submit_s"] for r in recs)) if recs else None,
          "evictions": st_all["evictions"], "batched": st_all.get("batched"), "clocks": clocks})
 
 
@@ -1252,7 +1257,7 @@ def main():
                              "c1", "pgrid"])
     ap.add_argument("--requests", type=int, default=24, help="uneven batch: requests of the seeded 4096")
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
-    ap.add_argument("--lane-workers", type=int, default=2,
+    ap.add_argument("--lane-workers", type=int, default=3,
                     help="serve: workers reserved, on high-priority streams, for the interactive clients")
     ap.add_argument("--bg-rate", type=float, default=1.0,
                     help="serve: arrivals per second of the uneven-batch background clients")

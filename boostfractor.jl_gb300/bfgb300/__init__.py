@@ -864,13 +864,14 @@ class Server:
     streams, admitted by device footprint against ``hbm_budget_bytes``
     (0 = the device's free memory).  ``dry_run`` schedules without device
     work (a request takes ``nmax`` microseconds and holds ``footprint_bytes``),
-    for exercising the scheduler without a GPU."""
+    for exercising the scheduler without a GPU.  ``reserve_hbm`` maps the
+    budget into the device pool at creation (BF_SERVER_RESERVE_HBM)."""
 
-    def __init__(self, device=0, hbm_budget_bytes=0, n_workers=4, dry_run=False):
+    def __init__(self, device=0, hbm_budget_bytes=0, n_workers=4, dry_run=False, reserve_hbm=False):
         L = _lib.lib()
         p = _lib._vp()
-        rc = L.bf_server_create(int(device), int(hbm_budget_bytes), int(n_workers),
-                                _lib.BF_SERVER_DRYRUN if dry_run else 0, ctypes.byref(p))
+        flags = (_lib.BF_SERVER_DRYRUN if dry_run else 0) | (_lib.BF_SERVER_RESERVE_HBM if reserve_hbm else 0)
+        rc = L.bf_server_create(int(device), int(hbm_budget_bytes), int(n_workers), flags, ctypes.byref(p))
         if rc != _lib.BF_OK:
             raise BFError(rc, "bf_server_create failed")
         self._p = p

@@ -44,6 +44,7 @@ BF_SOLVER_TRANSFORMER = 2
 BF_SOLVER_PGRID = 3
 BF_PENDING = -1
 BF_SERVER_DRYRUN = 1
+BF_SERVER_RESERVE_HBM = 2
 
 
 class BFRequest(ctypes.Structure):

@@ -120,6 +120,22 @@ int bf_dalloc(bf_handle* h, void** p, size_t bytes) {
   return BF_OK;
 }
 
+// Grow the device pool to hold `bytes`: allocated and freed at once on h's
+// stream (the pool keeps freed memory), so that later allocations are served
+// from memory already mapped.
+int bf_pool_reserve(bf_handle* h, size_t bytes) {
+  cudaMemPool_t pool = device_pool(h->device);
+  if (!pool || !bytes) return BF_OK;
+  void* p = nullptr;
+  if (cudaMallocFromPoolAsync(&p, bytes, pool, h->stream()) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(h, BF_ERR_NOMEM, "reserving " + std::to_string(bytes) + " bytes in the device pool");
+  }
+  CK(cudaFreeAsync(p, h->stream()));
+  CK(cudaStreamSynchronize(h->stream()));
+  return BF_OK;
+}
+
 void bf_dfree(bf_handle* h, void* p) {
   if (!p) return;
   std::lock_guard<std::mutex> lock(h->alloc_mu);

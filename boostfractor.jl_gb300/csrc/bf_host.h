@@ -162,6 +162,7 @@ size_t bf_stack_device_bytes(const bf_stack* s);
 // Release a stack's workspace and transformer cache (the geometry stays); the
 // next solve rebuilds them.  The stack must be idle.
 void bf_stack_trim(bf_stack* s);
+int bf_pool_reserve(bf_handle* h, size_t bytes);
 // Upper bound of the device bytes one solve adds to a stack (workspace,
 // per-call buffers, outputs): solver 0 cheerleader, 1 dancer, 2 transformer
 // with nm modes.

@@ -23,8 +23,8 @@
 //     transformer requests on different stacks that differ only in their air
 //     gaps (the steps of several disk-position optimisers) join one group
 //     solve (bf_transformer_group), up to kMaxGroup requests;
-//   * latency lane (bf_server_set_latency_lane): the last workers take only
-//     requests marked lane = 1, on high-priority streams;
+//   * latency lane (bf_server_set_latency_lane): requests marked lane = 1 run
+//     only on the last workers, whose streams have the highest priority;
 //   * completion: beta^2 (and the transformer boost) are copied to the caller's
 //     buffers, then the status becomes final; bf_poll / bf_wait report it.
 #include <algorithm>
@@ -174,7 +174,9 @@ Batch pick(bf_server* S, int w) {
   const size_t normal_cap = S->n_lane ? S->budget - S->budget / 8 : S->budget;
   for (size_t qi = 0; qi < S->queue.size(); ++qi) {
     Req* R = S->queue[qi];
-    if (lane_worker && R->r.lane == 0) continue;
+    // the lane's requests run only on its high-priority streams, the others
+    // only on the normal workers
+    if (lane_worker != (S->n_lane && R->r.lane == 1)) continue;
     StackInfo& si = S->stacks[R->r.stack];
     if (si.busy || bound_elsewhere(si, R, w)) continue;
     const size_t cap = R->r.lane ? S->budget : normal_cap;
@@ -210,7 +212,7 @@ Batch pick(bf_server* S, int w) {
       for (size_t qk = 0; qk < S->queue.size(); ++qk) first.emplace(S->queue[qk]->r.stack, qk);
       for (size_t qj = qi + 1; qj < S->queue.size() && (int)b.reqs.size() < kMaxGroup; ++qj) {
         Req* Q = S->queue[qj];
-        if (!groupable(S, R, Q) || (lane_worker && Q->r.lane == 0)) continue;
+        if (!groupable(S, R, Q) || Q->r.lane != R->r.lane) continue;
         bool dup = false;
         for (Req* G : b.reqs) dup |= G->r.stack == Q->r.stack;
         if (dup) continue;
@@ -455,6 +457,18 @@ extern "C" int bf_server_create(int device, unsigned long long hbm_budget_bytes,
         return rc;
       }
       S->hs.push_back(h);
+    }
+    if (flags & BF_SERVER_RESERVE_HBM) {
+      // the pool is grown once here instead of by the first large solves, whose
+      // mapping of new memory would stall the other workers' allocations
+      size_t fr = 0, tot = 0;
+      if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        fr = 0;
+      }
+      const size_t margin = 2ull << 30;
+      const size_t want = std::min<size_t>(S->budget, fr > margin ? fr - margin : 0);
+      if (want && bf_pool_reserve(S->hs[0], want) != BF_OK) S->err = "HBM reservation failed; the pool grows on demand";
     }
   } else if (!S->budget) {
     S->budget = ~0ull;

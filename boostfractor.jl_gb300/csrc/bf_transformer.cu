@@ -2311,7 +2311,9 @@ extern "C" int bf_modes2field(bf_handle* h, const bf_modes* m, const double* coe
 // After a solve with the tensor-core GEMMs has synchronised: their error flag.
 static int tc_status(bf_handle* h) {
   int e = 0;
-  TCK(cudaMemcpy(&e, reinterpret_cast<int*>(h->d_scalar + 2), sizeof(int), cudaMemcpyDeviceToHost));
+  TCK(cudaMemcpyAsync(&e, reinterpret_cast<int*>(h->d_scalar + 2), sizeof(int), cudaMemcpyDeviceToHost,
+                      h->stream()));
+  TCK(cudaStreamSynchronize(h->stream()));
   if (e) return bf_fail(h, BF_ERR_TIMEOUT, "tensor-core GEMM: a bounded wait expired (stage " + std::to_string(e) + ")");
   return BF_OK;
 }

@@ -393,6 +393,10 @@ typedef struct bf_server bf_server;
                                     "runs" for nmax microseconds and occupies
                                     footprint_bytes; for testing the scheduler
                                     on machines without a GPU */
+#define BF_SERVER_RESERVE_HBM 2  /* map the admission budget (at most the
+                                    free memory less 2 GB) into the device's
+                                    memory pool at creation, so that no solve
+                                    has to grow the pool while others run */
 
 typedef struct bf_request {
   int solver;                  /* BF_SOLVER_* */
@@ -418,15 +422,15 @@ int bf_server_create(int device, unsigned long long hbm_budget_bytes, int n_work
 /* Cancels queued requests (status BF_ERR_INVALID), waits for running ones,
  * releases the workspaces grown on served stacks and the workers. */
 int bf_server_destroy(bf_server* s);
-/* No counterpart in the reference.  Reserves the last n_lane workers (at
- * least one worker stays normal) for requests with lane = 1, on streams of
- * the device's highest priority, so that short interactive requests (an
- * optimiser's steps) are not queued behind long ones and their kernels are
- * scheduled ahead of those of the other workers; the persistent tensor-core
- * GEMM of the normal workers then leaves the lane's share of the SMs
- * (n_lane / n_workers) free, and normal requests are admitted within 7/8 of
- * the HBM budget (the last eighth is the lane's).  Normal workers still take
- * lane-1 requests when idle.  Call once, before the first bf_submit. */
+/* No counterpart in the reference.  Requests with lane = 1 run only on the
+ * last n_lane workers (at least one worker stays normal), on streams of the
+ * device's highest priority, and the other requests only on the normal
+ * workers: short interactive requests (an optimiser's steps) are not queued
+ * behind long ones and their kernels are scheduled ahead of the others'.
+ * The normal workers' persistent tensor-core GEMM leaves the lane's share of
+ * the SMs (n_lane / n_workers) free, and normal requests are admitted within
+ * 7/8 of the HBM budget (the last eighth is the lane's).  Call once, before
+ * the first bf_submit. */
 int bf_server_set_latency_lane(bf_server* s, int n_lane);
 int bf_submit(bf_server* s, const bf_request* req, unsigned long long* id);
 /* Non-blocking: *status = BF_PENDING, or the request's final status (BF_OK or

@@ -200,7 +200,8 @@ def test_reset_stats_starts_a_new_window(B):
 def test_latency_lane_workers_take_only_lane_requests(B):
     """With one of two workers reserved for lane 1, a second long normal
     request waits for the first (the lane worker does not take it), while a
-    lane-1 request starts at once on the reserved worker."""
+    lane-1 request starts at once on the reserved worker; a second lane-1
+    request waits for the lane worker even while the normal worker is idle."""
     srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
     try:
         srv.set_latency_lane(1)
@@ -213,6 +214,11 @@ def test_latency_lane_workers_take_only_lane_requests(B):
         rf, r1, r2 = (srv.wait(i, timeout_ms=20000) for i in (fast, first, second))
         assert r2["t_start"] >= r1["t_done"]
         assert rf["t_done"] < r1["t_done"]
+        # the normal worker is idle now; two lane requests run one after the other
+        l1 = srv.submit(0xF030, [1e10], nmax=50000, footprint_bytes=MB, lane=1)
+        l2 = srv.submit(0xF040, [1e10], nmax=50000, footprint_bytes=MB, lane=1)
+        a1, a2 = srv.wait(l1, timeout_ms=20000), srv.wait(l2, timeout_ms=20000)
+        assert a2["t_start"] >= a1["t_done"]
     finally:
         srv.close()
 
