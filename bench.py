@@ -1259,7 +1259,7 @@ def main():
     ap.add_argument("--workers", type=int, default=4, help="serving engine worker streams")
     ap.add_argument("--lane-workers", type=int, default=3,
                     help="serve: workers reserved, on high-priority streams, for the interactive clients")
-    ap.add_argument("--bg-rate", type=float, default=1.0,
+    ap.add_argument("--bg-rate", type=float, default=0.5,
                     help="serve: arrivals per second of the uneven-batch background clients")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--rate", type=float, default=2000.0, help="serving: mean Poisson arrival rate, requests/s")
