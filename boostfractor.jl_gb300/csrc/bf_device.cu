@@ -662,7 +662,10 @@ __global__ void __launch_bounds__(THREADS, MINB) k_fused_stage(FusedArgs<cplx_t<
     fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sa, sd.exitA, M, scr, tw, team, g);
     fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.ra), M, scr, tw, team, g);
     fused_phase3<C, N, false, NZ, NTEAM, HALF>(a, sd, f, sd.ra, false, M, scr, obuf, tw, team, g);
-    __syncthreads();
+    // no barrier: B's forward row pass writes row y of M through the same
+    // team (y mod NTEAM) and the same per-thread elements that A's inverse row
+    // pass just read from it, and A~ goes to global memory, read back in B's
+    // mix by the same thread; program order already orders every access
     fused_phase1<C, N, NZ, NTEAM, HALF>(a, f, sd.sb, sd.exitB, M, scr, tw, team, g);
     fused_phase2<C, N, NZ, NTEAM, HALF, STAGE>(a, qptr(sd.rb), M, scr, tw, team, g);
     fused_phase3<C, N, true, NZ, NTEAM, HALF>(a, sd, f, sd.rb, true, M, scr, obuf, tw, team, g);
