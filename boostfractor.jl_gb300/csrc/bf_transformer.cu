@@ -1094,7 +1094,8 @@ __device__ __forceinline__ DFc dfc_add(DFc x, DFc y) {
 
 __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2* Pinv, const ChainRegion* cr,
                                                   int nd, int nm, const double2* emit, DFc* T21g, DFc* T22g,
-                                                  double2* axg, double2* T21out, double2* T22out, int par_axion) {
+                                                  double2* axg, double2* T21out, double2* T22out, int par_axion,
+                                                  DFc* Wg) {
   extern __shared__ __align__(16) unsigned char sm[];
   const int n2 = nm * nm;
   DFc* U = reinterpret_cast<DFc*>(sm);
@@ -1108,10 +1109,11 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
   // the axion sum reads a row of T per step, one dependent load per entry
   DFc* T21 = T21g ? T21g + (size_t)f * n2 : em + nm;
   DFc* T22 = T21g ? T22g + (size_t)f * n2 : em + nm + n2;
-  // par_axion (T in shared memory and room for one more matrix): the axion
+  // par_axion (T in shared memory and room for one more matrix), or Wg (T in
+  // global memory, a global scratch of one matrix per frequency): the axion
   // terms of all (m, k) are formed in parallel into Wt, then each row is
   // summed in k order as the serial form does (same values, shorter chain)
-  DFc* Wt = par_axion ? em + nm + 2 * n2 : nullptr;
+  DFc* Wt = par_axion ? em + nm + 2 * n2 : (Wg ? Wg + (size_t)f * n2 : nullptr);
   const DFc zero = {0.f, 0.f, 0.f, 0.f}, one = {1.f, 0.f, 0.f, 0.f};
   for (int e = tid; e < n2; e += nt) {
     T21[e] = zero;
@@ -1172,6 +1174,7 @@ __global__ void __launch_bounds__(1024) k_chain_df(const float2* P, const float2
     if (Wt)   // reads only Wt: runs alongside the product below, which rewrites T
       for (int m = tid; m < nm; m += nt) {
         DFc acc = zero;
+#pragma unroll 8
         for (int k = 0; k < nm; ++k) acc = dfc_add(acc, Wt[m * nm + k]);
         const double2 v = dfc_to_d(acc);
         ax[m] = bf::cadd(ax[m], bf::cmul(g.S, v));
@@ -2593,7 +2596,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
                                        T21.as<D2>(), T22.as<D2>(), ax.as<double2>());
     TCK(cudaGetLastError());
   } else {
-    DBuf T21df, T22df;
+    DBuf T21df, T22df, Wdf;
     size_t smem = (sizeof(DFc) * 2 + sizeof(float2) * 2) * nm * nm + (sizeof(double2) + sizeof(DFc)) * nm;
     const bool t_in_smem = smem + sizeof(DFc) * 2 * nm * nm <= 160 * 1024;
     const bool par_axion = t_in_smem && smem + sizeof(DFc) * 3 * nm * nm <= 160 * 1024;
@@ -2602,6 +2605,10 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     } else {
       TCKS(T21df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
       TCKS(T22df.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
+      // the axion terms go to global scratch, so that their row sums (in k
+      // order) are a short chain beside the products instead of a long one
+      // before them
+      TCKS(Wdf.alloc(h, sizeof(DFc) * (size_t)nf * nm * nm));
     }
     TCK(cudaFuncSetAttribute(k_chain_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxDynSmem));
     bf::note_launch();
@@ -2612,7 +2619,7 @@ static int tf_run_t(bf_handle* h, bf_stack* s, bf_modes* md, int nf, const doubl
     k_chain_df<<<nf, nthr, smem, st>>>(Pd, Pinv.as<D2>(), d_cr.as<ChainRegion>(), nd, nm, d_em.as<double2>(),
                                       t_in_smem ? nullptr : T21df.as<DFc>(), t_in_smem ? nullptr : T22df.as<DFc>(),
                                       ax.as<double2>(), T21.as<double2>(),
-                                      T22.as<double2>(), par_axion ? 1 : 0);
+                                      T22.as<double2>(), par_axion ? 1 : 0, t_in_smem ? nullptr : Wdf.as<DFc>());
     TCK(cudaGetLastError());
   }
   if (reflect) {
