@@ -1300,24 +1300,38 @@ __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22
   }
   __syncthreads();
   // Gaussian elimination with partial pivoting (LAPACK getrf/getrs order)
+  const int lane = tid & 31, wid = tid >> 5, nwarp = nt >> 5;
   for (int c = 0; c < nm; ++c) {
+    // pivot: the largest |A[r][c]|^2 below the diagonal, the lowest row on
+    // ties (a warp's candidates by shuffles, then the warps' in warp 0)
     double best = -1.0;
     int bi = c;
     for (int r = c + tid; r < nm; r += nt) {
       const double v = A[r * w + c].x * A[r * w + c].x + A[r * w + c].y * A[r * w + c].y;
       if (v > best) { best = v; bi = r; }
     }
-    red_v[tid] = best;
-    red_i[tid] = bi;
-    __syncthreads();
-    for (int s = nt / 2; s > 0; s >>= 1) {
-      if (tid < s && (red_v[tid + s] > red_v[tid] || (red_v[tid + s] == red_v[tid] && red_i[tid + s] < red_i[tid]))) {
-        red_v[tid] = red_v[tid + s];
-        red_i[tid] = red_i[tid + s];
-      }
-      __syncthreads();
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
     }
-    const int p = red_i[0];
+    if (lane == 0) {
+      red_v[wid] = best;
+      red_i[wid] = bi;
+    }
+    __syncthreads();
+    if (wid == 0) {
+      best = lane < nwarp ? red_v[lane] : -1.0;
+      bi = lane < nwarp ? red_i[lane] : nm;
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
+      }
+      if (lane == 0) red_i[nwarp] = bi;
+    }
+    __syncthreads();
+    const int p = red_i[nwarp];
     if (p != c)
       for (int k = tid; k < w; k += nt) {
         double2 t = A[c * w + k];
@@ -1327,13 +1341,17 @@ __global__ void __launch_bounds__(256) k_final_solve(const C* T21g, const C* T22
     __syncthreads();
     const double2 piv = A[c * w + c];
     if (tid == 0 && piv.x == 0.0 && piv.y == 0.0) atomicMin(sing, f);   // T22 exactly singular
-    for (int e = tid; e < (nm - c - 1) * (w - c); e += nt) {
-      const int r = c + 1 + e / (w - c), k = c + e % (w - c);
-      if (k == c) continue;
-      const double d = piv.x * piv.x + piv.y * piv.y;
+    // the multipliers l / piv, once per row (two FP64 divisions each), into
+    // column c, which is cleared below
+    const double d = piv.x * piv.x + piv.y * piv.y;
+    for (int r = c + 1 + tid; r < nm; r += nt) {
       const double2 l = A[r * w + c];
-      const double2 fac = make_double2((l.x * piv.x + l.y * piv.y) / d, (l.y * piv.x - l.x * piv.y) / d);
-      A[r * w + k] = bf::csub(A[r * w + k], bf::cmul(fac, A[c * w + k]));
+      A[r * w + c] = make_double2((l.x * piv.x + l.y * piv.y) / d, (l.y * piv.x - l.x * piv.y) / d);
+    }
+    __syncthreads();
+    for (int e = tid; e < (nm - c - 1) * (w - c - 1); e += nt) {
+      const int r = c + 1 + e / (w - c - 1), k = c + 1 + e % (w - c - 1);
+      A[r * w + k] = bf::csub(A[r * w + k], bf::cmul(A[r * w + c], A[c * w + k]));
     }
     __syncthreads();
     for (int r = c + 1 + tid; r < nm; r += nt) A[r * w + c] = make_double2(0.0, 0.0);
