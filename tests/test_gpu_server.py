@@ -90,6 +90,40 @@ def test_results_alone_and_in_the_mix(B):
         h.close()
 
 
+def test_latency_lane_results_equal_alone(B):
+    """With a latency lane (one of three workers, high-priority stream) and
+    the budget mapped into the pool at creation, transformer steps in the lane
+    and bounce-loop solves on the normal workers (whose persistent GEMM is
+    capped) give the same beta^2 as alone."""
+    h = B.Handle(0)
+    s_cheer, _, _ = stack(B, h, 64, 3, 11)
+    s_tf, c_tf, _ = stack(B, h, 48, 2, 13)
+    modes = B.SeedModes(c_tf, ThreeDim=True, Mmax=4, Lmax=1, diskR=0.15, handle=h)
+    fa = np.linspace(19.6e9, 20.4e9, 24)
+    fc = np.linspace(19.5e9, 20.5e9, 9)
+    alone = {"cheer": s_cheer.cheerleader(fa, nmax=40, precision="mixed")[2],
+             "tf_mixed": transformer_alone(B, h, s_tf, modes, fc, "mixed"),
+             "tf_fp64": transformer_alone(B, h, s_tf, modes, fc, "fp64")}
+    srv = B.Server(hbm_budget_bytes=8 << 30, n_workers=3, reserve_hbm=True)
+    try:
+        srv.set_latency_lane(1)
+        ids = []
+        for rep in range(3):
+            ids.append(("cheer", srv.submit(s_cheer, fa, "cheerleader", nmax=40, precision="mixed")))
+            ids.append(("tf_mixed", srv.submit(s_tf, fc, "transformer", modes=modes, precision="mixed", lane=1)))
+            ids.append(("tf_fp64", srv.submit(s_tf, fc, "transformer", modes=modes, precision="fp64", lane=1)))
+        for key, rid in ids:
+            r = srv.wait(rid, timeout_ms=120000)
+            assert rel(r["beta2"], alone[key]) < TOL, key
+        assert srv.stats()["failed"] == 0
+    finally:
+        srv.close()
+        modes.close()
+        for s in (s_cheer, s_tf):
+            s.close()
+        h.close()
+
+
 def test_optimiser_gap_steps_in_submission_order(B):
     """A client moves the disks every step (bf_request.distance): the queued
     steps run in order on the resident stack and match set_distance + solve."""
