@@ -539,8 +539,10 @@ size_t bf_solve_bytes_estimate(const bf_stack* s, int solver, int nf, int nm, in
   if (prop_kind == BF_PROP_1D) return F * (16 * 4 * nd * npix + 64);
   const size_t slots = 2 * nd + 2;
   // split-phase row tiles: at most (SMs = 160 here, an upper bound) step x
-  // frequency pairs of two nby x (N + 2) tiles
-  const size_t split = 160 * 2 * (size_t)s->nby * (s->nx + 2) * csz;
+  // frequency pairs of two nby x (N + 2) tiles, or every step's when no stage
+  // fits the fused kernel's shared memory
+  const bool split_only = bf::fused_split_only(s->nx, s->nbx, s->nby, precision == BF_PREC_FP64);
+  const size_t split = (split_only ? nd * F : 160) * 2 * (size_t)s->nby * (s->nx + 2) * csz;
   const size_t fused = F * (csz * (slots * plane + nd * npix + nd * plane) + 16 * (2 * plane + 3 * npix)) + split;
   const size_t full = F * (csz * (slots + 1) * npix + 16 * 3 * npix);
   return std::max(fused, full) + F * 64;
@@ -1221,8 +1223,9 @@ static int run_fused(bf_handle* h, bf_stack* s, const std::string& key,
   // frequencies than SMs: short stacks, few frequencies, the wavefront's ends)
   {
     size_t split_len = 0;
+    const bool split_only = bf::fused_split_only(N, s->nbx, s->nby, fp64);
     for (size_t len : w.stage_len)
-      if (bf::split_stage((int)len, nf)) split_len = std::max(split_len, len);
+      if (split_only || bf::split_stage((int)len, nf)) split_len = std::max(split_len, len);
     a.mg = nullptr;
     if (split_len && N >= 64) {
       CKS(w.mg.ensure(h, bf::split_tile_bytes(N, s->nby, nf, (int)split_len, fp64)));

@@ -796,10 +796,16 @@ size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64) {
   return smem_for(N, nby, fp64 ? 16 : 8);
 }
 
+bool fused_split_only(int N, int nbx, int nby, bool fp64) {
+  return N >= 64 && fused_smem_bytes(N, nbx, nby, fp64) > kMaxSmem;
+}
+
 bool fused_supported(int N, int nbx, int nby, bool fp64) {
   if (N < 8 || N > 256 || (N & (N - 1))) return false;
   if (nbx < 1 || nby < 1 || nbx > N || nby > N) return false;
-  return fused_smem_bytes(N, nbx, nby, fp64) <= kMaxSmem;
+  // row tiles too large for shared memory (complex128 at 256^2): every stage
+  // takes the split-phase path, whose tiles live in global memory
+  return fused_smem_bytes(N, nbx, nby, fp64) <= kMaxSmem || fused_split_only(N, nbx, nby, fp64);
 }
 
 // Shared memory of one SM (bytes) and what the driver reserves per CTA.
@@ -902,10 +908,11 @@ static int launch_fused_t(const FusedArgs<cplx_t<R>>& a, int nsteps, cudaStream_
   const size_t csz = sizeof(cplx_t<R>);
   const FusedShape sh = fused_shape<N>(a.nby, csz);
   const size_t smem = sh.smem, smem_j = sh.smem_j;
-  if (smem > kMaxSmem) return (int)cudaErrorInvalidValue;
+  const bool split_only = smem > kMaxSmem;   // every stage in global-memory row tiles
+  if (split_only && !(a.mg && N >= 64)) return (int)cudaErrorInvalidValue;
   constexpr int G = Team<N>::G, RR = Team<N>::RR;
   const int rv = (std::max(a.nbx, a.nby) + G - 1) / G;
-  if (a.mg && split_stage(nsteps, a.nfreq) && N >= 64) {
+  if (a.mg && N >= 64 && (split_only || split_stage(nsteps, a.nfreq))) {
     if constexpr ((sizeof(R) == 4 && N >= 64) || (sizeof(R) == 8 && (N == 64 || N == 128)))
       if (rv <= pruned_slots<N>()) return launch_split<R, N, pruned_slots<N>()>(a, nsteps, st);
     return launch_split<R, N, RR>(a, nsteps, st);

@@ -71,6 +71,9 @@ std::vector<int> fused_variants(int N, int nbx, int nby, bool fp64);
 int launch_fused_stage_f(int N, const FusedArgs<float2>& a, int nsteps, cudaStream_t st);
 int launch_fused_stage_d(int N, const FusedArgs<double2>& a, int nsteps, cudaStream_t st);
 size_t fused_smem_bytes(int N, int nbx, int nby, bool fp64);
+// True when the fused kernel's row tiles do not fit in shared memory, so that
+// every stage runs the split-phase kernels (tiles in global memory).
+bool fused_split_only(int N, int nbx, int nby, bool fp64);
 bool fused_supported(int N, int nbx, int nby, bool fp64);
 // Split-phase path (stages with fewer steps x frequencies than SMs): the row
 // tiles it needs for a stage of nsteps steps, and whether a stage takes it.
