@@ -730,20 +730,43 @@ def transformer_1d_batch(distances, eps, freqs, emit=None, handle=None):
     return boost, beta2
 
 
+def _shift_gaps(bdry, spacing=0.0, tilt_x=0.0, tilt_y=0.0):
+    """A copy of bdry whose air gaps (the reference's regions 2, 4, ..., n_region)
+    are `spacing` longer and tilted by (tilt_x, tilt_y) more
+    (examples/transformer_optim_utilities.jl:22-24, 40-43)."""
+    b = SetupBoundaries(bdry.distance, bdry.r, bdry.eps, bdry.relative_tilt_x, bdry.relative_tilt_y,
+                        bdry.relative_surfaces)
+    b.distance[1::2] += spacing
+    b.relative_tilt_x[1::2] += tilt_x
+    b.relative_tilt_y[1::2] += tilt_y
+    return b
+
+
 class PGrid:
     """Propagation matrices on a grid of gap spacings, resident on the device,
     with spline interpolation (examples/transformer_optim_utilities.jl:11-91).
-    spacing_grid is an evenly spaced sequence (the reference's range)."""
+    spacing_grid is an evenly spaced sequence (the reference's range).  With
+    tilt grids the interpolation runs at their first points, as the
+    reference's interpolate_prop_matrix does (itp(r, f, shift, 1, 1, ...));
+    array() gives the whole (region, frequency, spacing, tilt_x, tilt_y,
+    mode, mode) array of calc_propagation_matrices_grid."""
 
     def __init__(self, bdry, coords, modes, frequencies, spacing_grid, prop=propagator, diskR=0.15,
-                 precision="fp64"):
+                 precision="fp64", tilt_x_grid=0.0, tilt_y_grid=0.0):
         sg = np.asarray(spacing_grid, dtype=np.float64)
         if sg.ndim != 1 or len(sg) < 2 or not np.allclose(np.diff(sg), sg[1] - sg[0], rtol=1e-9, atol=0):
             raise ValueError("spacing_grid must be an evenly spaced sequence of at least 2 values")
+        self.tilt_x_grid = np.atleast_1d(np.asarray(tilt_x_grid, dtype=np.float64))
+        self.tilt_y_grid = np.atleast_1d(np.asarray(tilt_y_grid, dtype=np.float64))
+        self.spacing_grid = sg
+        self._source = (bdry, coords, prop, diskR, precision)
         self.h = modes.h
         self.modes = modes
         self.freqs = np.ascontiguousarray(np.atleast_1d(frequencies), dtype=np.float64)
-        self.stack = Stack(bdry, coords, diskR, handle=self.h)
+        base = bdry
+        if self.tilt_x_grid[0] != 0.0 or self.tilt_y_grid[0] != 0.0:
+            base = _shift_gaps(bdry, 0.0, self.tilt_x_grid[0], self.tilt_y_grid[0])
+        self.stack = Stack(base, coords, diskR, handle=self.h)
         self.nd, self.nm = self.stack.nd, modes.nm
         self.spacing_first, self.spacing_step = float(sg[0]), float(sg[1] - sg[0])
         self.spacing_last = self.spacing_first + (len(sg) - 1) * self.spacing_step
@@ -770,6 +793,22 @@ class PGrid:
                                                      _lib.ptr(None if eb is None else eb.view(np.float64)),
                                                      _lib.ptr(boost.view(np.float64)), _lib.ptr(beta2)))
         return boost, beta2
+
+    def array(self):
+        """calc_propagation_matrices_grid's array [region, frequency, spacing,
+        tilt_x, tilt_y, mode, mode]: the matrices of every grid point, the air
+        gaps at their shifted spacing and tilts (computed on the device, one
+        geometry at a time)."""
+        bdry, coords, prop, diskR, precision = self._source
+        out = np.empty((self.nd, len(self.freqs), len(self.spacing_grid), len(self.tilt_x_grid),
+                        len(self.tilt_y_grid), self.nm, self.nm), dtype=np.complex128)
+        for si, sp in enumerate(self.spacing_grid):
+            for a, tx in enumerate(self.tilt_x_grid):
+                for b, ty in enumerate(self.tilt_y_grid):
+                    m = calc_propagation_matrices(_shift_gaps(bdry, sp, tx, ty), coords, self.modes, f=self.freqs,
+                                                  prop=prop, diskR=diskR, precision=precision)
+                    out[:, :, si, a, b] = m.transpose(1, 0, 2, 3)
+        return out
 
     @property
     def bounds(self):
@@ -801,12 +840,13 @@ _SOLVERS = {"cheerleader": _lib.BF_SOLVER_CHEERLEADER, "dancer": _lib.BF_SOLVER_
             "transformer": _lib.BF_SOLVER_TRANSFORMER, "pgrid": _lib.BF_SOLVER_PGRID}
 
 
-def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, prop=propagator, diskR=0.15,
-                                   precision="fp64"):
-    """examples/transformer_optim_utilities.jl:10-50 (without tilt grids): the
-    grid of propagation matrices over gap spacings x frequencies, kept on the
-    device as a PGrid instead of a 7-D host array."""
-    return PGrid(sbdry, coords, modes, frequencies, spacing_grid, prop=prop, diskR=diskR, precision=precision)
+def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, tilt_x_grid=0, tilt_y_grid=0,
+                                   prop=propagator, diskR=0.15, precision="fp64"):
+    """examples/transformer_optim_utilities.jl:10-50: the grid of propagation
+    matrices over gap spacings (and gap tilts) x frequencies, kept on the
+    device as a PGrid; PGrid.array() gives the reference's 7-D array."""
+    return PGrid(sbdry, coords, modes, frequencies, spacing_grid, prop=prop, diskR=diskR, precision=precision,
+                 tilt_x_grid=tilt_x_grid, tilt_y_grid=tilt_y_grid)
 
 
 def construct_prop_matrix_interpolation(prop_matrix_grid, spacing_grid=None):

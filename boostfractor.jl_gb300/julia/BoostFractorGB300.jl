@@ -247,19 +247,35 @@ function release(g::PGrid)
     return nothing
 end
 
+# a copy of sbdry whose air gaps (regions 2:2:n_region) are tilted by (tx, ty) more
+function tilt_gaps(sbdry::SetupBoundaries, tx, ty)
+    gx = Float64.(collect(sbdry.relative_tilt_x))
+    gy = Float64.(collect(sbdry.relative_tilt_y))
+    gx[2:2:end] .+= tx
+    gy[2:2:end] .+= ty
+    return SetupBoundaries(copy(sbdry.distance), copy(sbdry.r), copy(sbdry.eps), gx, gy,
+                           copy(sbdry.relative_surfaces))
+end
+
 """
     calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies;
-                                   prop=propagator, diskR=0.15, precision=:fp64)
+                                   tilt_x_grid=0, tilt_y_grid=0, prop=propagator, diskR=0.15,
+                                   precision=:fp64)
 
-examples/transformer_optim_utilities.jl:10 (without tilt grids) on the GPU.
-Returns a PGrid, which is also the interpolation object.
+examples/transformer_optim_utilities.jl:10 on the GPU.  Returns a PGrid, which
+is also the interpolation object.  With tilt grids the grid is built with the
+gaps at their first tilt points, the only ones the reference's
+interpolate_prop_matrix reads (itp(r, f, shift, 1, 1, ...)); the Python mirror's
+PGrid.array() gives the whole 7-D array.
 """
 function calc_propagation_matrices_grid(sbdry::SetupBoundaries, coords::CoordinateSystem, modes::Modes,
-                                        spacing_grid::AbstractRange, frequencies; prop=propagator, diskR=0.15,
-                                        precision=:fp64, handle=default_handle())
+                                        spacing_grid::AbstractRange, frequencies; tilt_x_grid=0, tilt_y_grid=0,
+                                        prop=propagator, diskR=0.15, precision=:fp64, handle=default_handle())
     freqs = Float64.(collect(frequencies))
+    tx, ty = first(tilt_x_grid), first(tilt_y_grid)
+    bd = (tx == 0 && ty == 0) ? sbdry : tilt_gaps(sbdry, tx, ty)
     m = modes_create(handle, coords, modes, diskR)
-    s = stack(handle, sbdry, coords, diskR)
+    s = stack(handle, bd, coords, diskR)
     ref = Ref{Ptr{Cvoid}}(C_NULL)
     rc = ccall((:bf_pgrid_create, lib), Cint,
         (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Float64, Float64, Cint, Cint,

@@ -678,32 +678,44 @@ def unnormalized_match(Eout, Eantenna, dx=0.01, dy=0.01):
 # --------------------------------------------------------------------------
 # Optimiser utilities (examples/transformer_optim_utilities.jl)
 # --------------------------------------------------------------------------
-def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, prop=propagator, diskR=0.15):
-    """examples/transformer_optim_utilities.jl:10-50, without tilt grids.
+def calc_propagation_matrices_grid(sbdry, coords, modes, spacing_grid, frequencies, prop=propagator, diskR=0.15,
+                                   tilt_x_grid=None, tilt_y_grid=None):
+    """examples/transformer_optim_utilities.jl:10-50.
 
-    Returns [region, frequency, spacing, nm, nm].  The gaps are the regions
-    1, 3, ..., nd-1 (0-based; the reference's ind_gap = 2:2:n_region, the
-    exit region included) and move by spacing_grid[s]; the mirror and the
-    disks (ind_solid) are computed once per frequency.  The reference splits
-    the setup into a gap setup and a solid setup; a region's matrix depends
-    only on that region's parameters, so shifting the gaps of one copy of the
-    setup gives the same matrices.
+    Returns [region, frequency, spacing, nm, nm], or with tilt grids the
+    reference's [region, frequency, spacing, tilt_x, tilt_y, nm, nm].  The
+    gaps are the regions 1, 3, ..., nd-1 (0-based; the reference's ind_gap =
+    2:2:n_region, the exit region included); they move by spacing_grid[s] and
+    tilt by tilt_x_grid[tx], tilt_y_grid[ty] on top of their own tilts
+    (:40-43); the mirror and the disks (ind_solid) are computed once per
+    frequency.  The reference splits the setup into a gap setup and a solid
+    setup; a region's matrix depends only on that region's parameters, so
+    shifting the gaps of one copy of the setup gives the same matrices.
     """
     nd = len(sbdry.distance)
     gaps = np.arange(1, nd, 2)
     nm = modes.M * (2 * modes.L + 1)
     sg = np.asarray(spacing_grid, dtype=float)
-    out = np.empty((nd, len(frequencies), len(sg), nm, nm), dtype=complex)
+    tilts = tilt_x_grid is not None or tilt_y_grid is not None
+    txg = np.atleast_1d(np.asarray(0.0 if tilt_x_grid is None else tilt_x_grid, dtype=float))
+    tyg = np.atleast_1d(np.asarray(0.0 if tilt_y_grid is None else tilt_y_grid, dtype=float))
+    out = np.empty((nd, len(frequencies), len(sg), len(txg), len(tyg), nm, nm), dtype=complex)
     for f, fr in enumerate(frequencies):
         solid = calc_propagation_matrices(sbdry, coords, modes, f=fr, prop=prop, diskR=diskR)
         for s, sp in enumerate(sg):
-            sb = copy.deepcopy(sbdry)
-            sb.distance = np.array(sbdry.distance, dtype=float)
-            sb.distance[gaps] += sp
-            pm = calc_propagation_matrices(sb, coords, modes, f=fr, prop=prop, diskR=diskR)
-            for r in range(nd):
-                out[r, f, s] = pm[r] if r % 2 == 1 else solid[r]
-    return out
+            for a, tx in enumerate(txg):
+                for b, ty in enumerate(tyg):
+                    sb = copy.deepcopy(sbdry)
+                    sb.distance = np.array(sbdry.distance, dtype=float)
+                    sb.distance[gaps] += sp
+                    sb.relative_tilt_x = np.array(sbdry.relative_tilt_x, dtype=float)
+                    sb.relative_tilt_y = np.array(sbdry.relative_tilt_y, dtype=float)
+                    sb.relative_tilt_x[gaps] += tx
+                    sb.relative_tilt_y[gaps] += ty
+                    pm = calc_propagation_matrices(sb, coords, modes, f=fr, prop=prop, diskR=diskR)
+                    for r in range(nd):
+                        out[r, f, s, a, b] = pm[r] if r % 2 == 1 else solid[r]
+    return out if tilts else out[:, :, :, 0, 0]
 
 
 class SpacingSpline:

@@ -210,3 +210,33 @@ def test_optimiser_utility_mirrors_vs_oracle(B):
         assert rel(E, Eo) < 1e-10
     finally:
         itp.close()
+
+
+def test_pgrid_tilt_grids_vs_oracle(B):
+    """calc_propagation_matrices_grid with tilt grids: the whole (region,
+    frequency, spacing, tilt_x, tilt_y) array against the oracle's, and the
+    interpolation at the tilt grids' first points, as the reference's
+    interpolate_prop_matrix evaluates it (itp(r, f, shift, 1, 1, ...))."""
+    kw, cb, co, mb, mo, grid, freqs = setup(B)
+    grid = grid[::2]
+    txg, tyg = np.array([1e-4, -2e-4]), np.array([0.0, 3e-4])
+    pg = B.calc_propagation_matrices_grid(B.SeedSetupBoundaries(cb, **kw), cb, mb, grid, freqs,
+                                          tilt_x_grid=txg, tilt_y_grid=tyg)
+    try:
+        nd = len(kw["distance"])
+        sb = O.seed_setup_boundaries(co, **kw)
+        ref = O.calc_propagation_matrices_grid(sb, co, mo, grid, freqs, tilt_x_grid=txg, tilt_y_grid=tyg)
+        got = pg.array()
+        assert got.shape == ref.shape
+        assert rel(got[1:], ref[1:]) < 1e-10   # the mirror (NaN permittivity) is not compared
+        ref0 = ref[:, :, :, 0, 0].copy()
+        ref0[0] = 0.0
+        itp = O.construct_prop_matrix_interpolation(ref0, grid)
+        shifts = [0.5 * (grid[0] + grid[1]), grid[2]]
+        m = pg.matrices(np.array(shifts))
+        want = O.interpolate_prop_matrix(itp, shifts)
+        for f in range(len(freqs)):
+            for j in range(1, nd):
+                assert rel(m[f, j], want[j][f]) < 1e-10, (f, j)
+    finally:
+        pg.close()
