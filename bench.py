@@ -631,7 +631,9 @@ def run_uneven(args):
     U{5..80}, grid {64,128,256}, U{64..1024} frequencies, half dancer / half
     transformer) solved through the serving engine (all requests submitted at
     once, 4 worker streams) and one after another on one handle ("plain");
-    each request's beta^2 must be the same both ways."""
+    each request's beta^2 must be the same both ways.  An untimed pass first
+    runs every bounce-loop request for a few bounces, so that the autotuner's
+    first-solve trials are paid by neither arm."""
     import torch
     torch.cuda.set_device(0)
     import build as _b
@@ -641,6 +643,14 @@ def run_uneven(args):
     reqs = W.config4_uneven()[:args.requests]
     h = B.Handle(0)
     mode_cache = {}   # requests on one grid with one mode set share a basis
+    # untimed: the autotuner's first-solve trials for every stage shape of the
+    # batch (a few bounces of each bounce-loop request), so that neither arm
+    # below pays them and neither reuses the other's
+    for r in reqs:
+        if r["solver"] != "transformer":
+            st, m = _build_request_stack(B, W, h, r, mode_cache)
+            _solve_plain(B, h, st, m, dict(r, nmax=min(r["nmax"], 3)))
+            st.close()
     # plain: one request after another on one handle; each stack is created
     # before and closed after its own (timed) solve, so that the workspaces of
     # hundreds of large stacks do not pile up on the device

@@ -960,17 +960,19 @@ static void prof_mark(bf_handle* h, int i) {
 // memory is allocated once the workspace has grown to the request's size.
 // ---------------------------------------------------------------------------
 // Autotuner.  The fused stage kernel has variants that give the same results
-// bit for bit (FusedVariant: joint or separate slot propagation, 256 or 512
-// threads); which is fastest depends on the grid, the box, the precision and
-// the frequency batch.  The first solve of a shape times every valid variant
-// on its largest fused stage, three launches each on scratch copies of the
-// state and the exit accumulators, and keeps the fastest for that shape on
-// that device.  Solves on a stream being captured, and any solve while
-// tuning is switched off (bf_autotune(0)), use the rule's choice.
+// bit for bit (FusedVariant: joint or separate slot propagation, 160 to 512
+// threads, 2 or 3 CTAs per SM, twiddles in registers or shared memory,
+// phasor rows from L2 or staged); which is fastest depends on the grid, the
+// box, the precision and the frequency batch.  The first solve of a shape
+// (the frequency count rounded up to a power of two) times every valid
+// variant on its largest fused stage, three launches each on scratch copies
+// of the state and the exit accumulators, and keeps the fastest for that
+// shape on that device.  Solves on a stream being captured, and any solve
+// while tuning is switched off (bf_autotune(0)), use the rule's choice.
 // ---------------------------------------------------------------------------
 namespace {
 std::mutex g_tune_mu;
-std::map<std::array<long long, 6>, int> g_fused_tuned;   // (device, N, nbx, nby, fp64, nf) -> variant
+std::map<std::array<long long, 6>, int> g_fused_tuned;   // (device, N, nbx, nby, fp64, nf bucket) -> variant
 std::vector<std::string> g_tune_log;
 std::atomic<int> g_autotune{1};
 std::atomic<int> g_force_variant{-1};
@@ -1008,7 +1010,11 @@ static int fused_autotune(bf_handle* h, const Workspace& w, const bf::FusedArgs<
     return BF_OK;
   }
   if (!g_autotune.load()) return BF_OK;
-  const std::array<long long, 6> key = {h->device, N, a.nbx, a.nby, (long long)fp64, a.nfreq};
+  // frequency counts share a decision within a power of two (a batch of
+  // requests of varying size, 64 .. 1024 frequencies, tunes a few times)
+  long long nfb = 1;
+  while (nfb < a.nfreq) nfb <<= 1;
+  const std::array<long long, 6> key = {h->device, N, a.nbx, a.nby, (long long)fp64, nfb};
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_fused_tuned.find(key);
