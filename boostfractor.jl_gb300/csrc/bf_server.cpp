@@ -160,9 +160,14 @@ bool mergeable(const Req* a, const Req* b) {
          a->r.beta2_scale == b->r.beta2_scale;
 }
 
-// Whether request R's stack holds workspace on a worker other than w.
-bool bound_elsewhere(const StackInfo& si, const Req* R, int w) {
-  return R->r.solver != BF_SOLVER_TRANSFORMER && si.home >= 0 && si.home != w;
+// Whether request R must wait for its stack's home worker (which holds the
+// stack's workspace) rather than run on worker w.  A home worker of the other
+// lane class cannot run R; the workspace then moves to w.
+bool bound_elsewhere(const bf_server* S, const StackInfo& si, const Req* R, int w) {
+  if (R->r.solver == BF_SOLVER_TRANSFORMER || si.home < 0 || si.home == w) return false;
+  const bool home_in_lane = si.home >= S->n_workers - S->n_lane;
+  const bool r_in_lane = S->n_lane && R->r.lane == 1;
+  return home_in_lane == r_in_lane;
 }
 
 // The next batch worker w may start, or an empty batch.  Caller holds the lock.
@@ -178,7 +183,7 @@ Batch pick(bf_server* S, int w) {
     // only on the normal workers
     if (lane_worker != (S->n_lane && R->r.lane == 1)) continue;
     StackInfo& si = S->stacks[R->r.stack];
-    if (si.busy || bound_elsewhere(si, R, w)) continue;
+    if (si.busy || bound_elsewhere(S, si, R, w)) continue;
     const size_t cap = R->r.lane ? S->budget : normal_cap;
     // the workspace the stack already holds is reused by the solve
     const size_t need = R->est > si.resident ? R->est - si.resident : 0;

@@ -252,3 +252,17 @@ def test_latency_lane_keeps_an_eighth_of_the_budget(B):
         assert ro["t_start"] >= rb["t_done"]
     finally:
         srv.close()
+
+
+def test_stack_changes_lane(B):
+    """A bounce-loop stack whose workspace lives on a normal worker runs a
+    lane-1 request on the lane worker (and back): a home worker of the other
+    lane class does not hold the request."""
+    srv = B.Server(hbm_budget_bytes=1 << 40, n_workers=2, dry_run=True)
+    try:
+        srv.set_latency_lane(1)
+        for lane in (0, 1, 0, 1):
+            r = srv.wait(srv.submit(0xF300, [1e10], nmax=1000, footprint_bytes=MB, lane=lane), timeout_ms=5000)
+            assert r["t_done"] >= r["t_start"]
+    finally:
+        srv.close()
