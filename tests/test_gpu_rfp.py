@@ -148,7 +148,7 @@ def test_cheerleader_fused_fp64_vs_oracle(B, n, ndisk, surfaces):
 
 
 def test_dancer_config1_fp64_vs_oracle(B):
-    """BASELINE config 1: dancer, mirror + 1 disk, 64x64, 20 GHz, 201 bounces, complex128."""
+    """Configuration 1: dancer, mirror + 1 disk, 64x64, 20 GHz, 201 bounces, complex128."""
     from bfgb300 import workloads as W
     w = W.config1_dancer()
     cb, co = coords_pair(B, w["X"])
